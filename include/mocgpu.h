@@ -1,0 +1,167 @@
+/*
+ * mocgpu: C ABI of the GB300 2-D MoC sweep and CMFD power iteration.
+ *
+ * Every entry point returns an int status (MOCGPU_OK on success). On failure
+ * mocgpu_last_error() returns a message for the calling thread. Pointer
+ * arguments are HOST pointers unless the name ends in _dev. Arrays follow
+ * MOCC's conventions: scalar flux is [n_fsr][n_group] row-major (MOCC's
+ * ArrayB2 flux_(n_reg, n_group)), pin-mesh arrays are in coarse-cell order
+ * (cell = iy * nx + ix, iy = 0 at the south face).
+ *
+ * Threading: a mocgpu_sweeper is bound to one CUDA stream and is not
+ * re-entrant; distinct handles may be driven from distinct host threads.
+ */
+#ifndef MOCGPU_H
+#define MOCGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MOCGPU_OK 0
+#define MOCGPU_ERR_ARG 1            /* invalid argument / unsupported option */
+#define MOCGPU_ERR_XML 2            /* malformed XML input */
+#define MOCGPU_ERR_IO 3             /* file could not be read */
+#define MOCGPU_ERR_XS 4             /* cross-section library problem */
+#define MOCGPU_ERR_GEOMETRY 5       /* invalid core geometry */
+#define MOCGPU_ERR_RAYS 6           /* ray tracing failure */
+#define MOCGPU_ERR_SOLVER 7         /* invalid solver options */
+#define MOCGPU_ERR_NONPOSITIVE 11   /* non-positive pin flux in set_pin_flux */
+#define MOCGPU_ERR_NAN 12           /* eigenvalue became NaN */
+#define MOCGPU_ERR_NOT_CONVERGED 13 /* iteration limit reached (result still valid) */
+#define MOCGPU_ERR_CUDA 20          /* CUDA runtime error (out of memory included) */
+#define MOCGPU_ERR_CAPACITY 21      /* serving admission: over the memory budget */
+#define MOCGPU_ERR_INTERNAL 99
+
+typedef struct mocgpu_problem mocgpu_problem; /* traced problem (host) */
+typedef struct mocgpu_sweeper mocgpu_sweeper; /* device-resident solve */
+
+/* sizes reported by mocgpu_problem_sizes(), in this order */
+enum {
+    MOCGPU_SZ_NGROUP = 0,
+    MOCGPU_SZ_NFSR,
+    MOCGPU_SZ_NMAT,
+    MOCGPU_SZ_NDIR_OCT,
+    MOCGPU_SZ_NANG,
+    MOCGPU_SZ_NSETS,
+    MOCGPU_SZ_POL_PER_SET,
+    MOCGPU_SZ_NX,
+    MOCGPU_SZ_NY,
+    MOCGPU_SZ_NPIN,
+    MOCGPU_SZ_NSURF,
+    MOCGPU_SZ_NFUEL,
+    MOCGPU_SZ_NTRACKS,
+    MOCGPU_SZ_NSEG,
+    MOCGPU_SZ_NCM,
+    MOCGPU_SZ_MAXSEG,
+    MOCGPU_SZ_COUNT
+};
+
+typedef struct mocgpu_options {
+    double k_tol, psi_tol;
+    int max_iter, min_iter;
+    int cmfd, cmfd_enabled;
+    double cmfd_k_tol, cmfd_psi_tol, cmfd_resid_reduction;
+    int cmfd_max_iter, cmfd_negative_fixup;
+    int n_inner, gs_boundary, precision;
+} mocgpu_options;
+
+typedef struct mocgpu_result {
+    double k;
+    int iterations;
+    int converged;
+    double error_k, error_psi;
+    double seconds;
+    int64_t sweeps;          /* one-group inner sweeps performed */
+    int64_t cmfd_iterations; /* CMFD power iterations performed */
+} mocgpu_result;
+
+/* ---- library ---------------------------------------------------------- */
+const char *mocgpu_last_error(void);
+int mocgpu_version(void);
+int mocgpu_device_count(int *n);
+
+/* ---- problem set-up (host only; replaces MOCC's input processing,
+ *      src/input_proc.cpp:164-213, CoreMesh + RayData construction,
+ *      src/core/core_mesh.cpp:36-260, src/sweepers/moc/ray_data.cpp:67-343)
+ * xsl_text, when non-NULL, replaces the file named by <material_lib path>.
+ * base_dir resolves a relative <material_lib path>. ------------------------ */
+int mocgpu_problem_create(const char *xml_text, const char *xsl_text, const char *base_dir, mocgpu_problem **out);
+void mocgpu_problem_destroy(mocgpu_problem *p);
+int mocgpu_problem_sizes(const mocgpu_problem *p, int64_t *sizes /* [MOCGPU_SZ_COUNT] */);
+int mocgpu_problem_options(const mocgpu_problem *p, mocgpu_options *out);
+int mocgpu_problem_set_options(mocgpu_problem *p, const mocgpu_options *in);
+/* Copies a named flat array (see FlatProblem: "seg_len", "seg_fsr", ...)
+ * into dst; nbytes must equal the array's size in bytes. */
+int mocgpu_problem_export(const mocgpu_problem *p, const char *field, void *dst, int64_t nbytes);
+int mocgpu_problem_field_bytes(const mocgpu_problem *p, const char *field, int64_t *nbytes);
+
+/* Seeded synthetic cross-section library in .xsl text form (materials
+ * fuel1..fuelN and moderator). Writes at most buflen bytes (NUL included)
+ * and reports the size needed. */
+int mocgpu_synthetic_xsl(uint64_t seed, int n_group, int n_fuel, const double *fuel_nf_scale, double mod_factor,
+                         double fuel_nf_factor, char *buf, int64_t buflen, int64_t *needed);
+
+/* Traces one ray through the geometry of xml_text (which needs only the
+ * geometry and material sections) as MOCC's Ray(p1, p2, bc, plane, mesh)
+ * does (src/sweepers/moc/ray.cpp:52-175). Arrays receive up to cap entries.
+ * coarse[] receives cm_cell_fw, cm_cell_bw, cm_surf_fw, cm_surf_bw; cm[]
+ * receives (fw, bw, nseg_fw, nseg_bw) per coarse crossing. */
+int mocgpu_trace_ray(const char *xml_text, const char *xsl_text, double x1, double y1, double x2, double y2,
+                     int *nseg, double *seg_len, int *seg_fsr, int cap, int *coarse, int *ncm, int *cm, int cm_cap);
+
+/* ---- sweeper: MOCC's TransportSweeper / MoCSweeper API
+ *      (src/core/transport_sweeper.hpp:41-351, src/sweepers/moc/moc_sweeper.cpp)
+ * precision: 0 = FP64 sweep, 1 = FP32 sweep with FP64 reductions and CMFD,
+ *            -1 = the <sweeper precision> of the input (default FP64). ---- */
+int mocgpu_sweeper_create(const mocgpu_problem *p, int precision, mocgpu_sweeper **out);
+void mocgpu_sweeper_destroy(mocgpu_sweeper *s);
+int mocgpu_sweeper_set_options(mocgpu_sweeper *s, const mocgpu_options *in);
+/* MoCSweeper::initialize (moc_sweeper.cpp:234-253): phi = 1, psi = 1/4pi */
+int mocgpu_initialize(mocgpu_sweeper *s);
+/* TransportSweeper::calc_fission_source (transport_sweeper.cpp:119-134);
+ * fs may be NULL (device copy only) */
+int mocgpu_calc_fission_source(mocgpu_sweeper *s, double k, double *fs);
+/* FixedSourceSolver::set_fission_source: device copy of a host fs[n_fsr] */
+int mocgpu_set_fission_source(mocgpu_sweeper *s, const double *fs);
+/* TransportSweeper::store_old_flux */
+int mocgpu_store_old_flux(mocgpu_sweeper *s);
+/* Source::initialize_group + fission + in_scatter (source.cpp:41-112) */
+int mocgpu_source_group(mocgpu_sweeper *s, int group);
+/* MoCSweeper::sweep(group) (moc_sweeper.cpp:189-225): n_inner inner sweeps;
+ * coarse currents on the last inner when coarse data is attached */
+int mocgpu_sweep_group(mocgpu_sweeper *s, int group);
+/* TransportSweeper::set_coarse_data: attach (1) or detach (0) the current tally */
+int mocgpu_set_coarse_data(mocgpu_sweeper *s, int enabled);
+/* TransportSweeper::total_fission(old) (transport_sweeper.cpp:104-117) */
+int mocgpu_total_fission(mocgpu_sweeper *s, int old, double *out);
+/* TransportSweeper::flux_residual (transport_sweeper.cpp:210-223) */
+int mocgpu_flux_residual(mocgpu_sweeper *s, double *out);
+int mocgpu_get_flux(mocgpu_sweeper *s, double *flux /* [n_fsr][G] */);
+int mocgpu_set_flux(mocgpu_sweeper *s, const double *flux /* [n_fsr][G] */);
+/* MoCSweeper::get_pin_flux_1g / set_pin_flux_1g, PIN_PLANE treatment
+ * (moc_sweeper.cpp:293-433); resid may be NULL */
+int mocgpu_get_pin_flux_1g(mocgpu_sweeper *s, int group, double *out /* [n_pin] */);
+int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in /* [n_pin] */, double *resid);
+/* TransportSweeper::pin_powers (transport_sweeper.cpp:140-193), [ny][nx] */
+int mocgpu_pin_powers(mocgpu_sweeper *s, double *out);
+/* CoarseData current and surface flux after the last current sweep, [G][n_surf] */
+int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux);
+/* EigenSolver::do_cmfd (eigen_solver.cpp:263-291) incl. CMFD::solve
+ * (cmfd.cpp:171-279); k is read and updated */
+int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
+/* EigenSolver::solve (eigen_solver.cpp:131-223): the whole power iteration.
+ * max_outer < 0 uses <solver max_iter>. */
+int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
+/* device bytes held by the handle; algorithmic bytes of one group sweep */
+int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOCGPU_H */

@@ -1,0 +1,340 @@
+"""mocc_gb300: GB300 2-D Method-of-Characteristics sweep and CMFD power iteration.
+
+Python mirror of MOCC's sweeper/solver interface over the library's C ABI
+(``include/mocgpu.h``). The classes keep MOCC's names and argument meanings:
+
+* :class:`Problem`    -- XML input processing, core mesh and ray tracing
+  (``src/input_proc.cpp``, ``src/core/core_mesh.cpp``,
+  ``src/sweepers/moc/ray_data.cpp``)
+* :class:`MoCSweeper` -- ``mocc::moc::MoCSweeper`` / ``TransportSweeper``
+  (``src/core/transport_sweeper.hpp:41-351``)
+* :class:`EigenSolver` -- ``mocc::EigenSolver`` (``src/solvers/eigen_solver.cpp``)
+
+Everything numeric runs in ``libmocgpu.so`` on the GPU; there is no CPU
+fallback, and constructing a sweeper without a CUDA device raises
+:class:`MocgpuError`. Errors that MOCC reports with ``EXCEPT`` surface as
+:class:`MocgpuError` carrying the C status code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["MocgpuError", "Problem", "MoCSweeper", "EigenSolver", "synthetic_xsl", "load_library", "SIZES"]
+
+_LIB = None
+
+SIZES = ["ngroup", "nfsr", "nmat", "ndir_oct", "nang", "nsets", "pol_per_set", "nx", "ny", "npin",
+         "nsurf", "nfuel", "ntracks", "nseg", "ncm", "maxseg"]
+
+
+class MocgpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[mocgpu {code}] {msg}")
+        self.code = code
+
+
+class _Options(C.Structure):
+    _fields_ = [("k_tol", C.c_double), ("psi_tol", C.c_double), ("max_iter", C.c_int), ("min_iter", C.c_int),
+                ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
+                ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
+                ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
+                ("precision", C.c_int)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("k", C.c_double), ("iterations", C.c_int), ("converged", C.c_int), ("error_k", C.c_double),
+                ("error_psi", C.c_double), ("seconds", C.c_double), ("sweeps", C.c_int64),
+                ("cmfd_iterations", C.c_int64)]
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "_build" / "libmocgpu.so"
+
+
+def load_library(build: bool = True):
+    """Loads libmocgpu.so (building it in-tree first when ``build``)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if build:
+        from . import _build
+        path = _build.build_library()
+    if not path.exists():
+        raise MocgpuError(99, f"libmocgpu.so not built at {path}")
+    lib = C.CDLL(str(path))
+    P, I, D, VP, CP = C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_char_p
+    DP, IP, I64P = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int64)
+    sig = {
+        "mocgpu_last_error": (CP, []),
+        "mocgpu_version": (I, []),
+        "mocgpu_device_count": (I, [IP]),
+        "mocgpu_problem_create": (I, [CP, CP, CP, C.POINTER(P)]),
+        "mocgpu_problem_destroy": (None, [P]),
+        "mocgpu_problem_sizes": (I, [P, I64P]),
+        "mocgpu_problem_options": (I, [P, C.POINTER(_Options)]),
+        "mocgpu_problem_set_options": (I, [P, C.POINTER(_Options)]),
+        "mocgpu_problem_export": (I, [P, CP, VP, C.c_int64]),
+        "mocgpu_problem_field_bytes": (I, [P, CP, I64P]),
+        "mocgpu_synthetic_xsl": (I, [C.c_uint64, I, I, DP, D, D, C.c_char_p, C.c_int64, I64P]),
+        "mocgpu_trace_ray": (I, [CP, CP, D, D, D, D, IP, DP, IP, I, IP, IP, IP, I]),
+        "mocgpu_sweeper_create": (I, [P, I, C.POINTER(P)]),
+        "mocgpu_sweeper_destroy": (None, [P]),
+        "mocgpu_sweeper_set_options": (I, [P, C.POINTER(_Options)]),
+        "mocgpu_initialize": (I, [P]),
+        "mocgpu_calc_fission_source": (I, [P, D, DP]),
+        "mocgpu_set_fission_source": (I, [P, DP]),
+        "mocgpu_store_old_flux": (I, [P]),
+        "mocgpu_source_group": (I, [P, I]),
+        "mocgpu_sweep_group": (I, [P, I]),
+        "mocgpu_set_coarse_data": (I, [P, I]),
+        "mocgpu_total_fission": (I, [P, I, DP]),
+        "mocgpu_flux_residual": (I, [P, DP]),
+        "mocgpu_get_flux": (I, [P, DP]),
+        "mocgpu_set_flux": (I, [P, DP]),
+        "mocgpu_get_pin_flux_1g": (I, [P, I, DP]),
+        "mocgpu_set_pin_flux_1g": (I, [P, I, DP, DP]),
+        "mocgpu_pin_powers": (I, [P, DP]),
+        "mocgpu_get_coarse_currents": (I, [P, DP, DP]),
+        "mocgpu_cmfd_solve": (I, [P, DP]),
+        "mocgpu_eigen_solve": (I, [P, I, C.POINTER(_Result)]),
+        "mocgpu_sweeper_bytes": (I, [P, I64P, DP]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise MocgpuError(rc, _LIB.mocgpu_last_error().decode())
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def synthetic_xsl(seed: int, n_group: int = 7, n_fuel: int = 1, fuel_nf_scale=None, mod_factor: float = 1.0,
+                  fuel_nf_factor: float = 1.0) -> str:
+    """Seeded synthetic .xsl library (materials fuel1..fuelN, moderator)."""
+    lib = load_library()
+    sc = None
+    if fuel_nf_scale is not None:
+        sc_arr = np.ascontiguousarray(fuel_nf_scale, dtype=np.float64)
+        assert sc_arr.size == n_fuel
+        sc = _dp(sc_arr)
+    need = C.c_int64(0)
+    _check(lib.mocgpu_synthetic_xsl(seed, n_group, n_fuel, sc, mod_factor, fuel_nf_factor, None, 0, C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    _check(lib.mocgpu_synthetic_xsl(seed, n_group, n_fuel, sc, mod_factor, fuel_nf_factor, buf, need.value,
+                                    C.byref(need)))
+    return buf.value.decode()
+
+
+class Problem:
+    """A traced 2-D problem from MOCC XML input (host side only)."""
+
+    INT_FIELDS = {"fsr_mat", "set_nx", "set_ny", "set_first_track", "trk_bc0", "trk_bc1", "trk_set",
+                  "trk_cm_cell_fw", "trk_cm_cell_bw", "trk_cm_surf_fw", "trk_cm_surf_bw", "trk_cm_begin",
+                  "cm_fw", "cm_bw", "cm_nseg_fw", "cm_nseg_bw", "seg_fsr", "pin_first_reg", "pin_cell",
+                  "pin_fuel", "bc"}
+    I64_FIELDS = {"trk_seg_begin"}
+
+    def __init__(self, xml: str, xsl: str | None = None, base_dir: str | None = None):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.mocgpu_problem_create(xml.encode(), xsl.encode() if xsl else None,
+                                         base_dir.encode() if base_dir else None, C.byref(h)))
+        self._h = h
+        self._lib = lib
+        arr = (C.c_int64 * len(SIZES))()
+        _check(lib.mocgpu_problem_sizes(h, arr))
+        self.sizes = dict(zip(SIZES, list(arr)))
+
+    @classmethod
+    def from_file(cls, path: str, xsl: str | None = None):
+        p = Path(path)
+        return cls(p.read_text(), xsl, str(p.parent))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.mocgpu_problem_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def export(self, field: str) -> np.ndarray:
+        n = C.c_int64(0)
+        _check(self._lib.mocgpu_problem_field_bytes(self._h, field.encode(), C.byref(n)))
+        dt = np.int32 if field in self.INT_FIELDS else np.int64 if field in self.I64_FIELDS else np.float64
+        out = np.empty(n.value // np.dtype(dt).itemsize, dtype=dt)
+        _check(self._lib.mocgpu_problem_export(self._h, field.encode(), out.ctypes.data_as(C.c_void_p), n.value))
+        return out
+
+    @property
+    def options(self) -> dict:
+        o = _Options()
+        _check(self._lib.mocgpu_problem_options(self._h, C.byref(o)))
+        return {f: getattr(o, f) for f, _ in _Options._fields_}
+
+    def set_options(self, **kw):
+        o = _Options()
+        _check(self._lib.mocgpu_problem_options(self._h, C.byref(o)))
+        for k, v in kw.items():
+            if k not in dict(_Options._fields_):
+                raise KeyError(k)
+            setattr(o, k, v)
+        _check(self._lib.mocgpu_problem_set_options(self._h, C.byref(o)))
+
+
+def trace_ray(xml: str, xsl: str, p1, p2, cap: int = 4096):
+    """MOCC's Ray(p1, p2, bc, 0, mesh) on the geometry in ``xml``."""
+    lib = load_library()
+    nseg, ncm = C.c_int(0), C.c_int(0)
+    L = np.zeros(cap)
+    F = np.zeros(cap, dtype=np.int32)
+    co = np.zeros(4, dtype=np.int32)
+    cm = np.zeros(4 * cap, dtype=np.int32)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    _check(lib.mocgpu_trace_ray(xml.encode(), xsl.encode() if xsl else None, p1[0], p1[1], p2[0], p2[1],
+                                C.byref(nseg), _dp(L), ip(F), cap, ip(co), C.byref(ncm), ip(cm), cap))
+    n, m = nseg.value, ncm.value
+    return {"seg_len": L[:n].copy(), "seg_fsr": F[:n].copy(), "cm_cell_fw": int(co[0]), "cm_cell_bw": int(co[1]),
+            "cm_surf_fw": int(co[2]), "cm_surf_bw": int(co[3]), "cm": cm[:4 * m].reshape(m, 4).copy()}
+
+
+class MoCSweeper:
+    """Device-resident MoC sweeper (MOCC's MoCSweeper API).
+
+    ``precision``: 0 = FP64 sweep, 1 = FP32 sweep with FP64 reductions and
+    CMFD, -1 = the ``<sweeper precision>`` of the input.
+    """
+
+    def __init__(self, problem: Problem, precision: int = -1):
+        self.problem = problem
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.mocgpu_sweeper_create(problem.handle, precision, C.byref(h)))
+        self._h = h
+        s = problem.sizes
+        self.n_group, self.n_reg, self.n_pin = s["ngroup"], s["nfsr"], s["npin"]
+        self.nx, self.ny, self.n_surf = s["nx"], s["ny"], s["nsurf"]
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.mocgpu_sweeper_destroy(self._h)
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_options(self, **kw):
+        o = _Options()
+        _check(self._lib.mocgpu_problem_options(self.problem.handle, C.byref(o)))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        _check(self._lib.mocgpu_sweeper_set_options(self._h, C.byref(o)))
+
+    def initialize(self):
+        _check(self._lib.mocgpu_initialize(self._h))
+
+    def set_coarse_data(self, enabled: bool = True):
+        _check(self._lib.mocgpu_set_coarse_data(self._h, 1 if enabled else 0))
+
+    def calc_fission_source(self, k: float) -> np.ndarray:
+        fs = np.empty(self.n_reg)
+        _check(self._lib.mocgpu_calc_fission_source(self._h, k, _dp(fs)))
+        return fs
+
+    def set_fission_source(self, fs: np.ndarray):
+        fs = np.ascontiguousarray(fs, dtype=np.float64)
+        _check(self._lib.mocgpu_set_fission_source(self._h, _dp(fs)))
+
+    def store_old_flux(self):
+        _check(self._lib.mocgpu_store_old_flux(self._h))
+
+    def source_group(self, g: int):
+        _check(self._lib.mocgpu_source_group(self._h, g))
+
+    def sweep(self, g: int):
+        _check(self._lib.mocgpu_sweep_group(self._h, g))
+
+    def total_fission(self, old: bool = False) -> float:
+        v = C.c_double()
+        _check(self._lib.mocgpu_total_fission(self._h, 1 if old else 0, C.byref(v)))
+        return v.value
+
+    def flux_residual(self) -> float:
+        v = C.c_double()
+        _check(self._lib.mocgpu_flux_residual(self._h, C.byref(v)))
+        return v.value
+
+    def flux(self) -> np.ndarray:
+        f = np.empty((self.n_reg, self.n_group))
+        _check(self._lib.mocgpu_get_flux(self._h, _dp(f)))
+        return f
+
+    def set_flux(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.n_reg, self.n_group)
+        _check(self._lib.mocgpu_set_flux(self._h, _dp(f)))
+
+    def get_pin_flux_1g(self, g: int) -> np.ndarray:
+        out = np.empty(self.n_pin)
+        _check(self._lib.mocgpu_get_pin_flux_1g(self._h, g, _dp(out)))
+        return out
+
+    def set_pin_flux_1g(self, g: int, pf: np.ndarray) -> float:
+        pf = np.ascontiguousarray(pf, dtype=np.float64)
+        r = C.c_double()
+        _check(self._lib.mocgpu_set_pin_flux_1g(self._h, g, _dp(pf), C.byref(r)))
+        return r.value
+
+    def pin_powers(self) -> np.ndarray:
+        out = np.empty(self.n_pin)
+        _check(self._lib.mocgpu_pin_powers(self._h, _dp(out)))
+        return out.reshape(self.ny, self.nx)
+
+    def coarse_currents(self):
+        cur = np.empty((self.n_group, self.n_surf))
+        sfl = np.empty((self.n_group, self.n_surf))
+        _check(self._lib.mocgpu_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
+        return cur, sfl
+
+    def cmfd_solve(self, k: float) -> float:
+        kk = C.c_double(k)
+        _check(self._lib.mocgpu_cmfd_solve(self._h, C.byref(kk)))
+        return kk.value
+
+    def bytes(self):
+        db, sb = C.c_int64(), C.c_double()
+        _check(self._lib.mocgpu_sweeper_bytes(self._h, C.byref(db), C.byref(sb)))
+        return db.value, sb.value
+
+
+class EigenSolver:
+    """k-eigenvalue power iteration with optional CMFD (MOCC's EigenSolver)."""
+
+    def __init__(self, problem: Problem, precision: int = -1, sweeper: MoCSweeper | None = None):
+        self.problem = problem
+        self.sweeper = sweeper or MoCSweeper(problem, precision)
+
+    def solve(self, max_outer: int = -1) -> dict:
+        r = _Result()
+        _check(self.sweeper._lib.mocgpu_eigen_solve(self.sweeper.handle, max_outer, C.byref(r)))
+        return {f: getattr(r, f) for f, _ in _Result._fields_}
+
+    def pin_powers(self) -> np.ndarray:
+        return self.sweeper.pin_powers()

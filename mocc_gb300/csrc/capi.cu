@@ -1,0 +1,463 @@
+// extern "C" boundary of the library (declarations in include/mocgpu.h).
+#include "../../include/mocgpu.h"
+
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "device/sweeper.hpp"
+#include "host/materials.hpp"
+#include "host/problem.hpp"
+#include "host/xml.hpp"
+
+struct mocgpu_problem {
+    std::unique_ptr<mocgpu::Problem> P;
+};
+struct mocgpu_sweeper {
+    std::unique_ptr<mocgpu::Sweeper> S;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+thread_local std::string g_err;
+
+template <typename F> int guarded(F &&f)
+{
+    try {
+        f();
+        return MOCGPU_OK;
+    } catch (const mocgpu::Error &e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_err = "host out of memory";
+        return MOCGPU_ERR_INTERNAL;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return MOCGPU_ERR_INTERNAL;
+    }
+}
+
+#define REQUIRE(cond, msg)                                                                                           \
+    do {                                                                                                             \
+        if (!(cond)) throw mocgpu::Error(MOCGPU_ERR_ARG, msg);                                                       \
+    } while (0)
+
+struct Field {
+    const void *p;
+    int64_t bytes;
+};
+
+template <typename T> Field fld(const std::vector<T> &v) { return Field{v.data(), (int64_t)(v.size() * sizeof(T))}; }
+
+Field find_field(const mocgpu::FlatProblem &f, const std::string &name)
+{
+    static const char *names[] = {nullptr};
+    (void)names;
+    if (name == "xstr") return fld(f.xstr);
+    if (name == "xsnf") return fld(f.xsnf);
+    if (name == "xsf") return fld(f.xsf);
+    if (name == "xsch") return fld(f.xsch);
+    if (name == "scat") return fld(f.scat);
+    if (name == "fsr_mat") return fld(f.fsr_mat);
+    if (name == "fsr_vol") return fld(f.fsr_vol);
+    if (name == "fsr_area") return fld(f.fsr_area);
+    if (name == "ang_ox") return fld(f.ang_ox);
+    if (name == "ang_oy") return fld(f.ang_oy);
+    if (name == "ang_oz") return fld(f.ang_oz);
+    if (name == "ang_alpha") return fld(f.ang_alpha);
+    if (name == "ang_theta") return fld(f.ang_theta);
+    if (name == "ang_weight") return fld(f.ang_weight);
+    if (name == "ang_rsintheta") return fld(f.ang_rsintheta);
+    if (name == "set_nx") return fld(f.set_nx);
+    if (name == "set_ny") return fld(f.set_ny);
+    if (name == "set_first_track") return fld(f.set_first_track);
+    if (name == "set_spacing") return fld(f.set_spacing);
+    if (name == "trk_bc0") return fld(f.trk_bc0);
+    if (name == "trk_bc1") return fld(f.trk_bc1);
+    if (name == "trk_set") return fld(f.trk_set);
+    if (name == "trk_seg_begin") return fld(f.trk_seg_begin);
+    if (name == "trk_cm_cell_fw") return fld(f.trk_cm_cell_fw);
+    if (name == "trk_cm_cell_bw") return fld(f.trk_cm_cell_bw);
+    if (name == "trk_cm_surf_fw") return fld(f.trk_cm_surf_fw);
+    if (name == "trk_cm_surf_bw") return fld(f.trk_cm_surf_bw);
+    if (name == "trk_cm_begin") return fld(f.trk_cm_begin);
+    if (name == "cm_fw") return fld(f.cm_fw);
+    if (name == "cm_bw") return fld(f.cm_bw);
+    if (name == "cm_nseg_fw") return fld(f.cm_nseg_fw);
+    if (name == "cm_nseg_bw") return fld(f.cm_nseg_bw);
+    if (name == "seg_len") return fld(f.seg_len);
+    if (name == "seg_fsr") return fld(f.seg_fsr);
+    if (name == "dx") return fld(f.dx);
+    if (name == "dy") return fld(f.dy);
+    if (name == "pin_first_reg") return fld(f.pin_first_reg);
+    if (name == "pin_cell") return fld(f.pin_cell);
+    if (name == "pin_fuel") return fld(f.pin_fuel);
+    if (name == "pin_area") return fld(f.pin_area);
+    if (name == "bc") return Field{f.bc, (int64_t)sizeof(f.bc)};
+    if (name == "hz") return Field{&f.hz, (int64_t)sizeof(double)};
+    throw mocgpu::Error(MOCGPU_ERR_ARG, "unknown problem field: " + name);
+}
+
+void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
+{
+    c->k_tol = o.k_tol;
+    c->psi_tol = o.psi_tol;
+    c->max_iter = o.max_iter;
+    c->min_iter = o.min_iter;
+    c->cmfd = o.cmfd;
+    c->cmfd_enabled = o.cmfd_enabled;
+    c->cmfd_k_tol = o.cmfd_k_tol;
+    c->cmfd_psi_tol = o.cmfd_psi_tol;
+    c->cmfd_resid_reduction = o.cmfd_resid_reduction;
+    c->cmfd_max_iter = o.cmfd_max_iter;
+    c->cmfd_negative_fixup = o.cmfd_negative_fixup;
+    c->n_inner = o.n_inner;
+    c->gs_boundary = o.gs_boundary;
+    c->precision = o.precision;
+}
+void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
+{
+    REQUIRE(c->k_tol > 0 && c->psi_tol > 0, "tolerances must be positive");
+    REQUIRE(c->max_iter >= 0 && c->min_iter >= 0 && c->n_inner >= 0, "iteration counts must be non-negative");
+    o.k_tol = c->k_tol;
+    o.psi_tol = c->psi_tol;
+    o.max_iter = c->max_iter;
+    o.min_iter = c->min_iter;
+    o.cmfd = c->cmfd != 0;
+    o.cmfd_enabled = c->cmfd_enabled != 0;
+    o.cmfd_k_tol = c->cmfd_k_tol;
+    o.cmfd_psi_tol = c->cmfd_psi_tol;
+    o.cmfd_resid_reduction = c->cmfd_resid_reduction;
+    o.cmfd_max_iter = c->cmfd_max_iter;
+    o.cmfd_negative_fixup = c->cmfd_negative_fixup != 0;
+    o.n_inner = c->n_inner;
+    o.gs_boundary = c->gs_boundary != 0;
+    o.precision = c->precision;
+}
+} // namespace
+
+extern "C" {
+
+const char *mocgpu_last_error(void) { return g_err.c_str(); }
+int mocgpu_version(void) { return 100; }
+
+int mocgpu_device_count(int *n)
+{
+    return guarded([&] {
+        REQUIRE(n, "null output");
+        int c = 0;
+        cudaError_t e = cudaGetDeviceCount(&c);
+        *n = (e == cudaSuccess) ? c : 0;
+    });
+}
+
+int mocgpu_problem_create(const char *xml_text, const char *xsl_text, const char *base_dir, mocgpu_problem **out)
+{
+    return guarded([&] {
+        REQUIRE(xml_text && out, "null argument");
+        auto h = std::make_unique<mocgpu_problem>();
+        h->P = mocgpu::Problem::from_xml(xml_text, xsl_text ? xsl_text : "", base_dir ? base_dir : "");
+        *out = h.release();
+    });
+}
+
+void mocgpu_problem_destroy(mocgpu_problem *p) { delete p; }
+
+int mocgpu_problem_sizes(const mocgpu_problem *p, int64_t *s)
+{
+    return guarded([&] {
+        REQUIRE(p && s, "null argument");
+        const auto &f = p->P->flat;
+        s[MOCGPU_SZ_NGROUP] = f.ng;
+        s[MOCGPU_SZ_NFSR] = f.n_fsr;
+        s[MOCGPU_SZ_NMAT] = f.n_mat;
+        s[MOCGPU_SZ_NDIR_OCT] = f.ndir_oct;
+        s[MOCGPU_SZ_NANG] = f.n_ang;
+        s[MOCGPU_SZ_NSETS] = f.n_sets;
+        s[MOCGPU_SZ_POL_PER_SET] = f.pol_per_set;
+        s[MOCGPU_SZ_NX] = f.nx;
+        s[MOCGPU_SZ_NY] = f.ny;
+        s[MOCGPU_SZ_NPIN] = f.n_pin;
+        s[MOCGPU_SZ_NSURF] = f.n_surf;
+        s[MOCGPU_SZ_NFUEL] = f.n_fuel_2d;
+        s[MOCGPU_SZ_NTRACKS] = f.n_tracks;
+        s[MOCGPU_SZ_NSEG] = f.n_seg;
+        s[MOCGPU_SZ_NCM] = (int64_t)f.cm_fw.size();
+        s[MOCGPU_SZ_MAXSEG] = f.max_seg;
+    });
+}
+
+int mocgpu_problem_options(const mocgpu_problem *p, mocgpu_options *out)
+{
+    return guarded([&] {
+        REQUIRE(p && out, "null argument");
+        opts_to_c(p->P->opts, out);
+    });
+}
+
+int mocgpu_problem_set_options(mocgpu_problem *p, const mocgpu_options *in)
+{
+    return guarded([&] {
+        REQUIRE(p && in, "null argument");
+        opts_from_c(in, p->P->opts);
+    });
+}
+
+int mocgpu_problem_field_bytes(const mocgpu_problem *p, const char *field, int64_t *nbytes)
+{
+    return guarded([&] {
+        REQUIRE(p && field && nbytes, "null argument");
+        *nbytes = find_field(p->P->flat, field).bytes;
+    });
+}
+
+int mocgpu_problem_export(const mocgpu_problem *p, const char *field, void *dst, int64_t nbytes)
+{
+    return guarded([&] {
+        REQUIRE(p && field && dst, "null argument");
+        Field f = find_field(p->P->flat, field);
+        REQUIRE(f.bytes == nbytes, std::string("size mismatch for field ") + field);
+        if (nbytes) std::memcpy(dst, f.p, (size_t)nbytes);
+    });
+}
+
+int mocgpu_synthetic_xsl(uint64_t seed, int n_group, int n_fuel, const double *fuel_nf_scale, double mod_factor,
+                         double fuel_nf_factor, char *buf, int64_t buflen, int64_t *needed)
+{
+    return guarded([&] {
+        REQUIRE(n_group >= 3 && n_fuel >= 1, "need n_group >= 3 and n_fuel >= 1");
+        mocgpu::SyntheticXsSpec spec;
+        spec.ng = n_group;
+        spec.seed = seed;
+        spec.n_fuel = n_fuel;
+        if (fuel_nf_scale) spec.fuel_nf_scale.assign(fuel_nf_scale, fuel_nf_scale + n_fuel);
+        spec.mod_factor = mod_factor;
+        spec.fuel_nf_factor = fuel_nf_factor;
+        std::string t = mocgpu::synthetic_xsl(spec);
+        if (needed) *needed = (int64_t)t.size() + 1;
+        if (buf && buflen > 0) {
+            size_t n = std::min<size_t>((size_t)buflen - 1, t.size());
+            std::memcpy(buf, t.data(), n);
+            buf[n] = '\0';
+        }
+    });
+}
+
+int mocgpu_trace_ray(const char *xml_text, const char *xsl_text, double x1, double y1, double x2, double y2,
+                     int *nseg, double *seg_len, int *seg_fsr, int cap, int *coarse, int *ncm, int *cm, int cm_cap)
+{
+    return guarded([&] {
+        REQUIRE(xml_text && nseg && ncm, "null argument");
+        auto doc = mocgpu::parse_xml(xml_text);
+        auto mesh = mocgpu::CoreMesh::from_xml(*doc, "", xsl_text ? xsl_text : "");
+        mocgpu::Ray r(mocgpu::Point2(x1, y1), mocgpu::Point2(x2, y2), {0, 0}, *mesh);
+        *nseg = r.nseg();
+        for (int i = 0; i < r.nseg() && i < cap; i++) {
+            if (seg_len) seg_len[i] = r.seg_len[i];
+            if (seg_fsr) seg_fsr[i] = r.seg_fsr[i];
+        }
+        if (coarse) {
+            coarse[0] = r.cm_cell_fw;
+            coarse[1] = r.cm_cell_bw;
+            coarse[2] = r.cm_surf_fw;
+            coarse[3] = r.cm_surf_bw;
+        }
+        *ncm = (int)r.cm_data.size();
+        for (int i = 0; i < (int)r.cm_data.size() && i < cm_cap; i++) {
+            if (!cm) break;
+            cm[4 * i + 0] = (int)r.cm_data[i].fw;
+            cm[4 * i + 1] = (int)r.cm_data[i].bw;
+            cm[4 * i + 2] = r.cm_data[i].nseg_fw;
+            cm[4 * i + 3] = r.cm_data[i].nseg_bw;
+        }
+    });
+}
+
+// ---------------------------------------------------------------------------
+int mocgpu_sweeper_create(const mocgpu_problem *p, int precision, mocgpu_sweeper **out)
+{
+    return guarded([&] {
+        REQUIRE(p && out, "null argument");
+        REQUIRE(precision >= -1 && precision <= 1, "precision must be -1, 0 or 1");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+            throw mocgpu::Error(MOCGPU_ERR_CUDA, "no CUDA device available: the sweeper runs on the GPU only");
+        auto h = std::make_unique<mocgpu_sweeper>();
+        MOCGPU_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        try {
+            h->S = std::make_unique<mocgpu::Sweeper>(*p->P, precision, h->stream);
+        } catch (...) {
+            cudaStreamDestroy(h->stream);
+            throw;
+        }
+        *out = h.release();
+    });
+}
+
+void mocgpu_sweeper_destroy(mocgpu_sweeper *s)
+{
+    if (!s) return;
+    cudaStream_t st = s->stream;
+    s->S.reset();
+    if (st) cudaStreamDestroy(st);
+    delete s;
+}
+
+static mocgpu::Sweeper &sw(mocgpu_sweeper *s)
+{
+    if (!s || !s->S) throw mocgpu::Error(MOCGPU_ERR_ARG, "null sweeper");
+    return *s->S;
+}
+
+int mocgpu_sweeper_set_options(mocgpu_sweeper *s, const mocgpu_options *in)
+{
+    return guarded([&] {
+        REQUIRE(in, "null argument");
+        auto &S = sw(s);
+        int prec = S.precision();
+        opts_from_c(in, S.options());
+        S.options().precision = prec;
+    });
+}
+int mocgpu_initialize(mocgpu_sweeper *s)
+{
+    return guarded([&] { sw(s).initialize(); });
+}
+int mocgpu_calc_fission_source(mocgpu_sweeper *s, double k, double *fs)
+{
+    return guarded([&] {
+        REQUIRE(k != 0.0, "k must be non-zero");
+        auto &S = sw(s);
+        S.calc_fission_source(k);
+        if (fs) S.get_fission_source(fs);
+    });
+}
+int mocgpu_set_fission_source(mocgpu_sweeper *s, const double *fs)
+{
+    return guarded([&] {
+        REQUIRE(fs, "null argument");
+        sw(s).set_fission_source(fs);
+    });
+}
+int mocgpu_store_old_flux(mocgpu_sweeper *s)
+{
+    return guarded([&] { sw(s).store_old_flux(); });
+}
+int mocgpu_source_group(mocgpu_sweeper *s, int group)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(group >= 0 && group < S.flat().ng, "group out of range");
+        S.group_source(group);
+    });
+}
+int mocgpu_sweep_group(mocgpu_sweeper *s, int group)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(group >= 0 && group < S.flat().ng, "group out of range");
+        S.sweep(group);
+        MOCGPU_CUDA(cudaStreamSynchronize(S.stream()));
+        MOCGPU_CUDA(cudaGetLastError());
+    });
+}
+int mocgpu_set_coarse_data(mocgpu_sweeper *s, int enabled)
+{
+    return guarded([&] { sw(s).set_coarse_enabled(enabled != 0); });
+}
+int mocgpu_total_fission(mocgpu_sweeper *s, int old, double *out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        *out = sw(s).total_fission(old != 0);
+    });
+}
+int mocgpu_flux_residual(mocgpu_sweeper *s, double *out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        *out = sw(s).flux_residual();
+    });
+}
+int mocgpu_get_flux(mocgpu_sweeper *s, double *flux)
+{
+    return guarded([&] {
+        REQUIRE(flux, "null argument");
+        sw(s).get_flux(flux);
+    });
+}
+int mocgpu_set_flux(mocgpu_sweeper *s, const double *flux)
+{
+    return guarded([&] {
+        REQUIRE(flux, "null argument");
+        sw(s).set_flux(flux);
+    });
+}
+int mocgpu_get_pin_flux_1g(mocgpu_sweeper *s, int group, double *out)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(out && group >= 0 && group < S.flat().ng, "bad argument");
+        S.get_pin_flux(group, out);
+    });
+}
+int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in, double *resid)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(in && group >= 0 && group < S.flat().ng, "bad argument");
+        double r = S.set_pin_flux(group, in);
+        if (resid) *resid = r;
+    });
+}
+int mocgpu_pin_powers(mocgpu_sweeper *s, double *out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        sw(s).pin_powers(out);
+    });
+}
+int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux)
+{
+    return guarded([&] {
+        REQUIRE(current && surface_flux, "null argument");
+        sw(s).get_currents(current, surface_flux);
+    });
+}
+int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k)
+{
+    return guarded([&] {
+        REQUIRE(k, "null argument");
+        sw(s).cmfd_solve(*k);
+    });
+}
+int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        mocgpu::EigenResult r = sw(s).eigen_solve(max_outer);
+        out->k = r.k;
+        out->iterations = r.iterations;
+        out->converged = r.converged;
+        out->error_k = r.error_k;
+        out->error_psi = r.error_psi;
+        out->seconds = r.seconds;
+        out->sweeps = r.sweeps;
+        out->cmfd_iterations = r.cmfd_iterations;
+    });
+}
+int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        if (device_bytes) *device_bytes = (int64_t)S.device_bytes();
+        if (sweep_bytes) *sweep_bytes = S.sweep_bytes();
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,95 @@
+// Shared device helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "../host/geom.hpp"
+
+namespace mocgpu {
+
+#define MOCGPU_CUDA(call)                                                                                        \
+    do {                                                                                                         \
+        cudaError_t e_ = (call);                                                                                 \
+        if (e_ != cudaSuccess)                                                                                   \
+            throw ::mocgpu::Error(20, std::string("CUDA error: ") + cudaGetErrorString(e_) + " at " + __FILE__ + \
+                                          ":" + std::to_string(__LINE__));                                       \
+    } while (0)
+
+// Status flags a kernel may raise (OR-ed into a device word, read by the host).
+enum DeviceStatus : unsigned {
+    DEV_OK = 0,
+    DEV_NONPOSITIVE_PIN_FLUX = 1u << 0,
+    DEV_NAN = 1u << 1,
+    DEV_BAD_INDEX = 1u << 2,
+    DEV_CMFD_NOT_CONVERGED = 1u << 3,
+};
+
+template <typename T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count)
+    {
+        release();
+        n = count;
+        if (count) MOCGPU_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    }
+    void upload(const T *h, size_t count)
+    {
+        alloc(count);
+        if (count) MOCGPU_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    template <typename V> void upload(const V &v) { upload(v.data(), v.size()); }
+    void zero(cudaStream_t s = 0)
+    {
+        if (n) MOCGPU_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum; every thread gets the result. scratch needs 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *scratch)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) scratch[wid] = v;
+    __syncthreads();
+    double t = (threadIdx.x < (unsigned)nw) ? scratch[threadIdx.x] : 0.0;
+    if (wid == 0) {
+        t = warp_sum(t);
+        if (lane == 0) scratch[0] = t;
+    }
+    __syncthreads();
+    double r = scratch[0];
+    __syncthreads();
+    return r;
+}
+
+} // namespace mocgpu

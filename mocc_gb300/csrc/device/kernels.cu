@@ -1,0 +1,966 @@
+// Kernels for the MoC transport sweep and the CMFD-accelerated power
+// iteration around it. Each kernel cites the MOCC routine whose arithmetic
+// it follows; the structure (one launch per pass over HBM-resident arrays)
+// is this project's own.
+#include <cmath>
+
+#include "kernels.cuh"
+
+namespace mocgpu {
+
+constexpr double kFpi = 4.0 * 3.1415926535897932;
+
+// ---------------------------------------------------------------------------
+__global__ void k_fill(double *p, double v, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+template <typename Real> __global__ void k_fill_real(Real *p, double v, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (Real)v;
+}
+
+static int grid_for(int64_t n, int block, int cap = 152 * 16)
+{
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+void launch_fill(double *p, double v, int64_t n, cudaStream_t s)
+{
+    if (n > 0) k_fill<<<grid_for(n, 256), 256, 0, s>>>(p, v, n);
+}
+template <typename Real> void launch_fill_real(Real *p, double v, int64_t n, cudaStream_t s)
+{
+    if (n > 0) k_fill_real<Real><<<grid_for(n, 256), 256, 0, s>>>(p, v, n);
+}
+template void launch_fill_real<float>(float *, double, int64_t, cudaStream_t);
+template void launch_fill_real<double>(double *, double, int64_t, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// fs_r = sum_g (1/k) nuSigma_f,g phi_g,r   (transport_sweeper.cpp:119-134)
+__global__ void k_fission_source(GeomView g, StateView st, double rk)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * g.G;
+    double f = 0.0;
+    for (int ig = 0; ig < g.G; ig++) f += rk * nf[ig] * st.phi[(size_t)ig * g.n_fsr + r];
+    st.fs[r] = f;
+}
+void launch_fission_source(const GeomView &g, const StateView &st, double k, cudaStream_t s)
+{
+    k_fission_source<<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, 1.0 / k);
+}
+
+// sum_r sum_g phi V nuSigma_f   (transport_sweeper.cpp:104-117)
+__global__ void k_total_fission(GeomView g, const double *phi, double *out)
+{
+    __shared__ double scratch[32];
+    double acc = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.n_fsr; r += gridDim.x * blockDim.x) {
+        const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * g.G;
+        double v = g.fsr_vol[r];
+        for (int ig = 0; ig < g.G; ig++) acc += phi[(size_t)ig * g.n_fsr + r] * v * nf[ig];
+    }
+    acc = block_sum(acc, scratch);
+    if (threadIdx.x == 0) atomicAdd(out, acc);
+}
+void launch_total_fission(const GeomView &g, const double *phi, double *out, cudaStream_t s)
+{
+    MOCGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+    k_total_fission<<<grid_for(g.n_fsr, 256, 304), 256, 0, s>>>(g, phi, out);
+}
+
+// Group source (source.cpp:41-112): src_r = chi_g fs_r + sum_{g'!=g} S(g<-g') phi_g'
+// and the transport source with self-scatter (source_isotropic.cpp:21-57):
+// qbar_r = (src_r + S(g<-g) phi_g,r) / (4 pi Sigma_tr,g). Also stages
+// Sigma_t of this group per FSR for the sweep.
+template <typename Real> __global__ void k_group_source(GeomView g, StateView st, int group)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    const int G = g.G;
+    const int m = g.fsr_mat[r];
+    const double *srow = g.scat + ((size_t)m * G + group) * G;
+    double src = g.xsch[(size_t)m * G + group] * st.fs[r];
+    for (int gg = 0; gg < G; gg++)
+        if (gg != group) src += srow[gg] * st.phi[(size_t)gg * g.n_fsr + r];
+    st.src1g[r] = src;
+    double xt = g.xstr[(size_t)m * G + group];
+    double q = (src + st.phi[(size_t)group * g.n_fsr + r] * srow[group]) * (1.0 / (xt * kFpi));
+    ((Real *)st.qbar)[r] = (Real)q;
+    ((Real *)st.sigt)[r] = (Real)xt;
+}
+template <typename Real> void launch_group_source(const GeomView &g, const StateView &st, int group, cudaStream_t s)
+{
+    k_group_source<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group);
+}
+template void launch_group_source<float>(const GeomView &, const StateView &, int, cudaStream_t);
+template void launch_group_source<double>(const GeomView &, const StateView &, int, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Attenuation 1 - exp(-tau).
+// FP64: MOCC's linear-interpolated table on [-10, 0] with 10000 intervals and
+// the library exponential outside it (exponential.hpp:56-112).
+// FP32: a 4-term Taylor series of 1 - e^{-tau} for tau < 1/64 (relative error
+// below 1e-9 there) and the fast hardware exponential above it.
+struct ExpConst {
+    double min, space, rspace;
+};
+__constant__ ExpConst c_exp;
+
+__device__ __forceinline__ double attenuation(double tau, const double *tab)
+{
+    double v = -tau;
+    if (v < c_exp.min || v > 0.0) return 1.0 - exp(v);
+    int i = (int)((v - c_exp.min) * c_exp.rspace);
+    if (i >= kExpN) i = kExpN - 1;
+    v -= c_exp.space * i + c_exp.min;
+    double d0 = __ldg(tab + i), d1 = __ldg(tab + i + 1);
+    return 1.0 - (d0 + (d1 - d0) * v * c_exp.rspace);
+}
+__device__ __forceinline__ float attenuation(float tau, const double *)
+{
+    if (tau < 0.015625f) return tau * (1.0f - tau * (0.5f - tau * (0.16666667f - tau * 0.041666668f)));
+    return 1.0f - __expf(-tau);
+}
+
+void set_exp_constants(double min, double space, double rspace)
+{
+    ExpConst c{min, space, rspace};
+    MOCGPU_CUDA(cudaMemcpyToSymbol(c_exp, &c, sizeof(c)));
+}
+
+// ---------------------------------------------------------------------------
+// One-group sweep of a range of tracks (moc_sweeper_kernel.inc.hpp:36-180):
+// one thread per track, all polar angles of the track's azimuth in
+// registers, forward then backward. The FSR tally of one segment is summed
+// over the polar angles in registers before a single atomic add.
+// Outgoing angular flux is written straight into the incoming slot of the
+// reflected angle (Gauss-Seidel, boundary_condition.cpp:155-191) or into the
+// outgoing buffer (Jacobi). With currents enabled the coarse-surface current
+// and surface flux are tallied at the precomputed crossing events
+// (moc_current_worker.hpp:202-264).
+template <typename Real, int NPOL, bool GS, bool CUR>
+__global__ void __launch_bounds__(128) k_sweep(GeomView g, StateView st, int group, int t0, int t1)
+{
+    int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= t1) return;
+    const Real *len = (const Real *)g.seg_len;
+    const Real *sigt = (const Real *)st.sigt;
+    const Real *qbar = (const Real *)st.qbar;
+    Real *tally = (Real *)st.tally;
+    Real *psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
+    Real *psi_out = (Real *)st.psi_out;
+    const int set = g.trk_set[t];
+    const int64_t b = g.seg_begin[t];
+    const int n = (int)(g.seg_begin[t + 1] - b);
+    const int bc0 = g.trk_bc0[t], bc1 = g.trk_bc1[t];
+    const int ny_set = g.set_ny[set];
+
+    Real rsin[NPOL], wt[NPOL], psi[NPOL];
+    int af[NPOL], ab[NPOL];
+    double cw[NPOL][2], fwt[NPOL][2];
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) {
+        const SetPolar sp = g.sp[set * NPOL + p];
+        rsin[p] = (Real)sp.rsin;
+        wt[p] = (Real)sp.wt;
+        af[p] = sp.ang_fwd;
+        ab[p] = sp.ang_bwd;
+        if (CUR) {
+            cw[p][0] = sp.cw[0];
+            cw[p][1] = sp.cw[1];
+            fwt[p][0] = sp.fw[0];
+            fwt[p][1] = sp.fw[1];
+        }
+    }
+    double *cur = st.cur + (size_t)group * g.n_surf;
+    double *sfl = st.sflux + (size_t)group * g.n_surf;
+
+    auto tally_events = [&](const int *pt, const int *code, int &ev, int ev_end, int k, double sign) {
+        while (ev < ev_end && pt[ev] == k) {
+            int c = code[ev];
+            int surf = c >> 1, nrm = c & 1;
+            double jc = 0.0, fc = 0.0;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                jc += (double)psi[p] * cw[p][nrm];
+                fc += (double)psi[p] * fwt[p][nrm];
+            }
+            atomicAdd(cur + surf, sign * jc);
+            atomicAdd(sfl + surf, fc);
+            ev++;
+        }
+    };
+    auto store_out = [&](int ang, int idx, Real v) {
+        if (GS) {
+            int tgt = g.wt_tgt[ang * 2 + (idx < ny_set ? 0 : 1)];
+            if (tgt >= 0) psi_in[tgt + idx] = v;
+        } else {
+            psi_out[g.bc_off[ang] + idx] = v;
+        }
+    };
+
+    // forward
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) psi[p] = psi_in[g.bc_off[af[p]] + bc0];
+    int ev = 0, ev_end = 0;
+    if (CUR) {
+        ev = g.ev_fw_begin[t];
+        ev_end = g.ev_fw_begin[t + 1];
+        tally_events(g.ev_fw_pt, g.ev_fw_code, ev, ev_end, 0, 1.0);
+    }
+    for (int s = 0; s < n; s++) {
+        const int r = g.seg_fsr[b + s];
+        const Real tau0 = sigt[r] * len[b + s];
+        const Real q = qbar[r];
+        Real acc = 0;
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) {
+            Real e = attenuation(tau0 * rsin[p], g.exp_tab);
+            Real d = (psi[p] - q) * e;
+            psi[p] -= d;
+            acc += d * wt[p];
+        }
+        atomicAdd(tally + r, acc);
+        if (CUR) tally_events(g.ev_fw_pt, g.ev_fw_code, ev, ev_end, s + 1, 1.0);
+    }
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) store_out(af[p], bc1, psi[p]);
+
+    // backward
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) psi[p] = psi_in[g.bc_off[ab[p]] + bc1];
+    if (CUR) {
+        ev = g.ev_bw_begin[t];
+        ev_end = g.ev_bw_begin[t + 1];
+        tally_events(g.ev_bw_pt, g.ev_bw_code, ev, ev_end, n, -1.0);
+    }
+    for (int s = n - 1; s >= 0; s--) {
+        const int r = g.seg_fsr[b + s];
+        const Real tau0 = sigt[r] * len[b + s];
+        const Real q = qbar[r];
+        Real acc = 0;
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) {
+            Real e = attenuation(tau0 * rsin[p], g.exp_tab);
+            Real d = (psi[p] - q) * e;
+            psi[p] -= d;
+            acc += d * wt[p];
+        }
+        atomicAdd(tally + r, acc);
+        if (CUR) tally_events(g.ev_bw_pt, g.ev_bw_code, ev, ev_end, s, -1.0);
+    }
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) store_out(ab[p], bc0, psi[p]);
+}
+
+template <typename Real, int NPOL>
+static void launch_sweep_np(const GeomView &g, const StateView &st, int group, int t0, int t1, bool gs, bool cur,
+                            cudaStream_t s)
+{
+    int n = t1 - t0;
+    if (n <= 0) return;
+    int grid = (n + 127) / 128;
+    if (gs) {
+        if (cur) k_sweep<Real, NPOL, true, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+        else k_sweep<Real, NPOL, true, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+    } else {
+        if (cur) k_sweep<Real, NPOL, false, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+        else k_sweep<Real, NPOL, false, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+    }
+}
+
+template <typename Real>
+void launch_sweep(const GeomView &g, const StateView &st, int group, int t0, int t1, bool gs, bool cur,
+                  cudaStream_t s)
+{
+    switch (g.pol) {
+    case 1: launch_sweep_np<Real, 1>(g, st, group, t0, t1, gs, cur, s); break;
+    case 2: launch_sweep_np<Real, 2>(g, st, group, t0, t1, gs, cur, s); break;
+    case 3: launch_sweep_np<Real, 3>(g, st, group, t0, t1, gs, cur, s); break;
+    case 4: launch_sweep_np<Real, 4>(g, st, group, t0, t1, gs, cur, s); break;
+    default: throw Error(1, "unsupported number of polar angles per track set");
+    }
+}
+template void launch_sweep<float>(const GeomView &, const StateView &, int, int, int, bool, bool, cudaStream_t);
+template void launch_sweep<double>(const GeomView &, const StateView &, int, int, int, bool, bool, cudaStream_t);
+
+// Jacobi boundary update: in(reflect(a, n)) <- out(a) on reflective faces,
+// 0 on vacuum faces (boundary_condition.cpp:145-191).
+template <typename Real> __global__ void k_jacobi_update(GeomView g, StateView st, int group)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.bc_per_group) return;
+    // locate the angle owning entry i
+    int lo = 0, hi = g.n_ang - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (g.bc_off[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const int a = lo;
+    const int idx = i - g.bc_off[a];
+    Real *in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
+    const Real *out = (const Real *)st.psi_out;
+    const int face = (idx < g.wt_tgt[2 * g.n_ang + a]) ? 0 : 1;
+    const int tgt = g.wt_tgt[a * 2 + face];
+    const int base = g.wt_tgt[3 * g.n_ang + a * 2 + face];
+    in[base + idx] = (tgt >= 0) ? out[i] : (Real)0;
+}
+template <typename Real> void launch_jacobi_update(const GeomView &g, const StateView &st, int group, cudaStream_t s)
+{
+    k_jacobi_update<Real><<<(g.bc_per_group + 255) / 256, 256, 0, s>>>(g, st, group);
+}
+template void launch_jacobi_update<float>(const GeomView &, const StateView &, int, cudaStream_t);
+template void launch_jacobi_update<double>(const GeomView &, const StateView &, int, cudaStream_t);
+
+// phi = tally / (Sigma_t V) + 4 pi qbar (moc_sweeper_kernel.inc.hpp:165-173),
+// then the self-scatter update of qbar for the next inner iteration.
+template <typename Real> __global__ void k_sweep_epilogue(GeomView g, StateView st, int group, int update_q)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    Real *tally = (Real *)st.tally;
+    Real *qbar = (Real *)st.qbar;
+    const Real *sigt = (const Real *)st.sigt;
+    double q = (double)qbar[r];
+    double ph = (double)tally[r] / ((double)sigt[r] * g.fsr_vol[r]) + q * kFpi;
+    st.phi[(size_t)group * g.n_fsr + r] = ph;
+    tally[r] = (Real)0;
+    if (update_q) {
+        const int G = g.G, m = g.fsr_mat[r];
+        double sgg = g.scat[((size_t)m * G + group) * G + group];
+        double xt = g.xstr[(size_t)m * G + group];
+        qbar[r] = (Real)((st.src1g[r] + ph * sgg) * (1.0 / (xt * kFpi)));
+    }
+}
+template <typename Real>
+void launch_sweep_epilogue(const GeomView &g, const StateView &st, int group, bool update_q, cudaStream_t s)
+{
+    k_sweep_epilogue<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group, update_q ? 1 : 0);
+}
+template void launch_sweep_epilogue<float>(const GeomView &, const StateView &, int, bool, cudaStream_t);
+template void launch_sweep_epilogue<double>(const GeomView &, const StateView &, int, bool, cudaStream_t);
+
+void launch_zero_radial_currents(const GeomView &g, const StateView &st, int group, cudaStream_t s)
+{
+    MOCGPU_CUDA(cudaMemsetAsync(st.cur + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
+    MOCGPU_CUDA(cudaMemsetAsync(st.sflux + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
+}
+
+// Currents per unit area on the x/y-normal surfaces (moc_current_worker.hpp:272-318).
+__global__ void k_normalize_currents(GeomView g, StateView st, int group, const double *area)
+{
+    int i = g.nx * g.ny + blockIdx.x * blockDim.x + threadIdx.x;
+    int end = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx + g.nx * g.ny;
+    if (i >= end) return;
+    st.cur[(size_t)group * g.n_surf + i] /= area[i];
+    st.sflux[(size_t)group * g.n_surf + i] /= area[i];
+}
+void launch_normalize_currents(const GeomView &g, const StateView &st, int group, const double *area, cudaStream_t s)
+{
+    int n = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx;
+    k_normalize_currents<<<(n + 255) / 256, 256, 0, s>>>(g, st, group, area);
+}
+
+// ---------------------------------------------------------------------------
+// Volume-averaged pin flux per group (moc_sweeper.cpp:293-326).
+__global__ void k_pin_flux(GeomView g, const double *phi, double *cflux)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.n_pin * g.G) return;
+    int ig = idx / g.n_pin, ip = idx % g.n_pin;
+    double v = 0.0, pf = 0.0;
+    for (int r = g.pin_first_reg[ip]; r < g.pin_first_reg[ip + 1]; r++) {
+        v += g.fsr_vol[r];
+        pf += phi[(size_t)ig * g.n_fsr + r] * g.fsr_vol[r];
+    }
+    cflux[(size_t)ig * g.n_pin + g.pin_cell[ip]] = pf / v;
+}
+void launch_pin_flux(const GeomView &g, const double *phi, double *cflux, cudaStream_t s)
+{
+    int n = g.n_pin * g.G;
+    k_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux);
+}
+
+// Rescale FSR fluxes by the coarse/fine pin-flux ratio (moc_sweeper.cpp:360-433).
+// A non-positive coarse flux raises a status flag and leaves that pin alone.
+__global__ void k_set_pin_flux(GeomView g, double *phi, const double *cflux, double *resid, unsigned *status)
+{
+    __shared__ double scratch[32];
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    double e2 = 0.0;
+    if (idx < g.n_pin * g.G) {
+        int ig = idx / g.n_pin, ip = idx % g.n_pin;
+        double c = cflux[(size_t)ig * g.n_pin + g.pin_cell[ip]];
+        if (!(c > 0.0)) {
+            atomicOr(status, (unsigned)DEV_NONPOSITIVE_PIN_FLUX);
+        } else {
+            double fm = 0.0;
+            int r0 = g.pin_first_reg[ip], r1 = g.pin_first_reg[ip + 1];
+            for (int r = r0; r < r1; r++) fm += phi[(size_t)ig * g.n_fsr + r] * g.fsr_area[r];
+            fm /= g.pin_area[ip];
+            double e = c - fm, f = c / fm;
+            for (int r = r0; r < r1; r++) phi[(size_t)ig * g.n_fsr + r] *= f;
+            e2 = e * e;
+        }
+    }
+    e2 = block_sum(e2, scratch);
+    if (threadIdx.x == 0 && resid) atomicAdd(resid, e2);
+}
+void launch_set_pin_flux(const GeomView &g, double *phi, const double *cflux, double *resid, unsigned *status,
+                         cudaStream_t s)
+{
+    int n = g.n_pin * g.G;
+    k_set_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux, resid, status);
+}
+
+// Flux-weighted pin homogenisation (xs_mesh_homogenized.cpp:261-363).
+__global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
+{
+    const double *fsr_area = g.fsr_area;
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ip >= g.n_pin) return;
+    const int G = g.G;
+    const int cell = g.pin_cell[ip];
+    const int r0 = g.pin_first_reg[ip], r1 = g.pin_first_reg[ip + 1];
+    double fs_sum = 0.0;
+    for (int r = r0; r < r1; r++) {
+        const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * G;
+        double f = 0.0;
+        for (int ig = 0; ig < G; ig++) f += nf[ig] * phi[(size_t)ig * g.n_fsr + r] * fsr_area[r];
+        fs_sum += f;
+    }
+    for (int ig = 0; ig < G; ig++) {
+        double fvs = 0.0, xt = 0.0, xnf = 0.0, xf = 0.0, xch = 0.0;
+        for (int r = r0; r < r1; r++) {
+            int m = g.fsr_mat[r];
+            double v = fsr_area[r], fl = phi[(size_t)ig * g.n_fsr + r];
+            fvs += v * fl;
+            xt += v * fl * g.xstr[(size_t)m * G + ig];
+            xnf += v * fl * g.xsnf[(size_t)m * G + ig];
+            xf += v * fl * g.xsf[(size_t)m * G + ig];
+            double fsr_fs = 0.0;
+            for (int gg = 0; gg < G; gg++) fsr_fs += g.xsnf[(size_t)m * G + gg] * phi[(size_t)gg * g.n_fsr + r] * v;
+            xch += fsr_fs * g.xsch[(size_t)m * G + ig];
+        }
+        for (int gg = 0; gg < G; gg++) {
+            double num = 0.0, den = 0.0;
+            for (int r = r0; r < r1; r++) {
+                int m = g.fsr_mat[r];
+                double v = fsr_area[r], fl = phi[(size_t)gg * g.n_fsr + r];
+                den += fl * v;
+                num += g.scat[((size_t)m * G + ig) * G + gg] * v * fl;
+            }
+            if (num > 0.0) num /= den;
+            c.scat[((size_t)cell * G + ig) * G + gg] = num;
+        }
+        c.xstr[(size_t)cell * G + ig] = xt / fvs;
+        c.xsnf[(size_t)cell * G + ig] = xnf / fvs;
+        c.xsf[(size_t)cell * G + ig] = xf / fvs;
+        c.xsch[(size_t)cell * G + ig] = (fs_sum > 0.0) ? xch / fs_sum : xch;
+    }
+    for (int ig = 0; ig < G; ig++)
+        c.xsrm[(size_t)cell * G + ig] = c.xstr[(size_t)cell * G + ig] - c.scat[((size_t)cell * G + ig) * G + ig];
+}
+void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, cudaStream_t s)
+{
+    k_homogenize<<<(g.n_pin + 127) / 128, 128, 0, s>>>(g, phi, c);
+}
+
+// ---------------------------------------------------------------------------
+// CMFD on the pin mesh (cmfd.cpp:171-666): coefficient build, then the CMFD
+// power iteration with one preconditioned BiCGSTAB solve per group. One CTA
+// runs the whole solve; all vectors live in global memory (L2 resident).
+namespace cm {
+__device__ __forceinline__ int cell_of(const CmfdView &c, int ix, int iy) { return iy * c.nx + ix; }
+__device__ int coarse_surf(const CmfdView &c, int cell, int s)
+{
+    const int nx = c.nx, ny = c.ny;
+    int ix = cell % nx, iy = cell / nx;
+    int nxy = (nx + 1) * ny + (ny + 1) * nx;
+    switch (s) {
+    case EAST: return (nx + 1) * iy + ix + 1 + nx * ny;
+    case WEST: return (nx + 1) * iy + ix + nx * ny;
+    case NORTH: return nx * ny + (nx + 1) * ny + (ny + 1) * ix + iy + 1;
+    case SOUTH: return (nx + 1) * ny + (ny + 1) * ix + iy + nx * ny;
+    case BOTTOM: return nx * iy + ix;
+    default: return nx * ny + nxy + nx * iy + ix; // TOP
+    }
+}
+__device__ int neighbor(const CmfdView &c, int cell, int s)
+{
+    int ix = cell % c.nx, iy = cell / c.nx;
+    switch (s) {
+    case NORTH: return iy < c.ny - 1 ? cell + c.nx : -1;
+    case SOUTH: return iy > 0 ? cell - c.nx : -1;
+    case EAST: return ix < c.nx - 1 ? cell + 1 : -1;
+    case WEST: return ix > 0 ? cell - 1 : -1;
+    default: return -1;
+    }
+}
+__device__ double area(const CmfdView &c, int cell, int s)
+{
+    int ix = cell % c.nx, iy = cell / c.nx;
+    if (s == EAST || s == WEST) return c.dy[iy] * c.hz;
+    if (s == NORTH || s == SOUTH) return c.dx[ix] * c.hz;
+    return c.dx[ix] * c.dy[iy];
+}
+// surface -> (low cell, high cell, normal, thickness direction)
+__device__ void surf_info(const CmfdView &c, int surf, int &c1, int &c2, int &nrm)
+{
+    const int nx = c.nx, ny = c.ny;
+    int nsz = nx * ny + (nx + 1) * ny + (ny + 1) * nx;
+    int s = surf % nsz;
+    int iz = surf / nsz;
+    if (s < nx * ny) {
+        nrm = Z_NORM;
+        c1 = (iz > 0) ? s : -1;
+        c2 = (iz < 1) ? s : -1;
+    } else if (s < nx * ny + (nx + 1) * ny) {
+        nrm = X_NORM;
+        int t = s - nx * ny;
+        int iy = t / (nx + 1), ix = t % (nx + 1);
+        c1 = ix > 0 ? cell_of(c, ix - 1, iy) : -1;
+        c2 = ix < nx ? cell_of(c, ix, iy) : -1;
+    } else {
+        nrm = Y_NORM;
+        int t = s - nx * ny - (nx + 1) * ny;
+        int iy = t % (ny + 1), ix = t / (ny + 1);
+        c1 = iy > 0 ? cell_of(c, ix, iy - 1) : -1;
+        c2 = iy < ny ? cell_of(c, ix, iy) : -1;
+    }
+}
+__device__ double thickness(const CmfdView &c, int cell, int nrm)
+{
+    if (nrm == X_NORM) return c.dx[cell % c.nx];
+    if (nrm == Y_NORM) return c.dy[cell / c.nx];
+    return c.hz;
+}
+__device__ double bc_diffusivity(int type)
+{
+    return (type == (int)BoundaryType::VACUUM) ? 0.5 / 2.0 : 0.0;
+}
+
+__device__ void spmv(const CmfdView &c, const double *m, const double *x, double *y)
+{
+    const int n = c.n_cell, nx = c.nx;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = m[i] * x[i];
+        int ix = i % nx;
+        if (ix > 0) v += m[n + i] * x[i - 1];
+        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
+        if (i >= nx) v += m[3 * n + i] * x[i - nx];
+        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
+        y[i] = v;
+    }
+}
+
+__device__ void block_sum2(double &a, double &b, double *scratch)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    __syncthreads();
+    if (lane == 0) {
+        scratch[wid] = a;
+        scratch[32 + wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double ta = (lane < nw) ? scratch[lane] : 0.0;
+        double tb = (lane < nw) ? scratch[32 + lane] : 0.0;
+        ta = warp_sum(ta);
+        tb = warp_sum(tb);
+        if (lane == 0) {
+            scratch[0] = ta;
+            scratch[32] = tb;
+        }
+    }
+    __syncthreads();
+    a = scratch[0];
+    b = scratch[32];
+    __syncthreads();
+}
+
+// b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
+__device__ void build_source(const CmfdView &c, int g, double *b)
+{
+    const int n = c.n_cell, G = c.G;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = c.xsch[(size_t)i * G + g] * c.fs[i];
+        const double *row = c.scat + ((size_t)i * G + g) * G;
+        for (int gg = 0; gg < G; gg++)
+            if (gg != g) s += row[gg] * c.flux[(size_t)gg * n + i];
+        double vol = c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz;
+        b[i] = s * vol;
+    }
+}
+
+// Preconditioned BiCGSTAB (van der Vorst 1992) with a diagonal (Jacobi)
+// preconditioner, stopping on ||r||^2 <= tol^2 ||b||^2 or max_it
+// iterations, restarting the shadow residual when it becomes orthogonal.
+__device__ int bicgstab(const CmfdView &c, const double *m, const double *b, double *x, double tol, int max_it,
+                        double *w, double *scratch)
+{
+    const int n = c.n_cell;
+    double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *y = w + 4 * n, *z = w + 5 * n, *s = w + 6 * n,
+           *t = w + 7 * n;
+    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
+    spmv(c, m, x, r);
+    __syncthreads();
+    double rr = 0.0, bb = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double ri = b[i] - r[i];
+        r[i] = ri;
+        r0[i] = ri;
+        p[i] = 0.0;
+        v[i] = 0.0;
+        rr += ri * ri;
+        bb += b[i] * b[i];
+    }
+    block_sum2(rr, bb, scratch);
+    if (bb == 0.0) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 0.0;
+        __syncthreads();
+        return 0;
+    }
+    double r0_sq = rr;
+    double rho = 1.0, alpha = 1.0, om = 1.0;
+    const double tol2 = tol * tol * bb;
+    int it = 0, restarts = 0;
+    double rho_new = rr; // r0 . r with r0 == r
+    while (rr > tol2 && it < max_it) {
+        double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0_sq) {
+            spmv(c, m, x, r);
+            __syncthreads();
+            double acc = 0.0, dummy = 0.0;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                double ri = b[i] - r[i];
+                r[i] = ri;
+                r0[i] = ri;
+                acc += ri * ri;
+            }
+            block_sum2(acc, dummy, scratch);
+            rho = r0_sq = acc;
+            if (restarts++ == 0) it = 0;
+        }
+        double beta = (rho / rho_old) * (alpha / om);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double pi = r[i] + beta * (p[i] - om * v[i]);
+            p[i] = pi;
+            double d = m[i];
+            y[i] = pi / (d != 0.0 ? d : 1.0);
+        }
+        __syncthreads();
+        spmv(c, m, y, v);
+        __syncthreads();
+        double r0v = 0.0, dummy = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) r0v += r0[i] * v[i];
+        block_sum2(r0v, dummy, scratch);
+        alpha = rho / r0v;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double si = r[i] - alpha * v[i];
+            s[i] = si;
+            double d = m[i];
+            z[i] = si / (d != 0.0 ? d : 1.0);
+        }
+        __syncthreads();
+        spmv(c, m, z, t);
+        __syncthreads();
+        double tt = 0.0, ts = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            tt += t[i] * t[i];
+            ts += t[i] * s[i];
+        }
+        block_sum2(tt, ts, scratch);
+        om = (tt > 0.0) ? ts / tt : 0.0;
+        double nrr = 0.0, nrho = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            x[i] += alpha * y[i] + om * z[i];
+            double ri = s[i] - om * t[i];
+            r[i] = ri;
+            nrr += ri * ri;
+            nrho += r0[i] * ri;
+        }
+        block_sum2(nrr, nrho, scratch);
+        rr = nrr;
+        rho_new = nrho;
+        it++;
+    }
+    return it;
+}
+
+__device__ double fission_source(const CmfdView &c, double k)
+{
+    const int n = c.n_cell, G = c.G;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double f = 0.0;
+        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
+        c.fs[i] = f * (1.0 / k);
+    }
+    __syncthreads();
+    return 0.0;
+}
+
+__device__ double total_fission(const CmfdView &c, double *scratch)
+{
+    const int n = c.n_cell, G = c.G;
+    double f = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
+    return block_sum(f, scratch);
+}
+
+// ||M_g x - b_g||^2 with x = current group flux
+__device__ double residual_g(const CmfdView &c, int g, const double *b, double *tmp, double *scratch)
+{
+    const int n = c.n_cell;
+    const double *m = c.mat + (size_t)g * 5 * n;
+    const double *x = c.flux + (size_t)g * n;
+    spmv(c, m, x, tmp);
+    __syncthreads();
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double d = tmp[i] - b[i];
+        acc += d * d;
+    }
+    return block_sum(acc, scratch);
+}
+} // namespace cm
+
+__global__ void __launch_bounds__(1024) k_cmfd_solve(CmfdView c)
+{
+    __shared__ double scratch[64];
+    const int n = c.n_cell, G = c.G, ns = c.n_surf;
+    double k = *c.k;
+    if (c.fixup)
+        for (int i = threadIdx.x; i < n * G; i += blockDim.x) c.flux[i] = fmax(c.flux[i], 0.0);
+    __syncthreads();
+
+    // surface coupling coefficients (cmfd.cpp:404-499)
+    for (int idx = threadIdx.x; idx < G * ns; idx += blockDim.x) {
+        int g = idx / ns, is = idx % ns;
+        int c1, c2, nrm;
+        cm::surf_info(c, is, c1, c2, nrm);
+        int lo_bc = (nrm == X_NORM) ? c.bc[WEST] : (nrm == Y_NORM) ? c.bc[SOUTH] : c.bc[BOTTOM];
+        int hi_bc = (nrm == X_NORM) ? c.bc[EAST] : (nrm == Y_NORM) ? c.bc[NORTH] : c.bc[TOP];
+        double d1 = (c1 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c1 * G + g])) / cm::thickness(c, c1, nrm)
+                              : cm::bc_diffusivity(lo_bc);
+        double d2 = (c2 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c2 * G + g])) / cm::thickness(c, c2, nrm)
+                              : cm::bc_diffusivity(hi_bc);
+        double dt = 2.0 * d1 * d2 / (d1 + d2);
+        double stil = (d1 > 0.0) ? d1 / (d1 + d2) : d2 / (d1 + d2);
+        double dh = 0.0, sh = 0.0;
+        bool have = (nrm != Z_NORM) && c.has_radial;
+        if (have) {
+            double j = c.cur[(size_t)g * ns + is];
+            double sfc = c.sflux[(size_t)g * ns + is];
+            double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
+            double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
+            dh = (j + dt * (fr - fl)) / (fl + fr);
+            if (!isfinite(dh)) dh = 0.0;
+            sh = (c1 >= 0) ? (sfc - stil * fl - (1.0 - stil) * fr) / (fl + fr) : (sfc - stil * fr) / fr;
+        }
+        c.d_tilde[idx] = dt;
+        c.s_tilde[idx] = stil;
+        c.d_hat[idx] = dh;
+        c.s_hat[idx] = sh;
+    }
+    __syncthreads();
+    // 5-point operator per group (cmfd.cpp:506-544)
+    for (int idx = threadIdx.x; idx < G * n; idx += blockDim.x) {
+        int g = idx / n, i = idx % n;
+        const double *dt = c.d_tilde + (size_t)g * ns;
+        const double *dh = c.d_hat + (size_t)g * ns;
+        double vol = c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz;
+        double diag = vol * c.xsrm[(size_t)i * G + g];
+        const int surfs[6] = {EAST, NORTH, WEST, SOUTH, TOP, BOTTOM};
+        for (int k6 = 0; k6 < 6; k6++) {
+            int s = surfs[k6];
+            int sf = cm::coarse_surf(c, i, s);
+            double a = cm::area(c, i, s);
+            double h = dh[sf];
+            if (s == WEST || s == SOUTH || s == BOTTOM) h = -h;
+            diag += a * (dt[sf] + h);
+        }
+        double *m = c.mat + (size_t)g * 5 * n;
+        m[i] = diag;
+        const int offs[4] = {WEST, EAST, SOUTH, NORTH};
+        for (int q = 0; q < 4; q++) {
+            int s = offs[q];
+            double v = 0.0;
+            if (cm::neighbor(c, i, s) >= 0) {
+                int sf = cm::coarse_surf(c, i, s);
+                double a = cm::area(c, i, s);
+                double h = dh[sf];
+                if (s == WEST || s == SOUTH) h = -h;
+                v = a * (h - dt[sf]);
+            }
+            m[(size_t)(q + 1) * n + i] = v;
+        }
+    }
+    __syncthreads();
+
+    double *b = c.vec, *tmp = c.vec + n, *work = c.vec + 2 * n;
+    cm::fission_source(c, k);
+    double tfis = cm::total_fission(c, scratch);
+    double r0 = 0.0;
+    for (int g = 0; g < G; g++) {
+        cm::build_source(c, g, b);
+        __syncthreads();
+        r0 += cm::residual_g(c, g, b, tmp, scratch);
+    }
+    r0 = sqrt(r0) / (double)(n * G);
+    const double tol = c.resid_reduction * r0;
+
+    int iter = 0, bic_its = 0;
+    double psi_err = 1.0, ri = 0.0, k_old = k;
+    while (true) {
+        iter++;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) c.fs_old[i] = c.fs[i];
+        __syncthreads();
+        cm::fission_source(c, k);
+        double tfis_old = tfis;
+        ri = 0.0;
+        for (int g = 0; g < G; g++) {
+            cm::build_source(c, g, b);
+            __syncthreads();
+            ri += cm::residual_g(c, g, b, tmp, scratch);
+            bic_its += cm::bicgstab(c, c.mat + (size_t)g * 5 * n, b, c.flux + (size_t)g * n, tol, 150, work, scratch);
+            __syncthreads();
+        }
+        ri = sqrt(ri) / (double)(n * G);
+        tfis = cm::total_fission(c, scratch);
+        k_old = k;
+        k = k * tfis / tfis_old;
+        double pe = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double e = c.fs[i] - c.fs_old[i];
+            pe += e * e;
+        }
+        psi_err = sqrt(block_sum(pe, scratch));
+        if ((fabs(k - k_old) < c.k_tol && psi_err < c.psi_tol && ri / r0 < c.resid_reduction) || iter > c.max_iter)
+            break;
+    }
+    for (int i = threadIdx.x; i < n * G; i += blockDim.x)
+        if (c.flux[i] < 0.0) c.flux[i] = -c.flux[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *c.k = k;
+        c.stats[0] = iter;
+        c.stats[1] = r0;
+        c.stats[2] = ri / r0;
+        c.stats[3] = psi_err;
+        c.stats[4] = bic_its;
+        if (iter > c.max_iter) atomicOr(c.status, (unsigned)DEV_CMFD_NOT_CONVERGED);
+        if (!isfinite(k)) atomicOr(c.status, (unsigned)DEV_NAN);
+    }
+}
+void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
+{
+    int threads = 1024;
+    if (c.n_cell < 1024) threads = ((c.n_cell + 31) / 32) * 32 < 128 ? 128 : ((c.n_cell + 31) / 32) * 32;
+    k_cmfd_solve<<<1, threads, 0, s>>>(c);
+}
+
+// ---------------------------------------------------------------------------
+// Fission-source change after MOCC's Normalize() of both vectors
+// (eigen_solver.cpp:171-184, util/utils.hpp:29-51). red[0..3] receive
+// (count>0, sum) of fs and fs_prev; red[4] the squared difference.
+__global__ void k_psi_err_sums(GeomView g, const double *fs, const double *fp, double *red)
+{
+    __shared__ double scratch[64];
+    double na = 0, sa = 0, nb = 0, sb = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.n_fsr; r += gridDim.x * blockDim.x) {
+        double a = fs[r], b = fp[r];
+        if (a > 0.0) na += 1.0;
+        sa += a;
+        if (b > 0.0) nb += 1.0;
+        sb += b;
+    }
+    cm::block_sum2(na, sa, scratch);
+    cm::block_sum2(nb, sb, scratch);
+    if (threadIdx.x == 0) {
+        atomicAdd(red + 0, na);
+        atomicAdd(red + 1, sa);
+        atomicAdd(red + 2, nb);
+        atomicAdd(red + 3, sb);
+    }
+}
+__global__ void k_psi_err_diff(GeomView g, const double *fs, const double *fp, double *red)
+{
+    __shared__ double scratch[32];
+    double fa = red[0] / red[1], fb = red[2] / red[3];
+    double acc = 0.0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < g.n_fsr; r += gridDim.x * blockDim.x) {
+        double e = fs[r] * fa - fp[r] * fb;
+        acc += e * e;
+    }
+    acc = block_sum(acc, scratch);
+    if (threadIdx.x == 0) atomicAdd(red + 4, acc);
+}
+void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev, double *red, cudaStream_t s)
+{
+    MOCGPU_CUDA(cudaMemsetAsync(red, 0, 5 * sizeof(double), s));
+    int grid = grid_for(g.n_fsr, 256, 304);
+    k_psi_err_sums<<<grid, 256, 0, s>>>(g, fs, fs_prev, red);
+    k_psi_err_diff<<<grid, 256, 0, s>>>(g, fs, fs_prev, red);
+}
+
+// sqrt(sum (phi - phi_old)^2)  (transport_sweeper.cpp:210-223); out = sum only
+__global__ void k_flux_residual(GeomView g, const double *a, const double *b, double *out)
+{
+    __shared__ double scratch[32];
+    double acc = 0.0;
+    int64_t n = (int64_t)g.n_fsr * g.G;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double e = a[i] - b[i];
+        acc += e * e;
+    }
+    acc = block_sum(acc, scratch);
+    if (threadIdx.x == 0) atomicAdd(out, acc);
+}
+void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s)
+{
+    MOCGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
+    k_flux_residual<<<grid_for((int64_t)g.n_fsr * g.G, 256, 304), 256, 0, s>>>(g, st.phi, st.phi_old, out);
+}
+
+// Fission-rate pin powers (transport_sweeper.cpp:140-193): pow[cell] gets
+// sum phi Sigma_f V over the pin's FSRs; pow[n_pin] gets the total.
+__global__ void k_pin_power(GeomView g, const double *phi, double *pow)
+{
+    __shared__ double scratch[32];
+    int ip = blockIdx.x * blockDim.x + threadIdx.x;
+    double tot = 0.0;
+    if (ip < g.n_pin) {
+        double p = 0.0;
+        for (int r = g.pin_first_reg[ip]; r < g.pin_first_reg[ip + 1]; r++) {
+            const double *xf = g.xsf + (size_t)g.fsr_mat[r] * g.G;
+            double fp = 0.0;
+            for (int ig = 0; ig < g.G; ig++) fp += phi[(size_t)ig * g.n_fsr + r] * xf[ig] * g.fsr_vol[r];
+            p += fp;
+        }
+        pow[g.pin_cell[ip]] = p;
+        tot = p;
+    }
+    tot = block_sum(tot, scratch);
+    if (threadIdx.x == 0) atomicAdd(pow + g.n_pin, tot);
+}
+void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s)
+{
+    MOCGPU_CUDA(cudaMemsetAsync(pow + g.n_pin, 0, sizeof(double), s));
+    k_pin_power<<<(g.n_pin + 255) / 256, 256, 0, s>>>(g, phi, pow);
+}
+
+} // namespace mocgpu

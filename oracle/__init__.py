@@ -1,0 +1,220 @@
+"""CPU oracle for the GPU library -- TEST INFRASTRUCTURE ONLY.
+
+FP64 OpenMP restatement of MOCC's 2-D MoC eigenvalue path (see oracle.h for
+the routine-by-routine citations). Used by tests/, ``__graft_entry__.smoke``
+and the CPU-baseline leg of ``bench.py`` as the checker; the product never
+loads it.
+
+``build()`` compiles ``oracle/_build/liboracle.so`` from oracle.cpp with
+g++ (``oracle/Makefile`` holds the same recipe).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_build"
+_LIB = None
+
+
+class _P(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("ng", "n_fsr", "n_mat", "ndir_oct", "n_ang", "n_sets", "pol_per_set",
+                                       "nx", "ny", "n_pin", "n_surf", "n_fuel_2d", "n_tracks")] + [
+        ("n_seg", C.c_int64), ("hz", C.c_double), ("bc", C.c_int * 6)] + [
+        (n, C.c_void_p) for n in ("xstr", "xsnf", "xsf", "xsch", "scat", "fsr_mat", "fsr_vol", "fsr_area",
+                                  "ang_ox", "ang_oy", "ang_oz", "ang_alpha", "ang_theta", "ang_weight",
+                                  "ang_rsintheta", "set_nx", "set_ny", "set_first_track", "set_spacing",
+                                  "trk_bc0", "trk_bc1", "trk_set", "trk_seg_begin", "trk_cm_cell_fw",
+                                  "trk_cm_cell_bw", "trk_cm_surf_fw", "trk_cm_surf_bw", "trk_cm_begin", "cm_fw",
+                                  "cm_bw", "cm_nseg_fw", "cm_nseg_bw", "seg_len", "seg_fsr", "dx", "dy",
+                                  "pin_first_reg", "pin_cell", "pin_fuel", "pin_area")]
+
+
+class _O(C.Structure):
+    _fields_ = [("k_tol", C.c_double), ("psi_tol", C.c_double), ("max_iter", C.c_int), ("min_iter", C.c_int),
+                ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
+                ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
+                ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
+                ("precision", C.c_int)]
+
+
+class _R(C.Structure):
+    _fields_ = [("k", C.c_double), ("iterations", C.c_int), ("converged", C.c_int), ("error_k", C.c_double),
+                ("error_psi", C.c_double), ("seconds", C.c_double), ("sweeps", C.c_int64),
+                ("cmfd_iterations", C.c_int64)]
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "oracle.cpp"
+    hdr = HERE / "oracle.h"
+    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-fPIC", "-shared", str(src), "-o"]
+    digest = hashlib.sha256(src.read_bytes() + hdr.read_bytes() + " ".join(cmd).encode()).hexdigest()
+    OUT.mkdir(exist_ok=True)
+    lib, stamp = OUT / "liboracle.so", OUT / "liboracle.stamp"
+    if not force and lib.exists() and stamp.exists() and stamp.read_text() == digest:
+        return lib
+    tmp = OUT / "liboracle.so.tmp"
+    r = subprocess.run(cmd + [str(tmp)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    tmp.replace(lib)
+    stamp.write_text(digest)
+    return lib
+
+
+def load():
+    global _LIB
+    if _LIB is None:
+        lib = C.CDLL(str(build()))
+        V, I, D = C.c_void_p, C.c_int, C.c_double
+        DP = C.POINTER(C.c_double)
+        for name, res, args in [
+            ("orc_last_error", C.c_char_p, []), ("orc_create", I, [C.POINTER(_P), C.POINTER(_O), I, C.POINTER(V)]),
+            ("orc_destroy", None, [V]), ("orc_threads", I, [V]), ("orc_initialize", I, [V]),
+            ("orc_set_coarse_data", I, [V, I]), ("orc_calc_fission_source", I, [V, D, DP]),
+            ("orc_set_fission_source", I, [V, DP]), ("orc_store_old_flux", I, [V]),
+            ("orc_source_group", I, [V, I]), ("orc_sweep_group", I, [V, I]), ("orc_total_fission", I, [V, I, DP]),
+            ("orc_flux_residual", I, [V, DP]), ("orc_get_flux", I, [V, DP]), ("orc_set_flux", I, [V, DP]),
+            ("orc_get_pin_flux_1g", I, [V, I, DP]), ("orc_set_pin_flux_1g", I, [V, I, DP, DP]),
+            ("orc_pin_powers", I, [V, DP]), ("orc_get_coarse_currents", I, [V, DP, DP]),
+            ("orc_cmfd_solve", I, [V, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
+            ("orc_table_exp", D, [D]),
+        ]:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def _chk(rc):
+    if rc != 0:
+        raise RuntimeError("oracle: " + _LIB.orc_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def table_exp(x: float) -> float:
+    return load().orc_table_exp(x)
+
+
+class OracleSolver:
+    """Oracle over the flat arrays of a traced ``mocc_gb300.Problem``."""
+
+    FIELDS = [f for f, t in _P._fields_ if t is C.c_void_p]
+
+    def __init__(self, problem, n_threads: int = 0, **option_overrides):
+        lib = load()
+        s = problem.sizes
+        self._keep = {f: np.ascontiguousarray(problem.export(f)) for f in self.FIELDS}
+        p = _P()
+        for k, src in (("ng", "ngroup"), ("n_fsr", "nfsr"), ("n_mat", "nmat"), ("ndir_oct", "ndir_oct"),
+                       ("n_ang", "nang"), ("n_sets", "nsets"), ("pol_per_set", "pol_per_set"), ("nx", "nx"),
+                       ("ny", "ny"), ("n_pin", "npin"), ("n_surf", "nsurf"), ("n_fuel_2d", "nfuel"),
+                       ("n_tracks", "ntracks")):
+            setattr(p, k, int(s[src]))
+        p.n_seg = int(s["nseg"])
+        p.hz = float(problem.export("hz")[0])
+        bc = problem.export("bc")
+        for i in range(6):
+            p.bc[i] = int(bc[i])
+        for f, arr in self._keep.items():
+            setattr(p, f, arr.ctypes.data_as(C.c_void_p))
+        self._p = p
+        opts = dict(problem.options)
+        opts.update(option_overrides)
+        o = _O(**{k: opts[k] for k, _ in _O._fields_})
+        self._o = o
+        h = C.c_void_p()
+        _chk(lib.orc_create(C.byref(p), C.byref(o), n_threads, C.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.n_group, self.n_reg, self.n_pin = int(s["ngroup"]), int(s["nfsr"]), int(s["npin"])
+        self.nx, self.ny, self.n_surf = int(s["nx"]), int(s["ny"]), int(s["nsurf"])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.orc_destroy(self._h)
+            self._h = None
+
+    @property
+    def threads(self):
+        return self._lib.orc_threads(self._h)
+
+    def initialize(self):
+        _chk(self._lib.orc_initialize(self._h))
+
+    def set_coarse_data(self, on=True):
+        _chk(self._lib.orc_set_coarse_data(self._h, 1 if on else 0))
+
+    def calc_fission_source(self, k):
+        fs = np.empty(self.n_reg)
+        _chk(self._lib.orc_calc_fission_source(self._h, k, _dp(fs)))
+        return fs
+
+    def set_fission_source(self, fs):
+        fs = np.ascontiguousarray(fs, dtype=np.float64)
+        _chk(self._lib.orc_set_fission_source(self._h, _dp(fs)))
+
+    def store_old_flux(self):
+        _chk(self._lib.orc_store_old_flux(self._h))
+
+    def source_group(self, g):
+        _chk(self._lib.orc_source_group(self._h, g))
+
+    def sweep(self, g):
+        _chk(self._lib.orc_sweep_group(self._h, g))
+
+    def total_fission(self, old=False):
+        v = C.c_double()
+        _chk(self._lib.orc_total_fission(self._h, 1 if old else 0, C.byref(v)))
+        return v.value
+
+    def flux(self):
+        f = np.empty((self.n_reg, self.n_group))
+        _chk(self._lib.orc_get_flux(self._h, _dp(f)))
+        return f
+
+    def set_flux(self, f):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        _chk(self._lib.orc_set_flux(self._h, _dp(f)))
+
+    def get_pin_flux_1g(self, g):
+        out = np.empty(self.n_pin)
+        _chk(self._lib.orc_get_pin_flux_1g(self._h, g, _dp(out)))
+        return out
+
+    def set_pin_flux_1g(self, g, pf):
+        pf = np.ascontiguousarray(pf, dtype=np.float64)
+        r = C.c_double()
+        _chk(self._lib.orc_set_pin_flux_1g(self._h, g, _dp(pf), C.byref(r)))
+        return r.value
+
+    def pin_powers(self):
+        out = np.empty(self.n_pin)
+        _chk(self._lib.orc_pin_powers(self._h, _dp(out)))
+        return out.reshape(self.ny, self.nx)
+
+    def coarse_currents(self):
+        cur = np.empty((self.n_group, self.n_surf))
+        sfl = np.empty((self.n_group, self.n_surf))
+        _chk(self._lib.orc_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
+        return cur, sfl
+
+    def cmfd_solve(self, k):
+        kk = C.c_double(k)
+        _chk(self._lib.orc_cmfd_solve(self._h, C.byref(kk)))
+        return kk.value
+
+    def solve(self, max_outer=-1):
+        r = _R()
+        _chk(self._lib.orc_eigen_solve(self._h, max_outer, C.byref(r)))
+        return {f: getattr(r, f) for f, _ in _R._fields_}

@@ -1,0 +1,182 @@
+"""GPU library against the CPU oracle on identical traced problems.
+
+Tolerances: the FP64 path must agree with the FP64 oracle to 1e-10 relative
+per sweep (only the order of floating-point sums differs); the mixed path
+(FP32 sweep, FP64 reductions and CMFD) must give k within 10 pcm and every
+fuel pin power within 0.1 %.
+"""
+import numpy as np
+import pytest
+
+import mocc_gb300 as m
+import oracle
+from mocc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+PCM_TOL = 10.0       # k error, pcm
+PIN_TOL = 1e-3       # max relative pin-power error
+FP64_TOL = 1e-10
+
+
+def pcm(k, k_ref):
+    return 1e5 * abs(k - k_ref) / k_ref
+
+
+def max_pin_err(p, p_ref):
+    mask = p_ref > 0
+    return float(np.max(np.abs(p[mask] - p_ref[mask]) / p_ref[mask]))
+
+
+def _pair(xml, xsl, precision, **opt):
+    P = m.Problem(xml, xsl)
+    if opt:
+        P.set_options(**opt)
+    return P, m.MoCSweeper(P, precision), oracle.OracleSolver(P)
+
+
+@pytest.mark.parametrize("gs", [1, 0])
+@pytest.mark.parametrize("currents", [False, True])
+def test_group_sweeps_fp64(gs, currents):
+    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs, n_inner=2)
+    S.initialize()
+    O.initialize()
+    S.set_coarse_data(currents)
+    O.set_coarse_data(currents)
+    rng = np.random.default_rng(11)
+    f0 = rng.uniform(0.5, 2.0, size=(P.sizes["nfsr"], P.sizes["ngroup"]))
+    S.set_flux(f0)
+    O.set_flux(f0)
+    fs = O.calc_fission_source(0.9)
+    S.set_fission_source(fs)
+    for sweep_round in range(2):
+        for g in range(P.sizes["ngroup"]):
+            S.source_group(g)
+            O.source_group(g)
+            S.sweep(g)
+            O.sweep(g)
+    a, b = S.flux(), O.flux()
+    assert np.max(np.abs(a - b) / np.abs(b)) < FP64_TOL
+    if currents:
+        ca, sa = S.coarse_currents()
+        cb, sb = O.coarse_currents()
+        scale = np.max(np.abs(cb))
+        assert np.max(np.abs(ca - cb)) < 1e-10 * scale
+        assert np.max(np.abs(sa - sb)) < 1e-10 * np.max(np.abs(sb))
+
+
+def test_group_sweeps_fp32_close():
+    P, S, O = _pair(*W.pin3x3(), 1, n_inner=2)
+    S.initialize()
+    O.initialize()
+    fs = O.calc_fission_source(1.0)
+    S.set_fission_source(fs)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        O.source_group(g)
+        S.sweep(g)
+        O.sweep(g)
+    a, b = S.flux(), O.flux()
+    assert np.max(np.abs(a - b) / np.abs(b)) < 2e-5
+
+
+def test_reductions_and_pin_flux_fp64():
+    P, S, O = _pair(*W.pin3x3(), 0)
+    S.initialize()
+    O.initialize()
+    rng = np.random.default_rng(5)
+    f0 = rng.uniform(0.5, 2.0, size=(P.sizes["nfsr"], P.sizes["ngroup"]))
+    S.set_flux(f0)
+    O.set_flux(f0)
+    assert abs(S.total_fission() - O.total_fission()) < 1e-12 * O.total_fission()
+    assert np.allclose(S.calc_fission_source(1.1), O.calc_fission_source(1.1), rtol=1e-13, atol=0)
+    for g in range(P.sizes["ngroup"]):
+        a = S.get_pin_flux_1g(g)
+        assert np.allclose(a, O.get_pin_flux_1g(g), rtol=1e-13, atol=0)
+        tgt = a * rng.uniform(0.8, 1.2, size=a.size)
+        ra = S.set_pin_flux_1g(g, tgt)
+        rb = O.set_pin_flux_1g(g, tgt)
+        assert abs(ra - rb) <= 1e-12 * max(rb, 1e-300)
+        assert np.allclose(S.get_pin_flux_1g(g), tgt, rtol=1e-12)
+    assert np.allclose(S.flux(), O.flux(), rtol=1e-12)
+    assert np.allclose(S.pin_powers(), O.pin_powers(), rtol=1e-12)
+    with pytest.raises(m.MocgpuError) as e:
+        S.set_pin_flux_1g(0, np.zeros(P.sizes["npin"]))
+    assert e.value.code == 11
+
+
+def test_cmfd_solve_fp64():
+    P, S, O = _pair(*W.pin3x3(), 0)
+    S.initialize()
+    O.initialize()
+    S.set_coarse_data(True)
+    O.set_coarse_data(True)
+    fs = O.calc_fission_source(1.0)
+    S.set_fission_source(fs)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        O.source_group(g)
+        S.sweep(g)
+        O.sweep(g)
+    ka = S.cmfd_solve(1.0)
+    kb = O.cmfd_solve(1.0)
+    assert abs(ka - kb) / kb < 1e-9
+    assert np.allclose(S.flux(), O.flux(), rtol=1e-8)
+
+
+@pytest.mark.parametrize("gs", [1, 0])
+def test_eigen_fp64_matches_oracle(gs):
+    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs)
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"] and rb["converged"]
+    assert ra["iterations"] == rb["iterations"]
+    assert abs(ra["k"] - rb["k"]) / rb["k"] < 1e-9
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < 1e-8
+
+
+def test_eigen_mixed_within_tolerance():
+    P, S, O = _pair(*W.pin3x3(), 1)
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"]
+    assert pcm(ra["k"], rb["k"]) < PCM_TOL
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < PIN_TOL
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_vacuum_boundaries_small_core(precision):
+    xml, xsl = W.minicore(n_lat=3, n_azi=4, spacing=0.05, precision="double")
+    P, S, O = _pair(xml, xsl, precision)
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"] and rb["converged"]
+    assert pcm(ra["k"], rb["k"]) < (1e-4 if precision == 0 else PCM_TOL)
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < (1e-8 if precision == 0 else PIN_TOL)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ihm_on_gpu(ref_xsl, precision):
+    from test_oracle_known_answers import analytic_spectrum, ihm_problem
+    P = ihm_problem(ref_xsl, n_inner=200)
+    k_ref, phi = analytic_spectrum(P)
+    S = m.MoCSweeper(P, precision)
+    n = P.sizes["nfsr"]
+    S.initialize()
+    S.set_flux(np.tile(phi, (n, 1)))
+    fs = S.calc_fission_source(k_ref)
+    assert np.allclose(fs, 1.0, atol=1e-13)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        S.sweep(g)
+        assert np.max(np.abs(S.flux()[:, g] - phi[g])) <= 0.005 * phi[g]
+
+
+def test_assembly17_mixed_vs_oracle():
+    xml, xsl = W.assembly17()
+    P, S, O = _pair(xml, xsl, 1)
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"] and rb["converged"]
+    assert pcm(ra["k"], rb["k"]) < PCM_TOL
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < PIN_TOL

@@ -1,0 +1,118 @@
+"""The CPU oracle against MOCC's own known-answer tests.
+
+* test_Exponential.cpp: table exponential within 2e-8 of exp on [-10, 0)
+* test_MoC_IHM.cpp: infinite homogeneous medium -- after one sweep per group
+  from the analytic spectrum the FSR flux equals the spectrum within 0.5 %
+* test_MoCSweeper.cpp: get -> set -> get pin flux is the identity
+The material of the IHM case is the synthetic fuel (the test's logic holds for
+any cross sections).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import mocc_gb300 as m
+import oracle
+
+IHM_GEOM = ('<mesh id="1" type="rect" pitch="1.26"><sub_x>3</sub_x><sub_y>3</sub_y></mesh>'
+            '<pin id="1" mesh="1">1 1 1 1 1 1 1 1 1</pin>'
+            '<lattice id="1" nx="3" ny="2">1 1 1 1 1 1</lattice>'
+            '<assembly id="1" np="1" hz="0.5"><lattices>1</lattices></assembly>'
+            '<core nx="1" ny="1" north="reflect" south="reflect" east="reflect" west="reflect" '
+            'top="reflect" bottom="reflect">1</core>'
+            '<material_lib path="x.xsl"><material id="1" name="UO2-3.3" /></material_lib>')
+
+
+def ihm_problem(ref_xsl, n_inner=800, quad='<ang_quad type="ls" order="2" />', spacing=0.01, extra=""):
+    solver = (f'<solver type="eigenvalue" k_tol="1e-8" psi_tol="1e-8" max_iter="300"><source scattering="P0" />'
+              f'<sweeper type="moc" n_inner="{n_inner}" {extra}>{quad}<rays spacing="{spacing}" /></sweeper></solver>')
+    return m.Problem(solver + IHM_GEOM, ref_xsl)
+
+
+def analytic_spectrum(P):
+    G = P.sizes["ngroup"]
+    xstr = P.export("xstr").reshape(-1, G)[0]
+    nf = P.export("xsnf").reshape(-1, G)[0]
+    chi = P.export("xsch").reshape(-1, G)[0]
+    S = P.export("scat").reshape(-1, G, G)[0]
+    M = np.diag(xstr) - S
+    phi = np.linalg.solve(M, chi)
+    return float(nf @ phi), phi
+
+
+def test_exponential_table():
+    xs = np.arange(-10.0, 0.0, 0.1)
+    err = max(abs(oracle.table_exp(x) - math.exp(x)) for x in xs)
+    assert err < 2e-8
+    # table nodes reproduce exp exactly (spacing 1e-3)
+    for i in (0, 1, 137, 5000, 9999):
+        x = -10.0 + i * (10.0 / 10000)
+        assert abs(oracle.table_exp(x) - math.exp(x)) < 1e-15
+    # outside the table the library exponential is used
+    assert oracle.table_exp(-12.5) == pytest.approx(math.exp(-12.5), rel=1e-15)
+
+
+def test_ihm_analytic_spectrum(ref_xsl):
+    P = ihm_problem(ref_xsl)
+    k_ref, phi = analytic_spectrum(P)
+    o = oracle.OracleSolver(P)
+    n, G = P.sizes["nfsr"], P.sizes["ngroup"]
+    o.set_flux(np.tile(phi, (n, 1)))
+    fs = o.calc_fission_source(k_ref)
+    assert np.allclose(fs, 1.0, atol=1e-14)
+    for g in range(G):
+        o.source_group(g)
+        o.sweep(g)
+        f = o.flux()[:, g]
+        assert np.max(np.abs(f - phi[g])) <= 0.005 * phi[g]
+
+
+def test_ihm_eigenvalue_converges_to_k_inf(ref_xsl):
+    P = ihm_problem(ref_xsl, n_inner=2)
+    k_ref, _ = analytic_spectrum(P)
+    r = oracle.OracleSolver(P).solve()
+    assert r["converged"]
+    assert abs(r["k"] - k_ref) / k_ref < 5e-5
+
+
+def test_pin_flux_get_set_identity(ref_xsl):
+    from mocc_gb300 import workloads as W
+    xml, xsl = W.pin3x3()
+    P = m.Problem(xml, xsl)
+    o = oracle.OracleSolver(P)
+    o.initialize()
+    rng = np.random.default_rng(3)
+    o.set_flux(rng.uniform(0.5, 2.0, size=(P.sizes["nfsr"], P.sizes["ngroup"])))
+    for g in (0, 3):
+        a = o.get_pin_flux_1g(g)
+        o.set_pin_flux_1g(g, a)
+        b = o.get_pin_flux_1g(g)
+        assert np.allclose(a, b, rtol=1e-13, atol=0)
+    with pytest.raises(RuntimeError):
+        o.set_pin_flux_1g(0, np.zeros(P.sizes["npin"]))
+
+
+def test_jacobi_and_gauss_seidel_reach_same_k():
+    from mocc_gb300 import workloads as W
+    xml, xsl = W.pin3x3()
+    P = m.Problem(xml, xsl)
+    gs = oracle.OracleSolver(P, k_tol=1e-9, psi_tol=1e-8).solve()
+    ja = oracle.OracleSolver(P, k_tol=1e-9, psi_tol=1e-8, gs_boundary=0).solve()
+    nocmfd = oracle.OracleSolver(P, k_tol=1e-9, psi_tol=1e-8, cmfd=0, max_iter=2000).solve()
+    for r in (gs, ja, nocmfd):
+        assert r["converged"]
+    assert abs(gs["k"] - ja["k"]) / gs["k"] < 1e-7
+    assert abs(gs["k"] - nocmfd["k"]) / gs["k"] < 1e-6
+    # CMFD accelerates: far fewer outer iterations
+    assert gs["iterations"] < nocmfd["iterations"]
+
+
+def test_thread_count_does_not_change_the_answer():
+    from mocc_gb300 import workloads as W
+    xml, xsl = W.pin3x3()
+    P = m.Problem(xml, xsl)
+    a = oracle.OracleSolver(P, n_threads=1).solve()
+    b = oracle.OracleSolver(P, n_threads=4).solve()
+    assert a["iterations"] == b["iterations"]
+    assert abs(a["k"] - b["k"]) < 1e-12
