@@ -160,6 +160,16 @@ int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
 /* device bytes held by the handle; algorithmic bytes of one group sweep */
 int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
 
+/* ---- measurement helpers (no MOCC counterpart) ------------------------- */
+/* The CUDA stream (cudaStream_t) every launch of this handle is ordered on. */
+int mocgpu_sweeper_stream(mocgpu_sweeper *s, void **stream);
+/* Runs reps single-inner sweeps of a group and returns the summed device
+ * time of the sweep kernels (CUDA events on the handle's stream) and the
+ * number of sweep-kernel launches. Leaves the flux of that group updated. */
+int mocgpu_time_sweep(mocgpu_sweeper *s, int group, int reps, double *ms, int *launches);
+/* Total kernels launched by the library in this process so far. */
+int mocgpu_launch_count(int64_t *n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -103,6 +103,9 @@ def load_library(build: bool = True):
         "mocgpu_cmfd_solve": (I, [P, DP]),
         "mocgpu_eigen_solve": (I, [P, I, C.POINTER(_Result)]),
         "mocgpu_sweeper_bytes": (I, [P, I64P, DP]),
+        "mocgpu_sweeper_stream": (I, [P, C.POINTER(C.c_void_p)]),
+        "mocgpu_time_sweep": (I, [P, I, I, DP, IP]),
+        "mocgpu_launch_count": (I, [I64P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -322,6 +325,23 @@ class MoCSweeper:
         db, sb = C.c_int64(), C.c_double()
         _check(self._lib.mocgpu_sweeper_bytes(self._h, C.byref(db), C.byref(sb)))
         return db.value, sb.value
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.mocgpu_sweeper_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    def time_sweep(self, g: int, reps: int):
+        """(summed ms of the sweep kernels, number of sweep launches)."""
+        ms, nl = C.c_double(), C.c_int()
+        _check(self._lib.mocgpu_time_sweep(self._h, g, reps, C.byref(ms), C.byref(nl)))
+        return ms.value, nl.value
+
+
+def launch_count() -> int:
+    n = C.c_int64()
+    _check(load_library().mocgpu_launch_count(C.byref(n)))
+    return n.value
 
 
 class EigenSolver:

@@ -460,4 +460,27 @@ int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep
     });
 }
 
+int mocgpu_sweeper_stream(mocgpu_sweeper *s, void **stream)
+{
+    return guarded([&] {
+        REQUIRE(s && stream, "null argument");
+        *stream = (void *)s->stream;
+    });
+}
+int mocgpu_time_sweep(mocgpu_sweeper *s, int group, int reps, double *ms, int *launches)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(ms && reps > 0 && group >= 0 && group < S.flat().ng, "bad argument");
+        *ms = S.time_sweep(group, reps, launches);
+    });
+}
+int mocgpu_launch_count(int64_t *n)
+{
+    return guarded([&] {
+        REQUIRE(n, "null argument");
+        *n = mocgpu::launch_count();
+    });
+}
+
 } // extern "C"

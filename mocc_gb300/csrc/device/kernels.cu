@@ -2,6 +2,7 @@
 // iteration around it. Each kernel cites the MOCC routine whose arithmetic
 // it follows; the structure (one launch per pass over HBM-resident arrays)
 // is this project's own.
+#include <atomic>
 #include <cmath>
 
 #include "kernels.cuh"
@@ -9,6 +10,11 @@
 namespace mocgpu {
 
 constexpr double kFpi = 4.0 * 3.1415926535897932;
+
+// Number of kernels this library has launched (all streams, all handles).
+static std::atomic<int64_t> g_launches{0};
+static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(); }
 
 // ---------------------------------------------------------------------------
 __global__ void k_fill(double *p, double v, int64_t n)
@@ -32,11 +38,11 @@ static int grid_for(int64_t n, int block, int cap = 152 * 16)
 
 void launch_fill(double *p, double v, int64_t n, cudaStream_t s)
 {
-    if (n > 0) k_fill<<<grid_for(n, 256), 256, 0, s>>>(p, v, n);
+    if (n > 0) { note_launch(); k_fill<<<grid_for(n, 256), 256, 0, s>>>(p, v, n); }
 }
 template <typename Real> void launch_fill_real(Real *p, double v, int64_t n, cudaStream_t s)
 {
-    if (n > 0) k_fill_real<Real><<<grid_for(n, 256), 256, 0, s>>>(p, v, n);
+    if (n > 0) { note_launch(); k_fill_real<Real><<<grid_for(n, 256), 256, 0, s>>>(p, v, n); }
 }
 template void launch_fill_real<float>(float *, double, int64_t, cudaStream_t);
 template void launch_fill_real<double>(double *, double, int64_t, cudaStream_t);
@@ -54,7 +60,7 @@ __global__ void k_fission_source(GeomView g, StateView st, double rk)
 }
 void launch_fission_source(const GeomView &g, const StateView &st, double k, cudaStream_t s)
 {
-    k_fission_source<<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, 1.0 / k);
+    { note_launch(); k_fission_source<<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, 1.0 / k); }
 }
 
 // sum_r sum_g phi V nuSigma_f   (transport_sweeper.cpp:104-117)
@@ -73,7 +79,7 @@ __global__ void k_total_fission(GeomView g, const double *phi, double *out)
 void launch_total_fission(const GeomView &g, const double *phi, double *out, cudaStream_t s)
 {
     MOCGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
-    k_total_fission<<<grid_for(g.n_fsr, 256, 304), 256, 0, s>>>(g, phi, out);
+    { note_launch(); k_total_fission<<<grid_for(g.n_fsr, 256, 304), 256, 0, s>>>(g, phi, out); }
 }
 
 // Group source (source.cpp:41-112): src_r = chi_g fs_r + sum_{g'!=g} S(g<-g') phi_g'
@@ -98,7 +104,7 @@ template <typename Real> __global__ void k_group_source(GeomView g, StateView st
 }
 template <typename Real> void launch_group_source(const GeomView &g, const StateView &st, int group, cudaStream_t s)
 {
-    k_group_source<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group);
+    { note_launch(); k_group_source<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group); }
 }
 template void launch_group_source<float>(const GeomView &, const StateView &, int, cudaStream_t);
 template void launch_group_source<double>(const GeomView &, const StateView &, int, cudaStream_t);
@@ -269,11 +275,11 @@ static void launch_sweep_np(const GeomView &g, const StateView &st, int group, i
     if (n <= 0) return;
     int grid = (n + 127) / 128;
     if (gs) {
-        if (cur) k_sweep<Real, NPOL, true, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
-        else k_sweep<Real, NPOL, true, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+        if (cur) { note_launch(); k_sweep<Real, NPOL, true, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1); }
+        else { note_launch(); k_sweep<Real, NPOL, true, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1); }
     } else {
-        if (cur) k_sweep<Real, NPOL, false, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
-        else k_sweep<Real, NPOL, false, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1);
+        if (cur) { note_launch(); k_sweep<Real, NPOL, false, true><<<grid, 128, 0, s>>>(g, st, group, t0, t1); }
+        else { note_launch(); k_sweep<Real, NPOL, false, false><<<grid, 128, 0, s>>>(g, st, group, t0, t1); }
     }
 }
 
@@ -316,7 +322,7 @@ template <typename Real> __global__ void k_jacobi_update(GeomView g, StateView s
 }
 template <typename Real> void launch_jacobi_update(const GeomView &g, const StateView &st, int group, cudaStream_t s)
 {
-    k_jacobi_update<Real><<<(g.bc_per_group + 255) / 256, 256, 0, s>>>(g, st, group);
+    { note_launch(); k_jacobi_update<Real><<<(g.bc_per_group + 255) / 256, 256, 0, s>>>(g, st, group); }
 }
 template void launch_jacobi_update<float>(const GeomView &, const StateView &, int, cudaStream_t);
 template void launch_jacobi_update<double>(const GeomView &, const StateView &, int, cudaStream_t);
@@ -344,7 +350,7 @@ template <typename Real> __global__ void k_sweep_epilogue(GeomView g, StateView 
 template <typename Real>
 void launch_sweep_epilogue(const GeomView &g, const StateView &st, int group, bool update_q, cudaStream_t s)
 {
-    k_sweep_epilogue<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group, update_q ? 1 : 0);
+    { note_launch(); k_sweep_epilogue<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group, update_q ? 1 : 0); }
 }
 template void launch_sweep_epilogue<float>(const GeomView &, const StateView &, int, bool, cudaStream_t);
 template void launch_sweep_epilogue<double>(const GeomView &, const StateView &, int, bool, cudaStream_t);
@@ -367,7 +373,7 @@ __global__ void k_normalize_currents(GeomView g, StateView st, int group, const 
 void launch_normalize_currents(const GeomView &g, const StateView &st, int group, const double *area, cudaStream_t s)
 {
     int n = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx;
-    k_normalize_currents<<<(n + 255) / 256, 256, 0, s>>>(g, st, group, area);
+    { note_launch(); k_normalize_currents<<<(n + 255) / 256, 256, 0, s>>>(g, st, group, area); }
 }
 
 // ---------------------------------------------------------------------------
@@ -387,7 +393,7 @@ __global__ void k_pin_flux(GeomView g, const double *phi, double *cflux)
 void launch_pin_flux(const GeomView &g, const double *phi, double *cflux, cudaStream_t s)
 {
     int n = g.n_pin * g.G;
-    k_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux);
+    { note_launch(); k_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux); }
 }
 
 // Rescale FSR fluxes by the coarse/fine pin-flux ratio (moc_sweeper.cpp:360-433).
@@ -419,7 +425,7 @@ void launch_set_pin_flux(const GeomView &g, double *phi, const double *cflux, do
                          cudaStream_t s)
 {
     int n = g.n_pin * g.G;
-    k_set_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux, resid, status);
+    { note_launch(); k_set_pin_flux<<<(n + 255) / 256, 256, 0, s>>>(g, phi, cflux, resid, status); }
 }
 
 // Flux-weighted pin homogenisation (xs_mesh_homogenized.cpp:261-363).
@@ -472,7 +478,7 @@ __global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
 }
 void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, cudaStream_t s)
 {
-    k_homogenize<<<(g.n_pin + 127) / 128, 128, 0, s>>>(g, phi, c);
+    { note_launch(); k_homogenize<<<(g.n_pin + 127) / 128, 128, 0, s>>>(g, phi, c); }
 }
 
 // ---------------------------------------------------------------------------
@@ -870,7 +876,7 @@ void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
 {
     int threads = 1024;
     if (c.n_cell < 1024) threads = ((c.n_cell + 31) / 32) * 32 < 128 ? 128 : ((c.n_cell + 31) / 32) * 32;
-    k_cmfd_solve<<<1, threads, 0, s>>>(c);
+    { note_launch(); k_cmfd_solve<<<1, threads, 0, s>>>(c); }
 }
 
 // ---------------------------------------------------------------------------
@@ -913,8 +919,8 @@ void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev
 {
     MOCGPU_CUDA(cudaMemsetAsync(red, 0, 5 * sizeof(double), s));
     int grid = grid_for(g.n_fsr, 256, 304);
-    k_psi_err_sums<<<grid, 256, 0, s>>>(g, fs, fs_prev, red);
-    k_psi_err_diff<<<grid, 256, 0, s>>>(g, fs, fs_prev, red);
+    { note_launch(); k_psi_err_sums<<<grid, 256, 0, s>>>(g, fs, fs_prev, red); }
+    { note_launch(); k_psi_err_diff<<<grid, 256, 0, s>>>(g, fs, fs_prev, red); }
 }
 
 // sqrt(sum (phi - phi_old)^2)  (transport_sweeper.cpp:210-223); out = sum only
@@ -933,7 +939,7 @@ __global__ void k_flux_residual(GeomView g, const double *a, const double *b, do
 void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s)
 {
     MOCGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(double), s));
-    k_flux_residual<<<grid_for((int64_t)g.n_fsr * g.G, 256, 304), 256, 0, s>>>(g, st.phi, st.phi_old, out);
+    { note_launch(); k_flux_residual<<<grid_for((int64_t)g.n_fsr * g.G, 256, 304), 256, 0, s>>>(g, st.phi, st.phi_old, out); }
 }
 
 // Fission-rate pin powers (transport_sweeper.cpp:140-193): pow[cell] gets
@@ -960,7 +966,7 @@ __global__ void k_pin_power(GeomView g, const double *phi, double *pow)
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s)
 {
     MOCGPU_CUDA(cudaMemsetAsync(pow + g.n_pin, 0, sizeof(double), s));
-    k_pin_power<<<(g.n_pin + 255) / 256, 256, 0, s>>>(g, phi, pow);
+    { note_launch(); k_pin_power<<<(g.n_pin + 255) / 256, 256, 0, s>>>(g, phi, pow); }
 }
 
 } // namespace mocgpu

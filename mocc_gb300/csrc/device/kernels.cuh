@@ -103,5 +103,6 @@ void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev
 void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s);
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);
 void set_exp_constants(double min, double space, double rspace);
+int64_t launch_count();
 
 } // namespace mocgpu

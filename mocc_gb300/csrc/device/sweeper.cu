@@ -475,6 +475,41 @@ void Sweeper::sweep(int g)
     }
 }
 
+double Sweeper::time_sweep(int g, int reps, int *launches)
+{
+    cudaEvent_t e0, e1;
+    MOCGPU_CUDA(cudaEventCreate(&e0));
+    MOCGPU_CUDA(cudaEventCreate(&e1));
+    double total = 0.0;
+    int nl = 0;
+    for (int r = 0; r < reps; r++) {
+        MOCGPU_CUDA(cudaEventRecord(e0, stream_));
+        if (opts_.gs_boundary) {
+            launch_sweep_pass(g, 0, phaseA_end_, true, false);
+            launch_sweep_pass(g, phaseA_end_, f_.n_tracks, true, false);
+            nl += 2;
+        } else {
+            launch_sweep_pass(g, 0, f_.n_tracks, false, false);
+            nl += 1;
+        }
+        MOCGPU_CUDA(cudaEventRecord(e1, stream_));
+        if (!opts_.gs_boundary) {
+            if (precision_ == 0) launch_jacobi_update<double>(gv_, sv_, g, stream_);
+            else launch_jacobi_update<float>(gv_, sv_, g, stream_);
+        }
+        launch_epilogue(g, true);
+        MOCGPU_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MOCGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        total += ms;
+    }
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (launches) *launches = nl;
+    return total;
+}
+
 double Sweeper::total_fission(bool old)
 {
     launch_total_fission(gv_, old ? phi_old_.p : phi_.p, red_.p + 8, stream_);

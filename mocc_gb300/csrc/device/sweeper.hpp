@@ -67,6 +67,11 @@ class Sweeper {
     int64_t sweeps_done = 0;
     int64_t cmfd_iters = 0;
 
+    // Runs `reps` single-inner sweeps of group g; returns the summed device
+    // time (ms, CUDA events on the handle's stream) of the sweep kernels only
+    // and the number of sweep-kernel launches they took.
+    double time_sweep(int g, int reps, int *launches);
+
     // device memory footprint (bytes)
     size_t device_bytes() const { return dev_bytes_; }
     // sweep-only algorithmic traffic per group sweep (bytes)
