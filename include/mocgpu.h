@@ -68,6 +68,7 @@ typedef struct mocgpu_options {
     double cmfd_k_tol, cmfd_psi_tol, cmfd_resid_reduction;
     int cmfd_max_iter, cmfd_negative_fixup;
     int n_inner, gs_boundary, precision;
+    int sweep_kernel; /* 0: one thread per track, 1: bundled work units (default) */
 } mocgpu_options;
 
 typedef struct mocgpu_result {
@@ -159,6 +160,14 @@ int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
 int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
 /* device bytes held by the handle; algorithmic bytes of one group sweep */
 int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
+
+/* ---- layout inspection (no MOCC counterpart) ---------------------------
+ * Builds the bundled work-unit layout of the GPU sweep on the host and
+ * reports: [0] units, [1] bundles, [2] rows, [3] real segment entries,
+ * [4] largest unit FSR set, [5] phases; stats_d: [0] sum of real segment
+ * lengths, [1] padding fraction. */
+int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int64_t *stats,
+                        double *stats_d);
 
 /* ---- measurement helpers (no MOCC counterpart) ------------------------- */
 /* The CUDA stream (cudaStream_t) every launch of this handle is ordered on. */

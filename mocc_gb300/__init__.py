@@ -42,7 +42,7 @@ class _Options(C.Structure):
                 ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("sweep_kernel", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -106,6 +106,7 @@ def load_library(build: bool = True):
         "mocgpu_sweeper_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "mocgpu_time_sweep": (I, [P, I, I, DP, IP]),
         "mocgpu_launch_count": (I, [I64P]),
+        "mocgpu_layout_stats": (I, [P, I, I, I, I64P, DP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -182,6 +183,16 @@ class Problem:
         out = np.empty(n.value // np.dtype(dt).itemsize, dtype=dt)
         _check(self._lib.mocgpu_problem_export(self._h, field.encode(), out.ctypes.data_as(C.c_void_p), n.value))
         return out
+
+    def layout_stats(self, gs: bool = True, tracks_per_unit: int = 64, max_local: int = 16384) -> dict:
+        """Host-side build of the GPU sweep's bundled layout, with checks."""
+        st = (C.c_int64 * 6)()
+        sd = (C.c_double * 2)()
+        _check(self._lib.mocgpu_layout_stats(self._h, 1 if gs else 0, tracks_per_unit, max_local, st, sd))
+        keys = ["units", "bundles", "rows", "real_segments", "max_local", "phases"]
+        d = dict(zip(keys, list(st)))
+        d["len_sum"], d["padding"] = sd[0], sd[1]
+        return d
 
     @property
     def options(self) -> dict:

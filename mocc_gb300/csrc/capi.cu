@@ -119,6 +119,7 @@ void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
     c->n_inner = o.n_inner;
     c->gs_boundary = o.gs_boundary;
     c->precision = o.precision;
+    c->sweep_kernel = o.sweep_kernel;
 }
 void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
 {
@@ -138,6 +139,8 @@ void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
     o.n_inner = c->n_inner;
     o.gs_boundary = c->gs_boundary != 0;
     o.precision = c->precision;
+    REQUIRE(c->sweep_kernel == 0 || c->sweep_kernel == 1, "sweep_kernel must be 0 or 1");
+    o.sweep_kernel = c->sweep_kernel;
 }
 } // namespace
 
@@ -457,6 +460,51 @@ int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep
         auto &S = sw(s);
         if (device_bytes) *device_bytes = (int64_t)S.device_bytes();
         if (sweep_bytes) *sweep_bytes = S.sweep_bytes();
+    });
+}
+
+int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int64_t *stats,
+                        double *stats_d)
+{
+    return guarded([&] {
+        REQUIRE(p && stats && stats_d, "null argument");
+        mocgpu::SweepLayout L = mocgpu::build_sweep_layout(p->P->flat, gs != 0, tracks_per_unit, max_local);
+        int64_t real = 0;
+        double sum = 0.0;
+        for (size_t b = 0; b < L.bundle_row.size(); b++)
+            for (int lane = 0; lane < 32; lane++) {
+                int t = L.bundle_track[b * 32 + lane];
+                if (t < 0) continue;
+                const auto &f = p->P->flat;
+                int n = (int)(f.trk_seg_begin[t + 1] - f.trk_seg_begin[t]);
+                for (int r = 0; r < L.bundle_nrows[b]; r++) {
+                    size_t i = (size_t)(L.bundle_row[b] + r) * 32 + lane;
+                    if (r < n) {
+                        real++;
+                        sum += L.len[i];
+                        // the unit-local index must map back to the segment's FSR
+                        int wu = -1;
+                        for (size_t u = 0; u < L.wu.size(); u++)
+                            if ((int)b >= L.wu[u].bundle_begin && (int)b < L.wu[u].bundle_begin + L.wu[u].n_bundles) {
+                                wu = (int)u;
+                                break;
+                            }
+                        if (wu < 0 || L.local_fsr[L.wu[wu].fsr_begin + L.lfsr[i]] != f.seg_fsr[f.trk_seg_begin[t] + r] ||
+                            L.len[i] != f.seg_len[f.trk_seg_begin[t] + r])
+                            throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "layout maps a segment to the wrong FSR or length");
+                    } else if (L.len[i] != 0.0) {
+                        throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "non-zero padding segment");
+                    }
+                }
+            }
+        stats[0] = (int64_t)L.wu.size();
+        stats[1] = (int64_t)L.bundle_row.size();
+        stats[2] = L.n_rows;
+        stats[3] = real;
+        stats[4] = L.max_local;
+        stats[5] = L.n_phases;
+        stats_d[0] = sum;
+        stats_d[1] = L.padding;
     });
 }
 

@@ -1,0 +1,434 @@
+// CMFD on the pin mesh (cmfd.cpp:171-666): surface coupling coefficients,
+// the 5-point operator per group, then the CMFD power iteration with one
+// preconditioned BiCGSTAB solve per group.
+//
+// One CTA runs a whole CMFD solve. Small meshes (up to 512 cells) run on a
+// single warp, so every reduction is a shuffle tree and every barrier a warp
+// barrier; larger meshes use up to 16 warps with one block barrier per
+// reduction. Work vectors live in shared memory when they fit.
+#include "kernels.cuh"
+
+namespace mocgpu {
+
+namespace {
+
+struct Blk {
+    int nw; // warps in the CTA
+    double *scratch;
+    int buf = 0;
+    __device__ void sync() const
+    {
+        if (nw == 1) __syncwarp();
+        else __syncthreads();
+    }
+    // Two block sums with a single barrier (double-buffered scratch).
+    __device__ void sum2(double &a, double &b)
+    {
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (nw == 1) return;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        double *s = scratch + buf * 64;
+        if (lane == 0) {
+            s[wid] = a;
+            s[32 + wid] = b;
+        }
+        __syncthreads();
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < nw; w++) {
+            ta += s[w];
+            tb += s[32 + w];
+        }
+        a = ta;
+        b = tb;
+        buf ^= 1;
+    }
+    __device__ double sum(double a)
+    {
+        double b = 0.0;
+        sum2(a, b);
+        return a;
+    }
+};
+
+__device__ __forceinline__ int cell_of(const CmfdView &c, int ix, int iy) { return iy * c.nx + ix; }
+
+__device__ int coarse_surf(const CmfdView &c, int cell, int s)
+{
+    const int nx = c.nx, ny = c.ny;
+    int ix = cell % nx, iy = cell / nx;
+    int nxy = (nx + 1) * ny + (ny + 1) * nx;
+    switch (s) {
+    case EAST: return (nx + 1) * iy + ix + 1 + nx * ny;
+    case WEST: return (nx + 1) * iy + ix + nx * ny;
+    case NORTH: return nx * ny + (nx + 1) * ny + (ny + 1) * ix + iy + 1;
+    case SOUTH: return (nx + 1) * ny + (ny + 1) * ix + iy + nx * ny;
+    case BOTTOM: return nx * iy + ix;
+    default: return nx * ny + nxy + nx * iy + ix; // TOP
+    }
+}
+__device__ int neighbor(const CmfdView &c, int cell, int s)
+{
+    int ix = cell % c.nx, iy = cell / c.nx;
+    switch (s) {
+    case NORTH: return iy < c.ny - 1 ? cell + c.nx : -1;
+    case SOUTH: return iy > 0 ? cell - c.nx : -1;
+    case EAST: return ix < c.nx - 1 ? cell + 1 : -1;
+    case WEST: return ix > 0 ? cell - 1 : -1;
+    default: return -1;
+    }
+}
+__device__ double area(const CmfdView &c, int cell, int s)
+{
+    int ix = cell % c.nx, iy = cell / c.nx;
+    if (s == EAST || s == WEST) return c.dy[iy] * c.hz;
+    if (s == NORTH || s == SOUTH) return c.dx[ix] * c.hz;
+    return c.dx[ix] * c.dy[iy];
+}
+__device__ void surf_info(const CmfdView &c, int surf, int &c1, int &c2, int &nrm)
+{
+    const int nx = c.nx, ny = c.ny;
+    int nsz = nx * ny + (nx + 1) * ny + (ny + 1) * nx;
+    int s = surf % nsz;
+    int iz = surf / nsz;
+    if (s < nx * ny) {
+        nrm = Z_NORM;
+        c1 = (iz > 0) ? s : -1;
+        c2 = (iz < 1) ? s : -1;
+    } else if (s < nx * ny + (nx + 1) * ny) {
+        nrm = X_NORM;
+        int t = s - nx * ny;
+        int iy = t / (nx + 1), ix = t % (nx + 1);
+        c1 = ix > 0 ? cell_of(c, ix - 1, iy) : -1;
+        c2 = ix < nx ? cell_of(c, ix, iy) : -1;
+    } else {
+        nrm = Y_NORM;
+        int t = s - nx * ny - (nx + 1) * ny;
+        int iy = t % (ny + 1), ix = t / (ny + 1);
+        c1 = iy > 0 ? cell_of(c, ix, iy - 1) : -1;
+        c2 = iy < ny ? cell_of(c, ix, iy) : -1;
+    }
+}
+__device__ double thickness(const CmfdView &c, int cell, int nrm)
+{
+    if (nrm == X_NORM) return c.dx[cell % c.nx];
+    if (nrm == Y_NORM) return c.dy[cell / c.nx];
+    return c.hz;
+}
+__device__ __forceinline__ double cell_vol(const CmfdView &c, int i) { return c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz; }
+
+__device__ void spmv(const CmfdView &c, const double *__restrict__ m, const double *x, double *y)
+{
+    const int n = c.n_cell, nx = c.nx;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = m[i] * x[i];
+        int ix = i % nx;
+        if (ix > 0) v += m[n + i] * x[i - 1];
+        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
+        if (i >= nx) v += m[3 * n + i] * x[i - nx];
+        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
+        y[i] = v;
+    }
+}
+
+// b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
+__device__ void build_source(const CmfdView &c, int g, double *b)
+{
+    const int n = c.n_cell, G = c.G;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = c.xsch[(size_t)i * G + g] * c.fs[i];
+        const double *row = c.scat + ((size_t)i * G + g) * G;
+        for (int gg = 0; gg < G; gg++)
+            if (gg != g) s += row[gg] * c.flux[(size_t)gg * n + i];
+        b[i] = s * cell_vol(c, i);
+    }
+}
+
+// Preconditioned BiCGSTAB (van der Vorst 1992) with a diagonal (Jacobi)
+// preconditioner, stopping on ||r||^2 <= tol^2 ||b||^2 or max_it
+// iterations, restarting the shadow residual when it becomes orthogonal.
+// x is in/out; w holds 8 work vectors.
+__device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double *b, double *x, double tol, int max_it,
+                        double *w)
+{
+    const int n = c.n_cell;
+    double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *y = w + 4 * n, *z = w + 5 * n, *s = w + 6 * n,
+           *t = w + 7 * n;
+    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
+    spmv(c, m, x, r);
+    double rr = 0.0, bb = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double ri = b[i] - r[i];
+        r[i] = ri;
+        r0[i] = ri;
+        p[i] = 0.0;
+        v[i] = 0.0;
+        rr += ri * ri;
+        bb += b[i] * b[i];
+    }
+    B.sum2(rr, bb);
+    if (bb == 0.0) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 0.0;
+        B.sync();
+        return 0;
+    }
+    double r0_sq = rr, rho = 1.0, alpha = 1.0, om = 1.0;
+    const double tol2 = tol * tol * bb;
+    int it = 0, restarts = 0;
+    double rho_new = rr;
+    while (rr > tol2 && it < max_it) {
+        double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0_sq) {
+            B.sync();
+            spmv(c, m, x, r);
+            double acc = 0.0;
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                double ri = b[i] - r[i];
+                r[i] = ri;
+                r0[i] = ri;
+                acc += ri * ri;
+            }
+            acc = B.sum(acc);
+            rho = r0_sq = acc;
+            if (restarts++ == 0) it = 0;
+        }
+        const double beta = (rho / rho_old) * (alpha / om);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double pi = r[i] + beta * (p[i] - om * v[i]);
+            p[i] = pi;
+            double d = m[i];
+            y[i] = pi / (d != 0.0 ? d : 1.0);
+        }
+        B.sync();
+        spmv(c, m, y, v);
+        double r0v = 0.0, dummy = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) r0v += r0[i] * v[i];
+        B.sum2(r0v, dummy);
+        alpha = rho / r0v;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double si = r[i] - alpha * v[i];
+            s[i] = si;
+            double d = m[i];
+            z[i] = si / (d != 0.0 ? d : 1.0);
+        }
+        B.sync();
+        spmv(c, m, z, t);
+        double tt = 0.0, ts = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            tt += t[i] * t[i];
+            ts += t[i] * s[i];
+        }
+        B.sum2(tt, ts);
+        om = (tt > 0.0) ? ts / tt : 0.0;
+        double nrr = 0.0, nrho = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            x[i] += alpha * y[i] + om * z[i];
+            double ri = s[i] - om * t[i];
+            r[i] = ri;
+            nrr += ri * ri;
+            nrho += r0[i] * ri;
+        }
+        B.sum2(nrr, nrho);
+        rr = nrr;
+        rho_new = nrho;
+        it++;
+    }
+    B.sync();
+    return it;
+}
+
+__device__ void fission_source(const CmfdView &c, double k)
+{
+    const int n = c.n_cell, G = c.G;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double f = 0.0;
+        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
+        c.fs[i] = f * (1.0 / k);
+    }
+}
+
+__device__ double total_fission(const CmfdView &c, Blk &B)
+{
+    const int n = c.n_cell, G = c.G;
+    double f = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
+    return B.sum(f);
+}
+
+// ||M_g x - b_g||^2 with x the group flux
+__device__ double residual_g(const CmfdView &c, Blk &B, const double *m, const double *x, const double *b)
+{
+    const int n = c.n_cell, nx = c.nx;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = m[i] * x[i];
+        int ix = i % nx;
+        if (ix > 0) v += m[n + i] * x[i - 1];
+        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
+        if (i >= nx) v += m[3 * n + i] * x[i - nx];
+        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
+        double d = v - b[i];
+        acc += d * d;
+    }
+    return B.sum(acc);
+}
+
+} // namespace
+
+__global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
+{
+    extern __shared__ __align__(16) double sm[];
+    Blk B;
+    B.nw = blockDim.x >> 5;
+    B.scratch = sm; // 128 doubles
+    const int n = c.n_cell, G = c.G, ns = c.n_surf;
+    // work vectors: b, x (group flux copy), 8 BiCGSTAB vectors
+    double *vec = vec_in_smem ? sm + 128 : c.vec;
+    double *b = vec, *x = vec + n, *w = vec + 2 * n;
+    double k = *c.k;
+    if (c.fixup)
+        for (int i = threadIdx.x; i < n * G; i += blockDim.x) c.flux[i] = fmax(c.flux[i], 0.0);
+    B.sync();
+
+    // surface coupling coefficients (cmfd.cpp:404-499)
+    for (int idx = threadIdx.x; idx < G * ns; idx += blockDim.x) {
+        int g = idx / ns, is = idx % ns;
+        int c1, c2, nrm;
+        surf_info(c, is, c1, c2, nrm);
+        int lo_bc = (nrm == X_NORM) ? c.bc[WEST] : (nrm == Y_NORM) ? c.bc[SOUTH] : c.bc[BOTTOM];
+        int hi_bc = (nrm == X_NORM) ? c.bc[EAST] : (nrm == Y_NORM) ? c.bc[NORTH] : c.bc[TOP];
+        double d1 = (c1 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c1 * G + g])) / thickness(c, c1, nrm)
+                              : (lo_bc == (int)BoundaryType::VACUUM ? 0.5 / 2.0 : 0.0);
+        double d2 = (c2 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c2 * G + g])) / thickness(c, c2, nrm)
+                              : (hi_bc == (int)BoundaryType::VACUUM ? 0.5 / 2.0 : 0.0);
+        double dt = 2.0 * d1 * d2 / (d1 + d2);
+        double stil = (d1 > 0.0) ? d1 / (d1 + d2) : d2 / (d1 + d2);
+        double dh = 0.0, sh = 0.0;
+        if (nrm != Z_NORM && c.has_radial) {
+            double j = c.cur[(size_t)g * ns + is];
+            double sfc = c.sflux[(size_t)g * ns + is];
+            double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
+            double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
+            dh = (j + dt * (fr - fl)) / (fl + fr);
+            if (!isfinite(dh)) dh = 0.0;
+            sh = (c1 >= 0) ? (sfc - stil * fl - (1.0 - stil) * fr) / (fl + fr) : (sfc - stil * fr) / fr;
+        }
+        c.d_tilde[idx] = dt;
+        c.s_tilde[idx] = stil;
+        c.d_hat[idx] = dh;
+        c.s_hat[idx] = sh;
+    }
+    B.sync();
+    // 5-point operator per group (cmfd.cpp:506-544)
+    for (int idx = threadIdx.x; idx < G * n; idx += blockDim.x) {
+        int g = idx / n, i = idx % n;
+        const double *dt = c.d_tilde + (size_t)g * ns;
+        const double *dh = c.d_hat + (size_t)g * ns;
+        double diag = cell_vol(c, i) * c.xsrm[(size_t)i * G + g];
+        const int surfs[6] = {EAST, NORTH, WEST, SOUTH, TOP, BOTTOM};
+        for (int k6 = 0; k6 < 6; k6++) {
+            int s = surfs[k6];
+            int sf = coarse_surf(c, i, s);
+            double h = dh[sf];
+            if (s == WEST || s == SOUTH || s == BOTTOM) h = -h;
+            diag += area(c, i, s) * (dt[sf] + h);
+        }
+        double *m = c.mat + (size_t)g * 5 * n;
+        m[i] = diag;
+        const int offs[4] = {WEST, EAST, SOUTH, NORTH};
+        for (int q = 0; q < 4; q++) {
+            int s = offs[q];
+            double v = 0.0;
+            if (neighbor(c, i, s) >= 0) {
+                int sf = coarse_surf(c, i, s);
+                double h = dh[sf];
+                if (s == WEST || s == SOUTH) h = -h;
+                v = area(c, i, s) * (h - dt[sf]);
+            }
+            m[(size_t)(q + 1) * n + i] = v;
+        }
+    }
+    B.sync();
+
+    fission_source(c, k);
+    B.sync();
+    double tfis = total_fission(c, B);
+    double r0 = 0.0;
+    for (int g = 0; g < G; g++) {
+        build_source(c, g, b);
+        B.sync();
+        r0 += residual_g(c, B, c.mat + (size_t)g * 5 * n, c.flux + (size_t)g * n, b);
+    }
+    r0 = sqrt(r0) / (double)(n * G);
+    const double tol = c.resid_reduction * r0;
+
+    int iter = 0, bic_its = 0;
+    double psi_err = 1.0, ri = 0.0, k_old = k;
+    while (true) {
+        iter++;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) c.fs_old[i] = c.fs[i];
+        B.sync();
+        fission_source(c, k);
+        double tfis_old = tfis;
+        ri = 0.0;
+        for (int g = 0; g < G; g++) {
+            const double *m = c.mat + (size_t)g * 5 * n;
+            double *fg = c.flux + (size_t)g * n;
+            B.sync();
+            build_source(c, g, b);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = fg[i];
+            B.sync();
+            ri += residual_g(c, B, m, x, b);
+            bic_its += bicgstab(c, B, m, b, x, tol, 150, w);
+            for (int i = threadIdx.x; i < n; i += blockDim.x) fg[i] = x[i];
+        }
+        B.sync();
+        ri = sqrt(ri) / (double)(n * G);
+        tfis = total_fission(c, B);
+        k_old = k;
+        k = k * tfis / tfis_old;
+        double pe = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double e = c.fs[i] - c.fs_old[i];
+            pe += e * e;
+        }
+        psi_err = sqrt(B.sum(pe));
+        if ((fabs(k - k_old) < c.k_tol && psi_err < c.psi_tol && ri / r0 < c.resid_reduction) || iter > c.max_iter)
+            break;
+    }
+    for (int i = threadIdx.x; i < n * G; i += blockDim.x)
+        if (c.flux[i] < 0.0) c.flux[i] = -c.flux[i];
+    B.sync();
+    if (threadIdx.x == 0) {
+        *c.k = k;
+        c.stats[0] = iter;
+        c.stats[1] = r0;
+        c.stats[2] = ri / r0;
+        c.stats[3] = psi_err;
+        c.stats[4] = bic_its;
+        if (!isfinite(k)) atomicOr(c.status, (unsigned)DEV_NAN);
+    }
+}
+
+void note_launch_external();
+
+void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
+{
+    int nw = (c.n_cell + 255) / 256;
+    if (c.n_cell <= 512) nw = 1;
+    nw = nw < 1 ? 1 : (nw > 16 ? 16 : nw);
+    size_t vec_bytes = (size_t)10 * c.n_cell * sizeof(double);
+    int in_smem = (vec_bytes + 128 * sizeof(double)) <= 200 * 1024 ? 1 : 0;
+    size_t smem = 128 * sizeof(double) + (in_smem ? vec_bytes : 0);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(k_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    note_launch_external();
+    k_cmfd_solve<<<1, 32 * nw, smem, s>>>(c, in_smem);
+}
+
+} // namespace mocgpu

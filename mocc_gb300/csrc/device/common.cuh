@@ -92,4 +92,32 @@ __device__ __forceinline__ double block_sum(double v, double *scratch)
     return r;
 }
 
+// Two block-wide sums at once; scratch needs 64 doubles.
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *scratch)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    a = warp_sum(a);
+    b = warp_sum(b);
+    __syncthreads();
+    if (lane == 0) {
+        scratch[wid] = a;
+        scratch[32 + wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double ta = (lane < nw) ? scratch[lane] : 0.0;
+        double tb = (lane < nw) ? scratch[32 + lane] : 0.0;
+        ta = warp_sum(ta);
+        tb = warp_sum(tb);
+        if (lane == 0) {
+            scratch[0] = ta;
+            scratch[32] = tb;
+        }
+    }
+    __syncthreads();
+    a = scratch[0];
+    b = scratch[32];
+    __syncthreads();
+}
+
 } // namespace mocgpu

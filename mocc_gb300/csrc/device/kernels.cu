@@ -15,6 +15,7 @@ constexpr double kFpi = 4.0 * 3.1415926535897932;
 static std::atomic<int64_t> g_launches{0};
 static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(); }
+void note_launch_external() { note_launch(); }
 
 // ---------------------------------------------------------------------------
 __global__ void k_fill(double *p, double v, int64_t n)
@@ -482,404 +483,6 @@ void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, 
 }
 
 // ---------------------------------------------------------------------------
-// CMFD on the pin mesh (cmfd.cpp:171-666): coefficient build, then the CMFD
-// power iteration with one preconditioned BiCGSTAB solve per group. One CTA
-// runs the whole solve; all vectors live in global memory (L2 resident).
-namespace cm {
-__device__ __forceinline__ int cell_of(const CmfdView &c, int ix, int iy) { return iy * c.nx + ix; }
-__device__ int coarse_surf(const CmfdView &c, int cell, int s)
-{
-    const int nx = c.nx, ny = c.ny;
-    int ix = cell % nx, iy = cell / nx;
-    int nxy = (nx + 1) * ny + (ny + 1) * nx;
-    switch (s) {
-    case EAST: return (nx + 1) * iy + ix + 1 + nx * ny;
-    case WEST: return (nx + 1) * iy + ix + nx * ny;
-    case NORTH: return nx * ny + (nx + 1) * ny + (ny + 1) * ix + iy + 1;
-    case SOUTH: return (nx + 1) * ny + (ny + 1) * ix + iy + nx * ny;
-    case BOTTOM: return nx * iy + ix;
-    default: return nx * ny + nxy + nx * iy + ix; // TOP
-    }
-}
-__device__ int neighbor(const CmfdView &c, int cell, int s)
-{
-    int ix = cell % c.nx, iy = cell / c.nx;
-    switch (s) {
-    case NORTH: return iy < c.ny - 1 ? cell + c.nx : -1;
-    case SOUTH: return iy > 0 ? cell - c.nx : -1;
-    case EAST: return ix < c.nx - 1 ? cell + 1 : -1;
-    case WEST: return ix > 0 ? cell - 1 : -1;
-    default: return -1;
-    }
-}
-__device__ double area(const CmfdView &c, int cell, int s)
-{
-    int ix = cell % c.nx, iy = cell / c.nx;
-    if (s == EAST || s == WEST) return c.dy[iy] * c.hz;
-    if (s == NORTH || s == SOUTH) return c.dx[ix] * c.hz;
-    return c.dx[ix] * c.dy[iy];
-}
-// surface -> (low cell, high cell, normal, thickness direction)
-__device__ void surf_info(const CmfdView &c, int surf, int &c1, int &c2, int &nrm)
-{
-    const int nx = c.nx, ny = c.ny;
-    int nsz = nx * ny + (nx + 1) * ny + (ny + 1) * nx;
-    int s = surf % nsz;
-    int iz = surf / nsz;
-    if (s < nx * ny) {
-        nrm = Z_NORM;
-        c1 = (iz > 0) ? s : -1;
-        c2 = (iz < 1) ? s : -1;
-    } else if (s < nx * ny + (nx + 1) * ny) {
-        nrm = X_NORM;
-        int t = s - nx * ny;
-        int iy = t / (nx + 1), ix = t % (nx + 1);
-        c1 = ix > 0 ? cell_of(c, ix - 1, iy) : -1;
-        c2 = ix < nx ? cell_of(c, ix, iy) : -1;
-    } else {
-        nrm = Y_NORM;
-        int t = s - nx * ny - (nx + 1) * ny;
-        int iy = t % (ny + 1), ix = t / (ny + 1);
-        c1 = iy > 0 ? cell_of(c, ix, iy - 1) : -1;
-        c2 = iy < ny ? cell_of(c, ix, iy) : -1;
-    }
-}
-__device__ double thickness(const CmfdView &c, int cell, int nrm)
-{
-    if (nrm == X_NORM) return c.dx[cell % c.nx];
-    if (nrm == Y_NORM) return c.dy[cell / c.nx];
-    return c.hz;
-}
-__device__ double bc_diffusivity(int type)
-{
-    return (type == (int)BoundaryType::VACUUM) ? 0.5 / 2.0 : 0.0;
-}
-
-__device__ void spmv(const CmfdView &c, const double *m, const double *x, double *y)
-{
-    const int n = c.n_cell, nx = c.nx;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = m[i] * x[i];
-        int ix = i % nx;
-        if (ix > 0) v += m[n + i] * x[i - 1];
-        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
-        if (i >= nx) v += m[3 * n + i] * x[i - nx];
-        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
-        y[i] = v;
-    }
-}
-
-__device__ void block_sum2(double &a, double &b, double *scratch)
-{
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    a = warp_sum(a);
-    b = warp_sum(b);
-    __syncthreads();
-    if (lane == 0) {
-        scratch[wid] = a;
-        scratch[32 + wid] = b;
-    }
-    __syncthreads();
-    if (wid == 0) {
-        double ta = (lane < nw) ? scratch[lane] : 0.0;
-        double tb = (lane < nw) ? scratch[32 + lane] : 0.0;
-        ta = warp_sum(ta);
-        tb = warp_sum(tb);
-        if (lane == 0) {
-            scratch[0] = ta;
-            scratch[32] = tb;
-        }
-    }
-    __syncthreads();
-    a = scratch[0];
-    b = scratch[32];
-    __syncthreads();
-}
-
-// b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
-__device__ void build_source(const CmfdView &c, int g, double *b)
-{
-    const int n = c.n_cell, G = c.G;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double s = c.xsch[(size_t)i * G + g] * c.fs[i];
-        const double *row = c.scat + ((size_t)i * G + g) * G;
-        for (int gg = 0; gg < G; gg++)
-            if (gg != g) s += row[gg] * c.flux[(size_t)gg * n + i];
-        double vol = c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz;
-        b[i] = s * vol;
-    }
-}
-
-// Preconditioned BiCGSTAB (van der Vorst 1992) with a diagonal (Jacobi)
-// preconditioner, stopping on ||r||^2 <= tol^2 ||b||^2 or max_it
-// iterations, restarting the shadow residual when it becomes orthogonal.
-__device__ int bicgstab(const CmfdView &c, const double *m, const double *b, double *x, double tol, int max_it,
-                        double *w, double *scratch)
-{
-    const int n = c.n_cell;
-    double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *y = w + 4 * n, *z = w + 5 * n, *s = w + 6 * n,
-           *t = w + 7 * n;
-    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
-    spmv(c, m, x, r);
-    __syncthreads();
-    double rr = 0.0, bb = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double ri = b[i] - r[i];
-        r[i] = ri;
-        r0[i] = ri;
-        p[i] = 0.0;
-        v[i] = 0.0;
-        rr += ri * ri;
-        bb += b[i] * b[i];
-    }
-    block_sum2(rr, bb, scratch);
-    if (bb == 0.0) {
-        for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 0.0;
-        __syncthreads();
-        return 0;
-    }
-    double r0_sq = rr;
-    double rho = 1.0, alpha = 1.0, om = 1.0;
-    const double tol2 = tol * tol * bb;
-    int it = 0, restarts = 0;
-    double rho_new = rr; // r0 . r with r0 == r
-    while (rr > tol2 && it < max_it) {
-        double rho_old = rho;
-        rho = rho_new;
-        if (fabs(rho) < eps2 * r0_sq) {
-            spmv(c, m, x, r);
-            __syncthreads();
-            double acc = 0.0, dummy = 0.0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double ri = b[i] - r[i];
-                r[i] = ri;
-                r0[i] = ri;
-                acc += ri * ri;
-            }
-            block_sum2(acc, dummy, scratch);
-            rho = r0_sq = acc;
-            if (restarts++ == 0) it = 0;
-        }
-        double beta = (rho / rho_old) * (alpha / om);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double pi = r[i] + beta * (p[i] - om * v[i]);
-            p[i] = pi;
-            double d = m[i];
-            y[i] = pi / (d != 0.0 ? d : 1.0);
-        }
-        __syncthreads();
-        spmv(c, m, y, v);
-        __syncthreads();
-        double r0v = 0.0, dummy = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) r0v += r0[i] * v[i];
-        block_sum2(r0v, dummy, scratch);
-        alpha = rho / r0v;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double si = r[i] - alpha * v[i];
-            s[i] = si;
-            double d = m[i];
-            z[i] = si / (d != 0.0 ? d : 1.0);
-        }
-        __syncthreads();
-        spmv(c, m, z, t);
-        __syncthreads();
-        double tt = 0.0, ts = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            tt += t[i] * t[i];
-            ts += t[i] * s[i];
-        }
-        block_sum2(tt, ts, scratch);
-        om = (tt > 0.0) ? ts / tt : 0.0;
-        double nrr = 0.0, nrho = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            x[i] += alpha * y[i] + om * z[i];
-            double ri = s[i] - om * t[i];
-            r[i] = ri;
-            nrr += ri * ri;
-            nrho += r0[i] * ri;
-        }
-        block_sum2(nrr, nrho, scratch);
-        rr = nrr;
-        rho_new = nrho;
-        it++;
-    }
-    return it;
-}
-
-__device__ double fission_source(const CmfdView &c, double k)
-{
-    const int n = c.n_cell, G = c.G;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double f = 0.0;
-        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
-        c.fs[i] = f * (1.0 / k);
-    }
-    __syncthreads();
-    return 0.0;
-}
-
-__device__ double total_fission(const CmfdView &c, double *scratch)
-{
-    const int n = c.n_cell, G = c.G;
-    double f = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
-    return block_sum(f, scratch);
-}
-
-// ||M_g x - b_g||^2 with x = current group flux
-__device__ double residual_g(const CmfdView &c, int g, const double *b, double *tmp, double *scratch)
-{
-    const int n = c.n_cell;
-    const double *m = c.mat + (size_t)g * 5 * n;
-    const double *x = c.flux + (size_t)g * n;
-    spmv(c, m, x, tmp);
-    __syncthreads();
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double d = tmp[i] - b[i];
-        acc += d * d;
-    }
-    return block_sum(acc, scratch);
-}
-} // namespace cm
-
-__global__ void __launch_bounds__(1024) k_cmfd_solve(CmfdView c)
-{
-    __shared__ double scratch[64];
-    const int n = c.n_cell, G = c.G, ns = c.n_surf;
-    double k = *c.k;
-    if (c.fixup)
-        for (int i = threadIdx.x; i < n * G; i += blockDim.x) c.flux[i] = fmax(c.flux[i], 0.0);
-    __syncthreads();
-
-    // surface coupling coefficients (cmfd.cpp:404-499)
-    for (int idx = threadIdx.x; idx < G * ns; idx += blockDim.x) {
-        int g = idx / ns, is = idx % ns;
-        int c1, c2, nrm;
-        cm::surf_info(c, is, c1, c2, nrm);
-        int lo_bc = (nrm == X_NORM) ? c.bc[WEST] : (nrm == Y_NORM) ? c.bc[SOUTH] : c.bc[BOTTOM];
-        int hi_bc = (nrm == X_NORM) ? c.bc[EAST] : (nrm == Y_NORM) ? c.bc[NORTH] : c.bc[TOP];
-        double d1 = (c1 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c1 * G + g])) / cm::thickness(c, c1, nrm)
-                              : cm::bc_diffusivity(lo_bc);
-        double d2 = (c2 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c2 * G + g])) / cm::thickness(c, c2, nrm)
-                              : cm::bc_diffusivity(hi_bc);
-        double dt = 2.0 * d1 * d2 / (d1 + d2);
-        double stil = (d1 > 0.0) ? d1 / (d1 + d2) : d2 / (d1 + d2);
-        double dh = 0.0, sh = 0.0;
-        bool have = (nrm != Z_NORM) && c.has_radial;
-        if (have) {
-            double j = c.cur[(size_t)g * ns + is];
-            double sfc = c.sflux[(size_t)g * ns + is];
-            double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
-            double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
-            dh = (j + dt * (fr - fl)) / (fl + fr);
-            if (!isfinite(dh)) dh = 0.0;
-            sh = (c1 >= 0) ? (sfc - stil * fl - (1.0 - stil) * fr) / (fl + fr) : (sfc - stil * fr) / fr;
-        }
-        c.d_tilde[idx] = dt;
-        c.s_tilde[idx] = stil;
-        c.d_hat[idx] = dh;
-        c.s_hat[idx] = sh;
-    }
-    __syncthreads();
-    // 5-point operator per group (cmfd.cpp:506-544)
-    for (int idx = threadIdx.x; idx < G * n; idx += blockDim.x) {
-        int g = idx / n, i = idx % n;
-        const double *dt = c.d_tilde + (size_t)g * ns;
-        const double *dh = c.d_hat + (size_t)g * ns;
-        double vol = c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz;
-        double diag = vol * c.xsrm[(size_t)i * G + g];
-        const int surfs[6] = {EAST, NORTH, WEST, SOUTH, TOP, BOTTOM};
-        for (int k6 = 0; k6 < 6; k6++) {
-            int s = surfs[k6];
-            int sf = cm::coarse_surf(c, i, s);
-            double a = cm::area(c, i, s);
-            double h = dh[sf];
-            if (s == WEST || s == SOUTH || s == BOTTOM) h = -h;
-            diag += a * (dt[sf] + h);
-        }
-        double *m = c.mat + (size_t)g * 5 * n;
-        m[i] = diag;
-        const int offs[4] = {WEST, EAST, SOUTH, NORTH};
-        for (int q = 0; q < 4; q++) {
-            int s = offs[q];
-            double v = 0.0;
-            if (cm::neighbor(c, i, s) >= 0) {
-                int sf = cm::coarse_surf(c, i, s);
-                double a = cm::area(c, i, s);
-                double h = dh[sf];
-                if (s == WEST || s == SOUTH) h = -h;
-                v = a * (h - dt[sf]);
-            }
-            m[(size_t)(q + 1) * n + i] = v;
-        }
-    }
-    __syncthreads();
-
-    double *b = c.vec, *tmp = c.vec + n, *work = c.vec + 2 * n;
-    cm::fission_source(c, k);
-    double tfis = cm::total_fission(c, scratch);
-    double r0 = 0.0;
-    for (int g = 0; g < G; g++) {
-        cm::build_source(c, g, b);
-        __syncthreads();
-        r0 += cm::residual_g(c, g, b, tmp, scratch);
-    }
-    r0 = sqrt(r0) / (double)(n * G);
-    const double tol = c.resid_reduction * r0;
-
-    int iter = 0, bic_its = 0;
-    double psi_err = 1.0, ri = 0.0, k_old = k;
-    while (true) {
-        iter++;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) c.fs_old[i] = c.fs[i];
-        __syncthreads();
-        cm::fission_source(c, k);
-        double tfis_old = tfis;
-        ri = 0.0;
-        for (int g = 0; g < G; g++) {
-            cm::build_source(c, g, b);
-            __syncthreads();
-            ri += cm::residual_g(c, g, b, tmp, scratch);
-            bic_its += cm::bicgstab(c, c.mat + (size_t)g * 5 * n, b, c.flux + (size_t)g * n, tol, 150, work, scratch);
-            __syncthreads();
-        }
-        ri = sqrt(ri) / (double)(n * G);
-        tfis = cm::total_fission(c, scratch);
-        k_old = k;
-        k = k * tfis / tfis_old;
-        double pe = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double e = c.fs[i] - c.fs_old[i];
-            pe += e * e;
-        }
-        psi_err = sqrt(block_sum(pe, scratch));
-        if ((fabs(k - k_old) < c.k_tol && psi_err < c.psi_tol && ri / r0 < c.resid_reduction) || iter > c.max_iter)
-            break;
-    }
-    for (int i = threadIdx.x; i < n * G; i += blockDim.x)
-        if (c.flux[i] < 0.0) c.flux[i] = -c.flux[i];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        *c.k = k;
-        c.stats[0] = iter;
-        c.stats[1] = r0;
-        c.stats[2] = ri / r0;
-        c.stats[3] = psi_err;
-        c.stats[4] = bic_its;
-        if (iter > c.max_iter) atomicOr(c.status, (unsigned)DEV_CMFD_NOT_CONVERGED);
-        if (!isfinite(k)) atomicOr(c.status, (unsigned)DEV_NAN);
-    }
-}
-void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
-{
-    int threads = 1024;
-    if (c.n_cell < 1024) threads = ((c.n_cell + 31) / 32) * 32 < 128 ? 128 : ((c.n_cell + 31) / 32) * 32;
-    { note_launch(); k_cmfd_solve<<<1, threads, 0, s>>>(c); }
-}
-
-// ---------------------------------------------------------------------------
 // Fission-source change after MOCC's Normalize() of both vectors
 // (eigen_solver.cpp:171-184, util/utils.hpp:29-51). red[0..3] receive
 // (count>0, sum) of fs and fs_prev; red[4] the squared difference.
@@ -894,8 +497,8 @@ __global__ void k_psi_err_sums(GeomView g, const double *fs, const double *fp, d
         if (b > 0.0) nb += 1.0;
         sb += b;
     }
-    cm::block_sum2(na, sa, scratch);
-    cm::block_sum2(nb, sb, scratch);
+    block_sum2(na, sa, scratch);
+    block_sum2(nb, sb, scratch);
     if (threadIdx.x == 0) {
         atomicAdd(red + 0, na);
         atomicAdd(red + 1, sa);

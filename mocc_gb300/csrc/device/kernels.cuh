@@ -79,7 +79,27 @@ struct CmfdView {
     unsigned *status;
 };
 
+// Bundled work-unit layout of the fast sweep (see host/layout.hpp).
+struct WorkUnitDev {
+    int set, bundle_begin, n_bundles, fsr_begin, n_local;
+};
+struct FastView {
+    const WorkUnitDev *wu;
+    const int64_t *bundle_row;
+    const int *bundle_nrows, *bundle_track;
+    const void *len; // Real [rows][32]
+    const uint16_t *lfsr;
+    const int *local_fsr;
+    int bundles_per_unit; // warps per CTA = bundles_per_unit * (split ? 2 : 1)
+    int split;            // forward and backward on separate warps
+    int max_local;
+};
+
 // ---- launchers (stream-ordered) ----
+template <typename Real>
+void launch_sweep_fast(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,
+                       bool gs, bool currents, cudaStream_t s);
+template <typename Real> size_t fast_sweep_smem(const FastView &fv);
 void launch_fill(double *p, double v, int64_t n, cudaStream_t s);
 template <typename Real> void launch_fill_real(Real *p, double v, int64_t n, cudaStream_t s);
 void launch_fission_source(const GeomView &g, const StateView &st, double k, cudaStream_t s);

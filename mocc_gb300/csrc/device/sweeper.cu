@@ -185,6 +185,44 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream)
     }
     phaseA_end_ = f.set_first_track[sets_oct];
 
+    // --- bundled work-unit layout (two Gauss-Seidel phases) -----------------
+    {
+        int tracks_phase = f.set_first_track[sets_oct];
+        int tpu = 32 * std::max(1, std::min(8, tracks_phase / (2 * 152 * 32)));
+        int max_local = (precision_ == 0) ? 8192 : 16384;
+        SweepLayout L = build_sweep_layout(f, true, tpu, max_local);
+        std::vector<WorkUnitDev> wud(L.wu.size());
+        for (size_t i = 0; i < L.wu.size(); i++)
+            wud[i] = WorkUnitDev{L.wu[i].set, L.wu[i].bundle_begin, L.wu[i].n_bundles, L.wu[i].fsr_begin,
+                                 L.wu[i].n_local};
+        wu_.upload(wud);
+        bundle_row_.upload(L.bundle_row);
+        bundle_nrows_.upload(L.bundle_nrows);
+        bundle_track_.upload(L.bundle_track);
+        local_fsr_.upload(L.local_fsr);
+        blfsr_.upload(L.lfsr);
+        if (precision_ == 0) blen_d_.upload(L.len);
+        else {
+            std::vector<float> lf(L.len.begin(), L.len.end());
+            blen_f_.upload(lf);
+        }
+        phase_wu_ = L.phase_wu_begin;
+        fv_.wu = wu_.p;
+        fv_.bundle_row = bundle_row_.p;
+        fv_.bundle_nrows = bundle_nrows_.p;
+        fv_.bundle_track = bundle_track_.p;
+        fv_.len = precision_ == 0 ? (const void *)blen_d_.p : (const void *)blen_f_.p;
+        fv_.lfsr = blfsr_.p;
+        fv_.local_fsr = local_fsr_.p;
+        fv_.bundles_per_unit = tpu / 32;
+        fv_.split = 1;
+        fv_.max_local = L.max_local;
+        layout_padding = L.padding;
+        layout_units = (int)L.wu.size();
+        layout_max_local = L.max_local;
+        layout_tracks_per_unit = tpu;
+    }
+
     // --- upload ---------------------------------------------------------------
     seg_begin_.upload(f.trk_seg_begin);
     trk_bc0_.upload(f.trk_bc0);
@@ -436,10 +474,20 @@ void Sweeper::group_source(int g)
     else launch_group_source<float>(gv_, sv_, g, stream_);
 }
 
-void Sweeper::launch_sweep_pass(int g, int t0, int t1, bool gs, bool cur)
+// phase 0: octant-1 track sets, 1: octant-2 track sets, -1: all (Jacobi)
+void Sweeper::launch_phase(int g, int phase, bool gs, bool cur)
 {
-    if (precision_ == 0) launch_sweep<double>(gv_, sv_, g, t0, t1, gs, cur, stream_);
-    else launch_sweep<float>(gv_, sv_, g, t0, t1, gs, cur, stream_);
+    if (opts_.sweep_kernel == 0) {
+        int t0 = (phase == 1) ? phaseA_end_ : 0;
+        int t1 = (phase == 0) ? phaseA_end_ : f_.n_tracks;
+        if (precision_ == 0) launch_sweep<double>(gv_, sv_, g, t0, t1, gs, cur, stream_);
+        else launch_sweep<float>(gv_, sv_, g, t0, t1, gs, cur, stream_);
+    } else {
+        int w0 = (phase == 1) ? phase_wu_[1] : 0;
+        int w1 = (phase == 0) ? phase_wu_[1] : phase_wu_[2];
+        if (precision_ == 0) launch_sweep_fast<double>(gv_, fv_, sv_, g, w0, w1, gs, cur, stream_);
+        else launch_sweep_fast<float>(gv_, fv_, sv_, g, w0, w1, gs, cur, stream_);
+    }
 }
 
 void Sweeper::launch_epilogue(int g, bool update_q)
@@ -459,10 +507,10 @@ void Sweeper::sweep(int g)
         bool cur = last && coarse_enabled_;
         if (cur) launch_zero_radial_currents(gv_, sv_, g, stream_);
         if (opts_.gs_boundary) {
-            launch_sweep_pass(g, 0, phaseA_end_, true, cur);
-            launch_sweep_pass(g, phaseA_end_, f_.n_tracks, true, cur);
+            launch_phase(g, 0, true, cur);
+            launch_phase(g, 1, true, cur);
         } else {
-            launch_sweep_pass(g, 0, f_.n_tracks, false, cur);
+            launch_phase(g, -1, false, cur);
             if (precision_ == 0) launch_jacobi_update<double>(gv_, sv_, g, stream_);
             else launch_jacobi_update<float>(gv_, sv_, g, stream_);
         }
@@ -485,11 +533,11 @@ double Sweeper::time_sweep(int g, int reps, int *launches)
     for (int r = 0; r < reps; r++) {
         MOCGPU_CUDA(cudaEventRecord(e0, stream_));
         if (opts_.gs_boundary) {
-            launch_sweep_pass(g, 0, phaseA_end_, true, false);
-            launch_sweep_pass(g, phaseA_end_, f_.n_tracks, true, false);
+            launch_phase(g, 0, true, false);
+            launch_phase(g, 1, true, false);
             nl += 2;
         } else {
-            launch_sweep_pass(g, 0, f_.n_tracks, false, false);
+            launch_phase(g, -1, false, false);
             nl += 1;
         }
         MOCGPU_CUDA(cudaEventRecord(e1, stream_));

@@ -10,6 +10,7 @@
 #include <memory>
 #include <vector>
 
+#include "../host/layout.hpp"
 #include "../host/problem.hpp"
 #include "kernels.cuh"
 
@@ -83,7 +84,7 @@ class Sweeper {
   private:
     template <typename Real> void sweep_impl(int g);
     void check_status();
-    void launch_sweep_pass(int g, int t0, int t1, bool gs, bool cur);
+    void launch_phase(int g, int phase, bool gs, bool cur);
     void launch_epilogue(int g, bool update_q);
 
     FlatProblem f_;
@@ -114,6 +115,21 @@ class Sweeper {
     DevBuf<double> cflux_, hxs_, hscat_, dtil_, dhat_, stil_, shat_, cmat_, cfs_, cfs_old_, cvec_, ck_, cstats_;
     DevBuf<double> pinbuf_;
     std::vector<double> psi_init_;
+    // bundled work-unit layout
+    DevBuf<WorkUnitDev> wu_;
+    DevBuf<int64_t> bundle_row_;
+    DevBuf<int> bundle_nrows_, bundle_track_, local_fsr_;
+    DevBuf<float> blen_f_;
+    DevBuf<double> blen_d_;
+    DevBuf<uint16_t> blfsr_;
+    std::vector<int> phase_wu_;
+    FastView fv_{};
+
+  public:
+    double layout_padding = 0.0;
+    int layout_units = 0, layout_max_local = 0, layout_tracks_per_unit = 0;
+
+  private:
 
     GeomView gv_{};
     StateView sv_{};

@@ -1,0 +1,107 @@
+#include "layout.hpp"
+
+#include <algorithm>
+#include <numeric>
+#include <unordered_map>
+
+namespace mocgpu {
+
+SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local)
+{
+    SweepLayout L;
+    const int W = SweepLayout::kLanes;
+    if (tracks_per_unit < W) tracks_per_unit = W;
+    tracks_per_unit = (tracks_per_unit / W) * W;
+    if (max_local > 65535) max_local = 65535;
+    const int sets_oct = f.n_sets / 2;
+    std::vector<std::vector<int>> phases;
+    if (gs) {
+        phases.resize(2);
+        for (int s = 0; s < f.n_sets; s++) phases[s < sets_oct ? 0 : 1].push_back(s);
+    } else {
+        phases.resize(1);
+        for (int s = 0; s < f.n_sets; s++) phases[0].push_back(s);
+    }
+    L.n_phases = (int)phases.size();
+    int64_t real = 0, padded = 0;
+    std::vector<int> mark(f.n_fsr, -1);
+    int stamp = 0;
+    for (const auto &ph : phases) {
+        L.phase_wu_begin.push_back((int)L.wu.size());
+        for (int s : ph) {
+            int t0 = f.set_first_track[s], t1 = f.set_first_track[s + 1];
+            int t = t0;
+            while (t < t1) {
+                // grow the unit while it stays within both caps
+                std::vector<int> tracks, fsrs;
+                stamp++;
+                while (t < t1 && (int)tracks.size() < tracks_per_unit) {
+                    int added = 0;
+                    for (int64_t k = f.trk_seg_begin[t]; k < f.trk_seg_begin[t + 1]; k++)
+                        if (mark[f.seg_fsr[k]] != stamp) added++;
+                    if (!tracks.empty() && (int)fsrs.size() + added > max_local) break;
+                    if ((int)fsrs.size() + added > max_local)
+                        MOCGPU_THROW(6, "a single track touches more FSRs than a work unit can hold");
+                    for (int64_t k = f.trk_seg_begin[t]; k < f.trk_seg_begin[t + 1]; k++)
+                        if (mark[f.seg_fsr[k]] != stamp) {
+                            mark[f.seg_fsr[k]] = stamp;
+                            fsrs.push_back(f.seg_fsr[k]);
+                        }
+                    tracks.push_back(t);
+                    t++;
+                }
+                std::sort(fsrs.begin(), fsrs.end());
+                std::unordered_map<int, int> loc;
+                loc.reserve(fsrs.size() * 2);
+                for (size_t i = 0; i < fsrs.size(); i++) loc[fsrs[i]] = (int)i;
+                WorkUnitHost u;
+                u.set = s;
+                u.bundle_begin = (int)L.bundle_row.size();
+                u.fsr_begin = (int)L.local_fsr.size();
+                u.n_local = (int)fsrs.size();
+                L.local_fsr.insert(L.local_fsr.end(), fsrs.begin(), fsrs.end());
+                L.max_local = std::max(L.max_local, u.n_local);
+                // longest first, bundles of W
+                std::stable_sort(tracks.begin(), tracks.end(), [&](int a, int b) {
+                    return (f.trk_seg_begin[a + 1] - f.trk_seg_begin[a]) > (f.trk_seg_begin[b + 1] - f.trk_seg_begin[b]);
+                });
+                for (size_t b0 = 0; b0 < tracks.size(); b0 += W) {
+                    int nrows = 0;
+                    for (size_t j = b0; j < std::min(tracks.size(), b0 + W); j++)
+                        nrows = std::max<int>(nrows, (int)(f.trk_seg_begin[tracks[j] + 1] - f.trk_seg_begin[tracks[j]]));
+                    L.bundle_row.push_back(L.n_rows);
+                    L.bundle_nrows.push_back(nrows);
+                    size_t base = L.len.size();
+                    L.len.resize(base + (size_t)nrows * W, 0.0);
+                    L.lfsr.resize(base + (size_t)nrows * W, 0);
+                    for (int lane = 0; lane < W; lane++) {
+                        size_t j = b0 + lane;
+                        if (j >= tracks.size()) {
+                            L.bundle_track.push_back(-1);
+                            continue;
+                        }
+                        int tr = tracks[j];
+                        L.bundle_track.push_back(tr);
+                        int64_t a = f.trk_seg_begin[tr];
+                        int n = (int)(f.trk_seg_begin[tr + 1] - a);
+                        for (int r = 0; r < n; r++) {
+                            L.len[base + (size_t)r * W + lane] = f.seg_len[a + r];
+                            L.lfsr[base + (size_t)r * W + lane] = (uint16_t)loc[f.seg_fsr[a + r]];
+                        }
+                        // padding rows keep length 0 and point at the unit's first FSR
+                        real += n;
+                    }
+                    padded += (int64_t)nrows * W;
+                    L.n_rows += nrows;
+                }
+                u.n_bundles = (int)L.bundle_row.size() - u.bundle_begin;
+                L.wu.push_back(u);
+            }
+        }
+    }
+    L.phase_wu_begin.push_back((int)L.wu.size());
+    L.padding = real ? (double)padded / (double)real - 1.0 : 0.0;
+    return L;
+}
+
+} // namespace mocgpu

@@ -61,6 +61,12 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
         else if (p == "mixed" || p == "single" || p == "fp32") o.precision = 1;
         else MOCGPU_THROW(7, "Unrecognized precision option (double|mixed).");
     }
+    if (sweeper->has_attr("kernel")) {
+        std::string k = sanitize(sweeper->attr("kernel"));
+        if (k == "plain") o.sweep_kernel = 0;
+        else if (k == "bundled") o.sweep_kernel = 1;
+        else MOCGPU_THROW(7, "Unrecognized sweep kernel option (plain|bundled).");
+    }
 }
 
 static RaySpec read_rays(const XmlNode &rn)

@@ -28,6 +28,7 @@ struct SolverOptions {
     int n_inner = 1;
     bool gs_boundary = true; // Gauss-Seidel (default) or Jacobi boundary update
     int precision = 0;       // 0: FP64 sweep, 1: FP32 sweep + FP64 reductions/CMFD
+    int sweep_kernel = 1;    // 0: one thread per track (plain), 1: bundled work units
 };
 
 // Flat problem description. Angles cover octants 1-4 (2-D); tracks are

@@ -35,10 +35,11 @@ def _pair(xml, xsl, precision, **opt):
     return P, m.MoCSweeper(P, precision), oracle.OracleSolver(P)
 
 
+@pytest.mark.parametrize("kernel", [0, 1])
 @pytest.mark.parametrize("gs", [1, 0])
 @pytest.mark.parametrize("currents", [False, True])
-def test_group_sweeps_fp64(gs, currents):
-    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs, n_inner=2)
+def test_group_sweeps_fp64(kernel, gs, currents):
+    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs, n_inner=2, sweep_kernel=kernel)
     S.initialize()
     O.initialize()
     S.set_coarse_data(currents)
@@ -65,8 +66,9 @@ def test_group_sweeps_fp64(gs, currents):
         assert np.max(np.abs(sa - sb)) < 1e-10 * np.max(np.abs(sb))
 
 
-def test_group_sweeps_fp32_close():
-    P, S, O = _pair(*W.pin3x3(), 1, n_inner=2)
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_group_sweeps_fp32_close(kernel):
+    P, S, O = _pair(*W.pin3x3(), 1, n_inner=2, sweep_kernel=kernel)
     S.initialize()
     O.initialize()
     fs = O.calc_fission_source(1.0)
@@ -124,9 +126,10 @@ def test_cmfd_solve_fp64():
     assert np.allclose(S.flux(), O.flux(), rtol=1e-8)
 
 
+@pytest.mark.parametrize("kernel", [0, 1])
 @pytest.mark.parametrize("gs", [1, 0])
-def test_eigen_fp64_matches_oracle(gs):
-    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs)
+def test_eigen_fp64_matches_oracle(kernel, gs):
+    P, S, O = _pair(*W.pin3x3(), 0, gs_boundary=gs, sweep_kernel=kernel)
     ra = m.EigenSolver(P, sweeper=S).solve()
     rb = O.solve()
     assert ra["converged"] and rb["converged"]
@@ -172,11 +175,41 @@ def test_ihm_on_gpu(ref_xsl, precision):
         assert np.max(np.abs(S.flux()[:, g] - phi[g])) <= 0.005 * phi[g]
 
 
-def test_assembly17_mixed_vs_oracle():
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_assembly17_mixed_vs_oracle(kernel):
     xml, xsl = W.assembly17()
-    P, S, O = _pair(xml, xsl, 1)
+    P, S, O = _pair(xml, xsl, 1, sweep_kernel=kernel)
     ra = m.EigenSolver(P, sweeper=S).solve()
     rb = O.solve()
     assert ra["converged"] and rb["converged"]
     assert pcm(ra["k"], rb["k"]) < PCM_TOL
     assert max_pin_err(S.pin_powers(), O.pin_powers()) < PIN_TOL
+
+
+def test_small_unit_cap_multi_unit_sweep():
+    """A tiny FSR cap forces many work units per track set; results unchanged."""
+    # the cap is fixed inside the library; a 7x7 lattice at fine spacing
+    # spreads each track set over many units
+    xml, xsl = W.lattice_case(7, 8, 0.02, "double", seed=3)
+    P, S, O = _pair(xml, xsl, 0, n_inner=1)
+    S.initialize()
+    O.initialize()
+    fs = O.calc_fission_source(1.0)
+    S.set_fission_source(fs)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        O.source_group(g)
+        S.sweep(g)
+        O.sweep(g)
+    assert np.max(np.abs(S.flux() - O.flux()) / np.abs(O.flux())) < FP64_TOL
+
+
+def test_time_sweep_reports_launches():
+    P = m.Problem(*W.pin3x3())
+    S = m.MoCSweeper(P, 1)
+    S.initialize()
+    ms, nl = S.time_sweep(0, 3)
+    assert nl == 6 and ms > 0.0
+    before = m.launch_count()
+    S.sweep(0)
+    assert m.launch_count() - before >= 2
