@@ -197,8 +197,7 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             double pi = r[i] + beta * (p[i] - om * v[i]);
             p[i] = pi;
-            double d = m[i];
-            y[i] = pi / (d != 0.0 ? d : 1.0);
+            y[i] = pi * m[5 * n + i];
         }
         B.sync();
         spmv(c, m, y, v);
@@ -209,8 +208,7 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             double si = r[i] - alpha * v[i];
             s[i] = si;
-            double d = m[i];
-            z[i] = si / (d != 0.0 ? d : 1.0);
+            z[i] = si * m[5 * n + i];
         }
         B.sync();
         spmv(c, m, z, t);
@@ -335,8 +333,9 @@ __global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
             if (s == WEST || s == SOUTH || s == BOTTOM) h = -h;
             diag += area(c, i, s) * (dt[sf] + h);
         }
-        double *m = c.mat + (size_t)g * 5 * n;
+        double *m = c.mat + (size_t)g * 6 * n;
         m[i] = diag;
+        m[(size_t)5 * n + i] = (diag != 0.0) ? 1.0 / diag : 1.0; // Jacobi preconditioner
         const int offs[4] = {WEST, EAST, SOUTH, NORTH};
         for (int q = 0; q < 4; q++) {
             int s = offs[q];
@@ -359,7 +358,7 @@ __global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
     for (int g = 0; g < G; g++) {
         build_source(c, g, b);
         B.sync();
-        r0 += residual_g(c, B, c.mat + (size_t)g * 5 * n, c.flux + (size_t)g * n, b);
+        r0 += residual_g(c, B, c.mat + (size_t)g * 6 * n, c.flux + (size_t)g * n, b);
     }
     r0 = sqrt(r0) / (double)(n * G);
     const double tol = c.resid_reduction * r0;
@@ -374,7 +373,7 @@ __global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
         double tfis_old = tfis;
         ri = 0.0;
         for (int g = 0; g < G; g++) {
-            const double *m = c.mat + (size_t)g * 5 * n;
+            const double *m = c.mat + (size_t)g * 6 * n;
             double *fg = c.flux + (size_t)g * n;
             B.sync();
             build_source(c, g, b);

@@ -68,7 +68,7 @@ struct CmfdView {
     double *xstr, *xsnf, *xsf, *xsch, *xsrm;      // [cell][G]
     double *scat;                                 // [cell][G][G] (to, from)
     double *d_tilde, *d_hat, *s_tilde, *s_hat;    // [G][n_surf]
-    double *mat;                                  // [G][5][n_cell]: diag, W, E, S, N
+    double *mat;                                  // [G][6][n_cell]: diag, W, E, S, N, 1/diag
     double *fs, *fs_old, *vec;                    // vec: 10 * n_cell work vectors
     const double *cur, *sflux;                    // [G][n_surf] from the sweep
     int has_radial;

@@ -3,10 +3,11 @@
 //
 // One CTA per work unit. The unit's FSR cross sections and sources are staged
 // into shared memory as (Sigma_t, qbar) pairs and the unit's FSR tally lives
-// in shared memory; one warp sweeps one bundle of 32 tracks, one track per
-// lane, all polar angles of the azimuth in registers. Segment rows are read
-// 32-wide and coalesced. With `split` the forward and the backward pass of a
-// bundle run on two warps; otherwise one lane does both in the same loop.
+// in shared memory; one warp sweeps one bundle of 32 tracks in one direction,
+// one track per lane, all polar angles of the azimuth in registers (the
+// forward and the backward pass of a bundle run on two warps). Each warp
+// streams its bundle's segment rows through a double-buffered shared-memory
+// ring with 16-byte cp.async copies, chunk c+1 landing while chunk c is swept.
 // After the bundles, the unit's tally is added to the global FSR tally with
 // one atomic per touched FSR.
 #include "kernels.cuh"
@@ -15,9 +16,10 @@ namespace mocgpu {
 
 __device__ __forceinline__ double att_fast(double tau, const double *tab)
 {
+    // MOCC's table exponential (exponential.hpp:56-112): [-10, 0], 10000 intervals
     double v = -tau;
     if (v < -10.0 || v > 0.0) return 1.0 - exp(v);
-    const double rspace = 1000.0, space = 1.0e-3; // 10000 intervals on [-10, 0]
+    const double rspace = 1000.0, space = 1.0e-3;
     int i = (int)((v + 10.0) * rspace);
     if (i >= kExpN) i = kExpN - 1;
     v -= space * i - 10.0;
@@ -26,6 +28,7 @@ __device__ __forceinline__ double att_fast(double tau, const double *tab)
 }
 __device__ __forceinline__ float att_fast(float tau, const double *)
 {
+    // 4-term Taylor series of 1 - e^{-tau} below 1/64, hardware exponential above
     if (tau < 0.015625f) return tau * (1.0f - tau * (0.5f - tau * (0.16666667f - tau * 0.041666668f)));
     return 1.0f - __expf(-tau);
 }
@@ -37,14 +40,38 @@ template <> struct Pair<float> {
 template <> struct Pair<double> {
     using T = double2;
 };
+template <typename Real> struct Chunk {
+    static constexpr int rows = sizeof(Real) == 4 ? 32 : 16; // rows per streamed chunk
+};
 
-template <typename Real, int NPOL, bool GS, bool CUR, bool SPLIT>
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Bytes of one warp's ring buffer (two chunks of lengths and local FSR ids).
+template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
+{
+    return 2 * (size_t)Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
+}
+
+template <typename Real, int NPOL, bool GS, bool CUR>
 __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, int wu0)
 {
     using R2 = typename Pair<Real>::T;
+    constexpr int CH = Chunk<Real>::rows;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const WorkUnitDev u = fv.wu[wu0 + blockIdx.x];
-    R2 *s_sq = reinterpret_cast<R2 *>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    // [warp rings][(sigma_t, qbar) pairs][tally]
+    unsigned char *ring = smem_raw + (size_t)warp * ring_bytes<Real>();
+    Real *ring_len = reinterpret_cast<Real *>(ring);                                   // [2][CH][32]
+    uint16_t *ring_fsr = reinterpret_cast<uint16_t *>(ring + 2 * CH * 32 * sizeof(Real)); // [2][CH][32]
+    R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real>());
     Real *s_tal = reinterpret_cast<Real *>(s_sq + fv.max_local);
 
     const Real *sigt = (const Real *)st.sigt;
@@ -56,9 +83,7 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
     }
     __syncthreads();
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = blockDim.x >> 5;
-    const int ntasks = SPLIT ? 2 * u.n_bundles : u.n_bundles;
+    const int ntasks = 2 * u.n_bundles;
     const Real *lenp = (const Real *)fv.len;
     Real *psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
     Real *psi_out = (Real *)st.psi_out;
@@ -85,38 +110,32 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
     double *sfl = st.sflux + (size_t)group * g.n_surf;
 
     for (int task = warp; task < ntasks; task += nwarps) {
-        const int b = u.bundle_begin + (SPLIT ? (task >> 1) : task);
-        const bool do_fwd = SPLIT ? ((task & 1) == 0) : true;
-        const bool do_bwd = SPLIT ? ((task & 1) == 1) : true;
+        const int b = u.bundle_begin + (task >> 1);
+        const bool fwd = (task & 1) == 0;
         const int t = fv.bundle_track[(size_t)b * 32 + lane];
         const int nrows = fv.bundle_nrows[b];
-        const int64_t base = fv.bundle_row[b] * 32 + lane;
-        int n = 0, bc0 = 0, bc1 = 0;
-        Real pf[NPOL], pb[NPOL];
+        const int64_t row0 = fv.bundle_row[b];
+        const int nch = (nrows + CH - 1) / CH;
+        int bc_in = 0, bc_out = 0;
+        const int *angs = fwd ? af : ab;
         if (t >= 0) {
-            n = (int)(g.seg_begin[t + 1] - g.seg_begin[t]);
-            bc0 = g.trk_bc0[t];
-            bc1 = g.trk_bc1[t];
+            bc_in = fwd ? g.trk_bc0[t] : g.trk_bc1[t];
+            bc_out = fwd ? g.trk_bc1[t] : g.trk_bc0[t];
         }
+        Real psi[NPOL];
 #pragma unroll
-        for (int p = 0; p < NPOL; p++) {
-            pf[p] = (t >= 0 && do_fwd) ? psi_in[g.bc_off[af[p]] + bc0] : (Real)0;
-            pb[p] = (t >= 0 && do_bwd) ? psi_in[g.bc_off[ab[p]] + bc1] : (Real)0;
-        }
-        int evf = 0, evf_end = 0, evb = 0, evb_end = 0;
+        for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? psi_in[g.bc_off[angs[p]] + bc_in] : (Real)0;
+        int ev = 0, ev_end = 0;
+        const int *ev_pt = fwd ? g.ev_fw_pt : g.ev_bw_pt;
+        const int *ev_code = fwd ? g.ev_fw_code : g.ev_bw_code;
         if (CUR && t >= 0) {
-            if (do_fwd) {
-                evf = g.ev_fw_begin[t];
-                evf_end = g.ev_fw_begin[t + 1];
-            }
-            if (do_bwd) {
-                evb = g.ev_bw_begin[t];
-                evb_end = g.ev_bw_begin[t + 1];
-            }
+            ev = fwd ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
+            ev_end = fwd ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
         }
-        auto events = [&](const int *pt, const int *code, int &ev, int ev_end, int k, double sign, const Real *psi) {
-            while (ev < ev_end && pt[ev] == k) {
-                int c = code[ev];
+        const double sign = fwd ? 1.0 : -1.0;
+        auto events = [&](int k) {
+            while (ev < ev_end && ev_pt[ev] == k) {
+                int c = ev_code[ev];
                 int surf = c >> 1;
                 bool ynorm = c & 1;
                 double jc = 0.0, fc = 0.0;
@@ -130,90 +149,75 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
                 ev++;
             }
         };
+        // chunk c of this direction covers rows [lo, hi)
+        auto chunk_rows = [&](int c, int &lo, int &hi) {
+            if (fwd) {
+                lo = c * CH;
+                hi = min(nrows, lo + CH);
+            } else {
+                hi = nrows - c * CH;
+                lo = max(0, hi - CH);
+            }
+        };
+        auto issue = [&](int c) {
+            int lo, hi;
+            chunk_rows(c, lo, hi);
+            const int nr = hi - lo;
+            const int buf = c & 1;
+            const char *gl = (const char *)(lenp + (row0 + lo) * 32);
+            char *sl = (char *)(ring_len + (size_t)buf * CH * 32);
+            const int nl = nr * 32 * (int)sizeof(Real) / 16;
+            for (int i = lane; i < nl; i += 32) cp_async16(sl + 16 * i, gl + 16 * i);
+            const char *gf = (const char *)(fv.lfsr + (row0 + lo) * 32);
+            char *sf = (char *)(ring_fsr + (size_t)buf * CH * 32);
+            const int nf = nr * 32 * (int)sizeof(uint16_t) / 16;
+            for (int i = lane; i < nf; i += 32) cp_async16(sf + 16 * i, gf + 16 * i);
+            cp_async_commit();
+        };
 
-        // software pipeline: rows for step r+1 are loaded while step r computes
-        Real Lf = 0, Lb = 0;
-        int lf = 0, lb = 0;
-        if (nrows > 0) {
-            if (do_fwd) {
-                Lf = lenp[base];
-                lf = fv.lfsr[base];
+        if (nch > 0) issue(0);
+        for (int c = 0; c < nch; c++) {
+            if (c + 1 < nch) {
+                issue(c + 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
-            if (do_bwd) {
-                Lb = lenp[base + (int64_t)(nrows - 1) * 32];
-                lb = fv.lfsr[base + (int64_t)(nrows - 1) * 32];
-            }
-        }
-        for (int r = 0; r < nrows; r++) {
-            Real nLf = 0, nLb = 0;
-            int nlf = 0, nlb = 0;
-            if (r + 1 < nrows) {
-                if (do_fwd) {
-                    nLf = lenp[base + (int64_t)(r + 1) * 32];
-                    nlf = fv.lfsr[base + (int64_t)(r + 1) * 32];
-                }
-                if (do_bwd) {
-                    nLb = lenp[base + (int64_t)(nrows - 2 - r) * 32];
-                    nlb = fv.lfsr[base + (int64_t)(nrows - 2 - r) * 32];
-                }
-            }
-            if (do_fwd) {
-                if (CUR && t >= 0) events(g.ev_fw_pt, g.ev_fw_code, evf, evf_end, r, 1.0, pf);
-                const R2 sq = s_sq[lf];
-                const Real tau0 = sq.x * Lf;
+            __syncwarp();
+            int lo, hi;
+            chunk_rows(c, lo, hi);
+            const Real *cl = ring_len + (size_t)(c & 1) * CH * 32;
+            const uint16_t *cf = ring_fsr + (size_t)(c & 1) * CH * 32;
+            const int nr = hi - lo;
+            for (int k = 0; k < nr; k++) {
+                const int j = fwd ? k : nr - 1 - k; // row within the chunk
+                const int row = lo + j;
+                if (CUR && t >= 0) events(fwd ? row : row + 1);
+                const Real L = cl[j * 32 + lane];
+                const int l = cf[j * 32 + lane];
+                const R2 sq = s_sq[l];
+                const Real tau0 = sq.x * L;
                 Real acc = 0;
 #pragma unroll
                 for (int p = 0; p < NPOL; p++) {
                     Real e = att_fast(tau0 * rsin[p], g.exp_tab);
-                    Real d = (pf[p] - sq.y) * e;
-                    pf[p] -= d;
+                    Real d = (psi[p] - sq.y) * e;
+                    psi[p] -= d;
                     acc += d * wt[p];
                 }
-                if (Lf > (Real)0) atomicAdd(s_tal + lf, acc);
+                if (L > (Real)0) atomicAdd(s_tal + l, acc);
             }
-            if (do_bwd) {
-                const int row = nrows - 1 - r;
-                if (CUR && t >= 0) events(g.ev_bw_pt, g.ev_bw_code, evb, evb_end, row + 1, -1.0, pb);
-                const R2 sq = s_sq[lb];
-                const Real tau0 = sq.x * Lb;
-                Real acc = 0;
-#pragma unroll
-                for (int p = 0; p < NPOL; p++) {
-                    Real e = att_fast(tau0 * rsin[p], g.exp_tab);
-                    Real d = (pb[p] - sq.y) * e;
-                    pb[p] -= d;
-                    acc += d * wt[p];
-                }
-                if (Lb > (Real)0) atomicAdd(s_tal + lb, acc);
-            }
-            Lf = nLf;
-            lf = nlf;
-            Lb = nLb;
-            lb = nlb;
+            __syncwarp();
         }
         if (t >= 0) {
-            if (CUR) {
-                if (do_fwd) events(g.ev_fw_pt, g.ev_fw_code, evf, evf_end, nrows, 1.0, pf);
-                if (do_bwd) events(g.ev_bw_pt, g.ev_bw_code, evb, evb_end, 0, -1.0, pb);
-            }
-            (void)n;
+            if (CUR) events(fwd ? nrows : 0);
 #pragma unroll
             for (int p = 0; p < NPOL; p++) {
-                if (do_fwd) {
-                    if (GS) {
-                        int tgt = g.wt_tgt[af[p] * 2 + (bc1 < ny_set ? 0 : 1)];
-                        if (tgt >= 0) psi_in[tgt + bc1] = pf[p];
-                    } else {
-                        psi_out[g.bc_off[af[p]] + bc1] = pf[p];
-                    }
-                }
-                if (do_bwd) {
-                    if (GS) {
-                        int tgt = g.wt_tgt[ab[p] * 2 + (bc0 < ny_set ? 0 : 1)];
-                        if (tgt >= 0) psi_in[tgt + bc0] = pb[p];
-                    } else {
-                        psi_out[g.bc_off[ab[p]] + bc0] = pb[p];
-                    }
+                if (GS) {
+                    int tgt = g.wt_tgt[angs[p] * 2 + (bc_out < ny_set ? 0 : 1)];
+                    if (tgt >= 0) psi_in[tgt + bc_out] = psi[p];
+                } else {
+                    psi_out[g.bc_off[angs[p]] + bc_out] = psi[p];
                 }
             }
         }
@@ -228,23 +232,24 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
 
 template <typename Real> size_t fast_sweep_smem(const FastView &fv)
 {
-    return (size_t)fv.max_local * (3 * sizeof(Real));
+    int nwarps = 2 * fv.bundles_per_unit;
+    return (size_t)nwarps * ring_bytes<Real>() + (size_t)fv.max_local * (3 * sizeof(Real));
 }
 template size_t fast_sweep_smem<float>(const FastView &);
 template size_t fast_sweep_smem<double>(const FastView &);
 
-template <typename Real, int NPOL, bool GS, bool CUR, bool SPLIT>
+template <typename Real, int NPOL, bool GS, bool CUR>
 static void launch_one(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,
                        cudaStream_t s)
 {
-    auto k = k_sweep_fast<Real, NPOL, GS, CUR, SPLIT>;
+    auto k = k_sweep_fast<Real, NPOL, GS, CUR>;
     size_t smem = fast_sweep_smem<Real>(fv);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         MOCGPU_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
     }
-    int threads = 32 * fv.bundles_per_unit * (SPLIT ? 2 : 1);
+    int threads = 64 * fv.bundles_per_unit;
     k<<<wu1 - wu0, threads, smem, s>>>(g, fv, st, group, wu0);
 }
 
@@ -252,20 +257,10 @@ template <typename Real, int NPOL>
 static void launch_np(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1, bool gs,
                       bool cur, cudaStream_t s)
 {
-#define MOCGPU_FAST_CASE(GS_, CUR_, SPLIT_)                                                                           \
-    if (gs == GS_ && cur == CUR_ && (fv.split != 0) == SPLIT_) {                                                     \
-        launch_one<Real, NPOL, GS_, CUR_, SPLIT_>(g, fv, st, group, wu0, wu1, s);                                     \
-        return;                                                                                                      \
-    }
-    MOCGPU_FAST_CASE(true, false, true)
-    MOCGPU_FAST_CASE(true, true, true)
-    MOCGPU_FAST_CASE(false, false, true)
-    MOCGPU_FAST_CASE(false, true, true)
-    MOCGPU_FAST_CASE(true, false, false)
-    MOCGPU_FAST_CASE(true, true, false)
-    MOCGPU_FAST_CASE(false, false, false)
-    MOCGPU_FAST_CASE(false, true, false)
-#undef MOCGPU_FAST_CASE
+    if (gs && !cur) launch_one<Real, NPOL, true, false>(g, fv, st, group, wu0, wu1, s);
+    else if (gs && cur) launch_one<Real, NPOL, true, true>(g, fv, st, group, wu0, wu1, s);
+    else if (!gs && !cur) launch_one<Real, NPOL, false, false>(g, fv, st, group, wu0, wu1, s);
+    else launch_one<Real, NPOL, false, true>(g, fv, st, group, wu0, wu1, s);
 }
 
 void note_launch_external();

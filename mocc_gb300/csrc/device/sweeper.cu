@@ -188,8 +188,10 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream)
     // --- bundled work-unit layout (two Gauss-Seidel phases) -----------------
     {
         int tracks_phase = f.set_first_track[sets_oct];
-        int tpu = 32 * std::max(1, std::min(8, tracks_phase / (2 * 152 * 32)));
-        int max_local = (precision_ == 0) ? 8192 : 16384;
+        // up to 4 bundles (8 warps) per unit; unit FSR sets sized so the
+        // staged pairs, the tally and the warps' segment rings fit in 227 KB
+        int tpu = 32 * std::max(1, std::min(4, tracks_phase / (2 * 152 * 32)));
+        int max_local = (precision_ == 0) ? 4096 : 8192;
         SweepLayout L = build_sweep_layout(f, true, tpu, max_local);
         std::vector<WorkUnitDev> wud(L.wu.size());
         for (size_t i = 0; i < L.wu.size(); i++)
@@ -291,7 +293,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream)
     dhat_.alloc((size_t)G * f.n_surf);
     stil_.alloc((size_t)G * f.n_surf);
     shat_.alloc((size_t)G * f.n_surf);
-    cmat_.alloc((size_t)G * 5 * nc);
+    cmat_.alloc((size_t)G * 6 * nc);
     cfs_.alloc(nc);
     cfs_old_.alloc(nc);
     cvec_.alloc((size_t)12 * nc);

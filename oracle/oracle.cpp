@@ -611,8 +611,12 @@ struct orc_solver {
     int bicgstab(int g, const std::vector<double> &b, double *x, double tol, int max_it) const
     {
         const int n = ncell;
-        std::vector<double> r(n), r0(n), pv(n, 0.0), v(n, 0.0), y(n), z(n), s(n), t(n);
-        const double *d = &mdiag[(size_t)g * n];
+        std::vector<double> r(n), r0(n), pv(n, 0.0), v(n, 0.0), y(n), z(n), s(n), t(n), dinv(n);
+        // diagonal preconditioner: multiply by the stored inverse diagonal
+        for (int i = 0; i < n; i++) {
+            double dd = mdiag[(size_t)g * n + i];
+            dinv[i] = (dd != 0.0) ? 1.0 / dd : 1.0;
+        }
         spmv(g, x, r.data());
         double rr = 0.0, bb = 0.0;
         for (int i = 0; i < n; i++) {
@@ -646,7 +650,7 @@ struct orc_solver {
             double beta = (rho / rho_old) * (alpha / w);
             for (int i = 0; i < n; i++) {
                 pv[i] = r[i] + beta * (pv[i] - w * v[i]);
-                y[i] = pv[i] / (d[i] != 0.0 ? d[i] : 1.0);
+                y[i] = pv[i] * dinv[i];
             }
             spmv(g, y.data(), v.data());
             double r0v = 0.0;
@@ -654,7 +658,7 @@ struct orc_solver {
             alpha = rho / r0v;
             for (int i = 0; i < n; i++) {
                 s[i] = r[i] - alpha * v[i];
-                z[i] = s[i] / (d[i] != 0.0 ? d[i] : 1.0);
+                z[i] = s[i] * dinv[i];
             }
             spmv(g, z.data(), t.data());
             double tt = 0.0, ts = 0.0;
