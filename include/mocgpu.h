@@ -39,6 +39,7 @@ extern "C" {
 
 typedef struct mocgpu_problem mocgpu_problem; /* traced problem (host) */
 typedef struct mocgpu_sweeper mocgpu_sweeper; /* device-resident solve */
+typedef struct mocgpu_batch mocgpu_batch;     /* batched solve engine */
 
 /* sizes reported by mocgpu_problem_sizes(), in this order */
 enum {
@@ -178,6 +179,64 @@ int mocgpu_sweeper_stream(mocgpu_sweeper *s, void **stream);
 int mocgpu_time_sweep(mocgpu_sweeper *s, int group, int reps, double *ms, int *launches);
 /* Total kernels launched by the library in this process so far. */
 int mocgpu_launch_count(int64_t *n);
+
+/* ---- batched solves (no MOCC counterpart) -------------------------------
+ * MOCC runs one EigenSolver::solve (eigen_solver.cpp:131-223) per input.
+ * The batch engine runs many independent solves (different cross sections,
+ * lattice sizes and group counts) at once: every active solve advances one
+ * power iteration per replay of one captured CUDA graph, with its own k,
+ * sources and convergence test (k_tol, psi_tol, min_iter, max_iter of its
+ * problem). Converged solves retire between iterations and queued ones take
+ * their slots (continuous batching); admission waits until the device bytes
+ * of the solve's geometry and state fit the memory budget. All solves of one
+ * engine must share polar angles per track set, inner iterations and the
+ * CMFD switch; the Gauss-Seidel boundary update is the only one batched.
+ * The engine keeps what it needs of a submitted problem, so the problem
+ * handle may be destroyed after submission; its options must not change
+ * while its solves are queued. */
+typedef struct mocgpu_batch_result {
+    int64_t id;
+    int error;          /* 0, or the MOCGPU_ERR_* code that ended this solve */
+    char message[128];  /* error text */
+    double k;
+    int iterations;
+    int converged;
+    double error_k, error_psi;
+    int64_t cmfd_iterations;
+    double t_submit, t_admit, t_done; /* engine clock, seconds */
+    int n_pin;                        /* entries of the pin-power map */
+} mocgpu_batch_result;
+
+typedef struct mocgpu_batch_stats {
+    int64_t submitted, completed, outer_iterations, graph_replays, captures;
+    int active, queued, capacity, geometries, bundles_per_unit;
+    double bytes_in_use, bytes_budget, geometry_bytes;
+    double now; /* engine clock, seconds */
+} mocgpu_batch_stats;
+
+/* precision: 0 FP64 sweep, 1 FP32 sweep (mixed); capacity: solves advanced
+ * together; mem_budget_bytes: device bytes for geometry + state (0: 80% of
+ * the free memory); bundles_per_unit: sweep work-unit shape, 1..4 bundles
+ * of 32 tracks per CTA. Fails with MOCGPU_ERR_CUDA without a GPU. */
+int mocgpu_batch_create(int precision, int capacity, double mem_budget_bytes, int bundles_per_unit,
+                        mocgpu_batch **out);
+void mocgpu_batch_destroy(mocgpu_batch *b);
+/* Queues a solve of p; xsl_text, when not NULL, gives other cross sections
+ * for p's materials (same names, groups and fissile flags) and the traced
+ * geometry of p is shared. *id names the solve in mocgpu_batch_take. */
+int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xsl_text, int64_t *id);
+/* Admits what fits, runs one outer iteration of every active solve, retires
+ * finished ones; *n_active = solves still active. */
+int mocgpu_batch_step(mocgpu_batch *b, int *n_active);
+/* Steps until nothing is queued or active. */
+int mocgpu_batch_run(mocgpu_batch *b);
+/* *ready = 1 and the result (removed from the engine) once solve id is done;
+ * pin_powers (may be NULL) receives res->n_pin values. */
+int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_result *res, double *pin_powers,
+                        int n_pin_capacity);
+int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out);
+/* The CUDA stream (cudaStream_t) of the engine's launches. */
+int mocgpu_batch_stream(mocgpu_batch *b, void **stream);
 
 #ifdef __cplusplus
 }

@@ -23,7 +23,8 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["MocgpuError", "Problem", "MoCSweeper", "EigenSolver", "synthetic_xsl", "load_library", "SIZES"]
+__all__ = ["MocgpuError", "Problem", "MoCSweeper", "EigenSolver", "BatchEngine", "synthetic_xsl", "load_library",
+           "SIZES"]
 
 _LIB = None
 
@@ -49,6 +50,21 @@ class _Result(C.Structure):
     _fields_ = [("k", C.c_double), ("iterations", C.c_int), ("converged", C.c_int), ("error_k", C.c_double),
                 ("error_psi", C.c_double), ("seconds", C.c_double), ("sweeps", C.c_int64),
                 ("cmfd_iterations", C.c_int64)]
+
+
+class _BatchResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("error", C.c_int), ("message", C.c_char * 128), ("k", C.c_double),
+                ("iterations", C.c_int), ("converged", C.c_int), ("error_k", C.c_double),
+                ("error_psi", C.c_double), ("cmfd_iterations", C.c_int64), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double), ("n_pin", C.c_int)]
+
+
+class _BatchStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("outer_iterations", C.c_int64),
+                ("graph_replays", C.c_int64), ("captures", C.c_int64), ("active", C.c_int), ("queued", C.c_int),
+                ("capacity", C.c_int), ("geometries", C.c_int), ("bundles_per_unit", C.c_int),
+                ("bytes_in_use", C.c_double), ("bytes_budget", C.c_double), ("geometry_bytes", C.c_double),
+                ("now", C.c_double)]
 
 
 def library_path() -> Path:
@@ -107,6 +123,14 @@ def load_library(build: bool = True):
         "mocgpu_time_sweep": (I, [P, I, I, DP, IP]),
         "mocgpu_launch_count": (I, [I64P]),
         "mocgpu_layout_stats": (I, [P, I, I, I, I64P, DP]),
+        "mocgpu_batch_create": (I, [I, I, D, I, C.POINTER(P)]),
+        "mocgpu_batch_destroy": (None, [P]),
+        "mocgpu_batch_submit": (I, [P, P, CP, I64P]),
+        "mocgpu_batch_step": (I, [P, IP]),
+        "mocgpu_batch_run": (I, [P]),
+        "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
+        "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
+        "mocgpu_batch_stream": (I, [P, C.POINTER(C.c_void_p)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -369,3 +393,68 @@ class EigenSolver:
 
     def pin_powers(self) -> np.ndarray:
         return self.sweeper.pin_powers()
+
+
+class BatchEngine:
+    """Many independent k-eigenvalue solves advanced together on one GPU.
+
+    Each submitted solve runs MOCC's EigenSolver power iteration
+    (``src/solvers/eigen_solver.cpp:131-253``) with its own k, sources and
+    convergence test; every active solve advances one outer iteration per
+    replay of one captured CUDA graph. Converged solves retire between
+    iterations and queued solves take their slots. ``submit(problem, xsl)``
+    reuses ``problem``'s traced geometry with the cross sections of ``xsl``.
+    """
+
+    def __init__(self, precision: int = 1, capacity: int = 64, mem_budget: float = 0.0,
+                 bundles_per_unit: int = 1):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.mocgpu_batch_create(precision, capacity, float(mem_budget), bundles_per_unit,
+                                             C.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mocgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, problem: Problem, xsl: str | None = None) -> int:
+        i = C.c_int64()
+        _check(self._lib.mocgpu_batch_submit(self._h, problem.handle, xsl.encode() if xsl else None, C.byref(i)))
+        return i.value
+
+    def step(self) -> int:
+        n = C.c_int()
+        _check(self._lib.mocgpu_batch_step(self._h, C.byref(n)))
+        return n.value
+
+    def run(self):
+        _check(self._lib.mocgpu_batch_run(self._h))
+
+    def take(self, solve_id: int, n_pin_max: int = 1 << 16):
+        """Result dict of a finished solve (None while it runs)."""
+        r = _BatchResult()
+        ready = C.c_int()
+        pins = np.zeros(n_pin_max)
+        _check(self._lib.mocgpu_batch_take(self._h, solve_id, C.byref(ready), C.byref(r), _dp(pins), n_pin_max))
+        if not ready.value:
+            return None
+        out = {f: getattr(r, f) for f, _ in _BatchResult._fields_ if f != "message"}
+        out["message"] = r.message.decode()
+        out["pin_powers"] = pins[:r.n_pin].copy()
+        return out
+
+    def stats(self) -> dict:
+        st = _BatchStats()
+        _check(self._lib.mocgpu_batch_get_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in _BatchStats._fields_}
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.mocgpu_batch_stream(self._h, C.byref(p)))
+        return p.value or 0

@@ -9,16 +9,21 @@
 
 #include <cuda_runtime.h>
 
+#include "device/batch.hpp"
 #include "device/sweeper.hpp"
 #include "host/materials.hpp"
 #include "host/problem.hpp"
 #include "host/xml.hpp"
 
 struct mocgpu_problem {
-    std::unique_ptr<mocgpu::Problem> P;
+    std::shared_ptr<mocgpu::Problem> P;
 };
 struct mocgpu_sweeper {
     std::unique_ptr<mocgpu::Sweeper> S;
+    cudaStream_t stream = nullptr;
+};
+struct mocgpu_batch {
+    std::unique_ptr<mocgpu::BatchEngine> E;
     cudaStream_t stream = nullptr;
 };
 
@@ -528,6 +533,136 @@ int mocgpu_launch_count(int64_t *n)
     return guarded([&] {
         REQUIRE(n, "null argument");
         *n = mocgpu::launch_count();
+    });
+}
+
+/* ---- batched solves ------------------------------------------------------ */
+static mocgpu::BatchEngine &eng(mocgpu_batch *b)
+{
+    if (!b || !b->E) throw mocgpu::Error(MOCGPU_ERR_ARG, "null batch handle");
+    return *b->E;
+}
+
+int mocgpu_batch_create(int precision, int capacity, double mem_budget_bytes, int bundles_per_unit,
+                        mocgpu_batch **out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        REQUIRE(precision == 0 || precision == 1, "precision must be 0 or 1");
+        REQUIRE(capacity >= 1 && capacity <= 65535, "capacity must be in [1, 65535]");
+        REQUIRE(bundles_per_unit >= 1 && bundles_per_unit <= 4, "bundles_per_unit must be in [1, 4]");
+        REQUIRE(mem_budget_bytes >= 0.0, "negative memory budget");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+            throw mocgpu::Error(MOCGPU_ERR_CUDA, "no CUDA device available: the batch engine runs on the GPU only");
+        auto h = std::make_unique<mocgpu_batch>();
+        MOCGPU_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        try {
+            h->E = std::make_unique<mocgpu::BatchEngine>(precision, capacity, (size_t)mem_budget_bytes,
+                                                         bundles_per_unit, h->stream);
+        } catch (...) {
+            cudaStreamDestroy(h->stream);
+            throw;
+        }
+        *out = h.release();
+    });
+}
+
+void mocgpu_batch_destroy(mocgpu_batch *b)
+{
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    b->E.reset();
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xsl_text, int64_t *id)
+{
+    return guarded([&] {
+        REQUIRE(p && p->P && id, "null argument");
+        auto &E = eng(b);
+        if (xsl_text && *xsl_text) {
+            mocgpu::CrossSections xs = mocgpu::cross_sections_from_xsl(*p->P, xsl_text);
+            *id = E.submit(p->P, &xs);
+        } else {
+            *id = E.submit(p->P, nullptr);
+        }
+    });
+}
+
+int mocgpu_batch_step(mocgpu_batch *b, int *n_active)
+{
+    return guarded([&] {
+        int n = eng(b).step();
+        if (n_active) *n_active = n;
+    });
+}
+
+int mocgpu_batch_run(mocgpu_batch *b)
+{
+    return guarded([&] { eng(b).run(); });
+}
+
+int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_result *res, double *pin_powers,
+                        int n_pin_capacity)
+{
+    return guarded([&] {
+        REQUIRE(ready && res, "null argument");
+        auto &E = eng(b);
+        mocgpu::BatchResult r;
+        *ready = E.take_result(id, r) ? 1 : 0;
+        if (!*ready) return;
+        std::memset(res, 0, sizeof(*res));
+        res->id = r.id;
+        res->error = r.error;
+        std::strncpy(res->message, r.message.c_str(), sizeof(res->message) - 1);
+        res->k = r.k;
+        res->iterations = r.iterations;
+        res->converged = r.converged;
+        res->error_k = r.error_k;
+        res->error_psi = r.error_psi;
+        res->cmfd_iterations = r.cmfd_iterations;
+        res->t_submit = r.t_submit;
+        res->t_admit = r.t_admit;
+        res->t_done = r.t_done;
+        res->n_pin = (int)r.pin_powers.size();
+        if (pin_powers && res->n_pin) {
+            REQUIRE(n_pin_capacity >= res->n_pin, "pin_powers buffer too small");
+            std::memcpy(pin_powers, r.pin_powers.data(), sizeof(double) * r.pin_powers.size());
+        }
+    });
+}
+
+int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out)
+{
+    return guarded([&] {
+        REQUIRE(out, "null argument");
+        auto &E = eng(b);
+        mocgpu::BatchStats s = E.stats();
+        out->submitted = s.submitted;
+        out->completed = s.completed;
+        out->outer_iterations = s.outer_iterations;
+        out->graph_replays = s.graph_replays;
+        out->captures = s.captures;
+        out->active = s.active;
+        out->queued = s.queued;
+        out->capacity = s.capacity;
+        out->geometries = s.geometries;
+        out->bundles_per_unit = s.bundles_per_unit;
+        out->bytes_in_use = (double)s.bytes_in_use;
+        out->bytes_budget = (double)s.bytes_budget;
+        out->geometry_bytes = (double)s.geometry_bytes;
+        out->now = E.now();
+    });
+}
+
+int mocgpu_batch_stream(mocgpu_batch *b, void **stream)
+{
+    return guarded([&] {
+        REQUIRE(stream, "null argument");
+        eng(b);
+        *stream = (void *)b->stream;
     });
 }
 

@@ -1,0 +1,464 @@
+#include "batch.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+
+namespace mocgpu {
+
+static double wall_seconds()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+BatchEngine::BatchEngine(int precision, int capacity, size_t mem_budget, int bundles_per_unit, cudaStream_t stream)
+    : precision_(precision), cap_(capacity), bpu_(bundles_per_unit), stream_(stream), t0_(wall_seconds())
+{
+    if (precision != 0 && precision != 1) MOCGPU_THROW(1, "precision must be 0 (double) or 1 (mixed)");
+    if (capacity < 1 || capacity > 65535) MOCGPU_THROW(1, "batch capacity must be in [1, 65535]");
+    if (bpu_ < 1 || bpu_ > 4) MOCGPU_THROW(1, "bundles per work unit must be in [1, 4]");
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) MOCGPU_THROW(20, "no CUDA device");
+    if (mem_budget == 0) {
+        size_t fr = 0, tot = 0;
+        MOCGPU_CUDA(cudaMemGetInfo(&fr, &tot));
+        mem_budget = (size_t)(0.8 * (double)fr);
+    }
+    budget_ = mem_budget;
+    slots_.resize(cap_);
+    d_gv_.alloc(cap_);
+    d_sv_.alloc(cap_);
+    d_cv_.alloc(cap_);
+    d_fv_.alloc(cap_);
+    d_area_.alloc(cap_);
+    d_act_.alloc(cap_);
+    d_nact_.alloc(1);
+    d_nact_.zero(stream_);
+    d_sum_.alloc((size_t)cap_ * 6);
+    MOCGPU_CUDA(cudaMallocHost((void **)&h_sum_, sizeof(double) * 6 * (size_t)cap_));
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+BatchEngine::~BatchEngine()
+{
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (h_sum_) cudaFreeHost(h_sum_);
+}
+
+double BatchEngine::now() const { return wall_seconds() - t0_; }
+
+// All solves of one batch share the launch sequence: polar angles per track
+// set (a kernel template parameter), inner iterations, Gauss-Seidel boundary
+// update and whether CMFD runs.
+void BatchEngine::check_config(const Problem &P)
+{
+    const SolverOptions &o = P.opts;
+    if (!o.gs_boundary) MOCGPU_THROW(1, "the batched engine runs the Gauss-Seidel boundary update only");
+    const bool cm = o.cmfd && o.cmfd_enabled;
+    if (!configured_) {
+        pol_ = P.flat.pol_per_set;
+        n_inner_ = o.n_inner;
+        cmfd_ = cm;
+        configured_ = true;
+        return;
+    }
+    if (P.flat.pol_per_set != pol_ || o.n_inner != n_inner_ || cm != cmfd_)
+        MOCGPU_THROW(1, "solve does not share the batch's sweep configuration (polar angles per set, inner "
+                        "iterations, CMFD)");
+}
+
+size_t BatchEngine::geometry_estimate(const FlatProblem &f) const
+{
+    // plain and bundled segment streams (bundles padded to 32 lanes), crossing
+    // events and per-track data; the measured size replaces this once built
+    const size_t rb = precision_ == 0 ? 8 : 4;
+    return (size_t)((double)f.n_seg * ((rb + 4) + 1.5 * (rb + 2))) + (size_t)f.n_tracks * 64 +
+           (size_t)f.n_fsr * 64 + (size_t)f.cm_fw.size() * 24 + (1 << 20);
+}
+
+std::shared_ptr<const DeviceGeometry> BatchEngine::geometry_for(const Problem &P)
+{
+    for (auto &kv : geos_)
+        if (kv.first == &P) return kv.second.geo;
+    return nullptr;
+}
+
+int64_t BatchEngine::submit(std::shared_ptr<const Problem> P, const CrossSections *xs)
+{
+    if (!P) MOCGPU_THROW(1, "null problem");
+    check_config(*P);
+    if (xs && (xs->ng != P->flat.ng || xs->xstr.size() != P->flat.xstr.size()))
+        MOCGPU_THROW(4, "cross sections do not match the problem's materials and groups");
+    for (int s : {EAST, NORTH, WEST, SOUTH})
+        if (P->flat.bc[s] != (int)BoundaryType::VACUUM && P->flat.bc[s] != (int)BoundaryType::REFLECT)
+            MOCGPU_THROW(5, "radial boundaries must be vacuum or reflect for the eigenvalue path");
+    Pending p;
+    p.id = next_id_++;
+    p.t_submit = now();
+    if (xs) p.xs = std::make_unique<CrossSections>(*xs);
+    p.P = std::move(P);
+    queue_.push_back(std::move(p));
+    st_.submitted++;
+    return queue_.back().id;
+}
+
+bool BatchEngine::try_admit(Pending &p)
+{
+    int slot = -1;
+    for (int i = 0; i < cap_; i++)
+        if (slots_[i].id < 0) {
+            slot = i;
+            break;
+        }
+    if (slot < 0) return false;
+    const FlatProblem &f = p.P->flat;
+    std::shared_ptr<const DeviceGeometry> geo = geometry_for(*p.P);
+    size_t need_geo = geo ? 0 : geometry_estimate(f);
+    // boundary-flux entries per group: both faces of every angle's set
+    size_t bcpg = 0;
+    {
+        const int nd = f.ndir_oct, sets_oct = f.n_sets / 2;
+        for (int a = 0; a < f.n_ang; a++) {
+            int r = (a / nd >= 2) ? (a + 2 * nd) % (4 * nd) : a;
+            int s = (r % nd) / f.pol_per_set + (r / nd) * sets_oct;
+            bcpg += f.set_nx[s] + f.set_ny[s];
+        }
+    }
+    size_t need_state = Sweeper::state_bytes_for(f, precision_, (int)bcpg);
+    if (in_use_ + need_geo + need_state > budget_) {
+        // release resident geometries that no solve uses
+        for (auto it = geos_.begin(); it != geos_.end() && in_use_ + need_geo + need_state > budget_;) {
+            if (it->second.users == 0 && it->first != p.P.get()) {
+                in_use_ -= it->second.geo->bytes();
+                it = geos_.erase(it);
+            } else {
+                ++it;
+            }
+        }
+        if (in_use_ + need_geo + need_state > budget_) return false;
+    }
+    if (!geo) {
+        geo = std::make_shared<const DeviceGeometry>(f, precision_, bpu_);
+        GeoEntry e;
+        e.P = p.P;
+        e.geo = geo;
+        geos_[p.P.get()] = e;
+        in_use_ += geo->bytes();
+    }
+    GeoEntry &ge = geos_[p.P.get()];
+    ge.users++;
+
+    Slot &S = slots_[slot];
+    S.sw = std::make_unique<Sweeper>(*p.P, precision_, stream_, geo, p.xs.get());
+    S.geo = geo;
+    S.key = p.P.get();
+    S.id = p.id;
+    S.max_iter = p.P->opts.max_iter;
+    S.min_iter = p.P->opts.min_iter;
+    S.k_tol = p.P->opts.k_tol;
+    S.psi_tol = p.P->opts.psi_tol;
+    S.iterations = 0;
+    S.t_submit = p.t_submit;
+    S.t_admit = now();
+    S.bytes = S.sw->state_bytes();
+    in_use_ += S.bytes;
+
+    // EigenSolver::solve start (eigen_solver.cpp:131-160): flat flux, k = 1,
+    // fission source at k = 1.
+    Sweeper &sw = *S.sw;
+    sw.set_coarse_enabled(cmfd_);
+    sw.initialize();
+    double init[16] = {0};
+    init[RED_K - RED_K] = 1.0;                          // RED_K
+    init[RED_K_PREV - RED_K] = 1.0;                     // RED_K_PREV
+    init[RED_N_FISSILE - RED_K] = (double)sw.n_fissile(); // RED_N_FISSILE
+    MOCGPU_CUDA(cudaMemcpyAsync(sw.state().red + RED_K, init, sizeof(double) * 14, cudaMemcpyHostToDevice, stream_));
+    sw.calc_fission_source(1.0);
+
+    // shape of the captured graph
+    shape_.max_fsr = std::max(shape_.max_fsr, f.n_fsr);
+    shape_.max_pin = std::max(shape_.max_pin, f.n_pin);
+    shape_.max_surf = std::max(shape_.max_surf, f.n_surf);
+    shape_.max_cell = std::max(shape_.max_cell, f.n_pin);
+    shape_.max_g = std::max(shape_.max_g, f.ng);
+    shape_.max_local = std::max(shape_.max_local, geo->fv.max_local);
+    int wmax = std::max(geo->phase_wu[1] - geo->phase_wu[0], geo->phase_wu[2] - geo->phase_wu[1]);
+    max_items_phase_ = std::max(max_items_phase_, wmax);
+    lists_dirty_ = true;
+    return true;
+}
+
+void BatchEngine::retire(int slot, int error, const std::string &msg, bool converged, double k, double ek, double ep,
+                         int64_t cmfd_its)
+{
+    Slot &S = slots_[slot];
+    BatchResult r;
+    r.id = S.id;
+    r.error = error;
+    r.message = msg;
+    r.k = k;
+    r.iterations = S.iterations;
+    r.converged = converged ? 1 : 0;
+    r.error_k = ek;
+    r.error_psi = ep;
+    r.cmfd_iterations = cmfd_its;
+    r.t_submit = S.t_submit;
+    r.t_admit = S.t_admit;
+    if (!error) {
+        r.pin_powers.resize(S.sw->flat().n_pin);
+        S.sw->pin_powers(r.pin_powers.data());
+    }
+    r.t_done = now();
+    done_[r.id] = std::move(r);
+    in_use_ -= S.bytes;
+    auto it = geos_.find(S.key);
+    if (it != geos_.end()) it->second.users--;
+    S.sw.reset();
+    S.geo.reset();
+    S.key = nullptr;
+    S.id = -1;
+    st_.completed++;
+    lists_dirty_ = true;
+}
+
+// Device copies of every slot's views, the active list and the sweep work
+// lists. One list per Gauss-Seidel phase holds (slot, work unit) items sorted
+// by the slot's group count (descending) and then by unit size (descending),
+// so the items of group g are a prefix of the list.
+void BatchEngine::rebuild_lists()
+{
+    act_.clear();
+    std::vector<GeomView> gv(cap_);
+    std::vector<StateView> sv(cap_);
+    std::vector<CmfdView> cv(cap_);
+    std::vector<FastView> fv(cap_);
+    std::vector<const double *> area(cap_, nullptr);
+    for (int i = 0; i < cap_; i++) {
+        const Slot &S = slots_[i];
+        if (S.id < 0) continue;
+        act_.push_back(i);
+        gv[i] = S.sw->geom();
+        sv[i] = S.sw->state();
+        cv[i] = S.sw->cmfd_view();
+        fv[i] = S.geo->fv;
+        area[i] = S.geo->surf_area();
+    }
+    const int items_cap = std::max(1, max_items_phase_ * cap_);
+    if (items_cap > shape_.items_cap) shape_.items_cap = items_cap;
+    if ((size_t)shape_.items_cap * 2 > d_items_.n) d_items_.alloc((size_t)shape_.items_cap * 2);
+    if ((size_t)shape_.max_g * 2 > d_nitems_.n) d_nitems_.alloc((size_t)std::max(shape_.max_g, 1) * 2);
+
+    std::vector<int2> items[2];
+    std::vector<int> nitems((size_t)shape_.max_g * 2, 0);
+    for (int ph = 0; ph < 2; ph++) {
+        struct It {
+            int g, rows, slot, wu;
+        };
+        std::vector<It> v;
+        for (int s : act_) {
+            const DeviceGeometry &geo = *slots_[s].geo;
+            for (int w = geo.phase_wu[ph]; w < geo.phase_wu[ph + 1]; w++) v.push_back({geo.G, geo.wu_rows[w], s, w});
+        }
+        std::stable_sort(v.begin(), v.end(), [](const It &a, const It &b) {
+            if (a.g != b.g) return a.g > b.g;
+            return a.rows > b.rows;
+        });
+        for (const It &x : v) items[ph].push_back(make_int2(x.slot, x.wu));
+        for (int g = 0; g < shape_.max_g; g++) {
+            int n = 0;
+            for (const It &x : v) n += (x.g > g) ? 1 : 0;
+            nitems[(size_t)g * 2 + ph] = n;
+        }
+    }
+    MOCGPU_CUDA(cudaMemcpyAsync(d_gv_.p, gv.data(), sizeof(GeomView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(d_sv_.p, sv.data(), sizeof(StateView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(d_cv_.p, cv.data(), sizeof(CmfdView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(d_fv_.p, fv.data(), sizeof(FastView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(
+        cudaMemcpyAsync(d_area_.p, area.data(), sizeof(const double *) * cap_, cudaMemcpyHostToDevice, stream_));
+    int nact = (int)act_.size();
+    if (nact)
+        MOCGPU_CUDA(cudaMemcpyAsync(d_act_.p, act_.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(d_nact_.p, &nact, sizeof(int), cudaMemcpyHostToDevice, stream_));
+    for (int ph = 0; ph < 2; ph++)
+        if (!items[ph].empty())
+            MOCGPU_CUDA(cudaMemcpyAsync(d_items_.p + (size_t)ph * shape_.items_cap, items[ph].data(),
+                                        sizeof(int2) * items[ph].size(), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(d_nitems_.p, nitems.data(), sizeof(int) * nitems.size(), cudaMemcpyHostToDevice,
+                                stream_));
+    // pageable sources: wait for the copies before the host vectors go away
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    lists_dirty_ = false;
+}
+
+// One outer iteration of every active solve (EigenSolver::step,
+// eigen_solver.cpp:225-253), captured once per batch shape.
+void BatchEngine::capture()
+{
+    if (exec_) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
+    if (graph_) {
+        cudaGraphDestroy(graph_);
+        graph_ = nullptr;
+    }
+    BatchViews b{};
+    b.gv = d_gv_.p;
+    b.sv = d_sv_.p;
+    b.cv = d_cv_.p;
+    b.fv = d_fv_.p;
+    b.surf_area = d_area_.p;
+    b.act = d_act_.p;
+    b.n_act = d_nact_.p;
+    b.cap = cap_;
+    b.max_fsr = shape_.max_fsr;
+    b.max_pin = shape_.max_pin;
+    b.max_surf = shape_.max_surf;
+    b.max_cell = shape_.max_cell;
+    b.max_g = shape_.max_g;
+    if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local);
+    else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local);
+
+    const int64_t l0 = launch_count();
+    MOCGPU_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
+    try {
+        if (cmfd_) {
+            launch_b_pin_flux(b, stream_);
+            launch_b_homogenize(b, stream_);
+            launch_b_cmfd(b, stream_);
+            launch_b_set_pin_flux(b, stream_);
+        }
+        launch_b_fission_source(b, stream_);
+        launch_b_copy_old(b, stream_);
+        for (int g = 0; g < shape_.max_g; g++) {
+            if (precision_ == 0) launch_b_group_source<double>(b, g, stream_);
+            else launch_b_group_source<float>(b, g, stream_);
+            for (int inner = 0; inner < n_inner_; inner++) {
+                const bool last = inner == n_inner_ - 1;
+                const bool cur = last && cmfd_;
+                if (cur) launch_b_zero_currents(b, g, stream_);
+                for (int ph = 0; ph < 2; ph++) {
+                    const int2 *items = d_items_.p + (size_t)ph * shape_.items_cap;
+                    const int *nit = d_nitems_.p + (size_t)g * 2 + ph;
+                    if (precision_ == 0)
+                        launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
+                                               shape_.max_local, stream_);
+                    else
+                        launch_b_sweep<float>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
+                                              shape_.max_local, stream_);
+                }
+                if (precision_ == 0) launch_b_epilogue<double>(b, g, !last, stream_);
+                else launch_b_epilogue<float>(b, g, !last, stream_);
+                if (cur) launch_b_normalize_currents(b, g, stream_);
+            }
+        }
+        launch_b_k_update(b, stream_);
+        launch_b_errors(b, stream_);
+        launch_b_summary(b, d_sum_.p, stream_);
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream_, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    MOCGPU_CUDA(cudaStreamEndCapture(stream_, &graph_));
+    MOCGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+    graph_nodes_ = launch_count() - l0;
+    note_launches(-graph_nodes_); // capture records launches; replays count them
+    captured_ = shape_;
+    st_.captures++;
+}
+
+int BatchEngine::step()
+{
+    // continuous batching: fill free slots from the queue, in order
+    while (!queue_.empty()) {
+        if (try_admit(queue_.front())) {
+            queue_.pop_front();
+            continue;
+        }
+        bool any = false;
+        for (const Slot &S : slots_) any |= S.id >= 0;
+        if (any) break;
+        // the head does not fit an empty engine: it never will
+        Pending p = std::move(queue_.front());
+        queue_.pop_front();
+        BatchResult r;
+        r.id = p.id;
+        r.error = 21;
+        r.message = "solve does not fit the engine's device-memory budget";
+        r.t_submit = p.t_submit;
+        r.t_done = now();
+        done_[r.id] = std::move(r);
+        st_.completed++;
+    }
+    if (lists_dirty_) rebuild_lists();
+    if (act_.empty()) return 0;
+    if (!exec_ || shape_ != captured_) capture();
+
+    MOCGPU_CUDA(cudaGraphLaunch(exec_, stream_));
+    note_launches(graph_nodes_);
+    MOCGPU_CUDA(cudaMemcpyAsync(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    st_.graph_replays++;
+    st_.outer_iterations += (int64_t)act_.size();
+
+    const std::vector<int> act = act_;
+    for (int s : act) {
+        Slot &S = slots_[s];
+        const double *o = h_sum_ + (size_t)s * 6;
+        S.iterations++;
+        const double k = o[0], ek = o[1], ep = o[2];
+        const unsigned status = (unsigned)o[3];
+        const int64_t cits = (int64_t)o[4];
+        if (status & DEV_NONPOSITIVE_PIN_FLUX) {
+            retire(s, 11, "Negative or zero input flux in set_pin_flux", false, k, ek, ep, cits);
+        } else if ((status & DEV_NAN) || !std::isfinite(k)) {
+            retire(s, 12, "Eigenvalue is not a number. Giving up.", false, k, ek, ep, cits);
+        } else if (ek < S.k_tol && ep < S.psi_tol && S.iterations - 1 >= S.min_iter) {
+            retire(s, 0, "", true, k, ek, ep, cits);
+        } else if (S.iterations >= S.max_iter) {
+            retire(s, 0, "", false, k, ek, ep, cits);
+        }
+    }
+    int n = 0;
+    for (const Slot &S : slots_) n += S.id >= 0;
+    return n;
+}
+
+void BatchEngine::run()
+{
+    while (true) {
+        int n = step();
+        if (n == 0 && queue_.empty()) break;
+    }
+}
+
+bool BatchEngine::take_result(int64_t id, BatchResult &out)
+{
+    auto it = done_.find(id);
+    if (it == done_.end()) return false;
+    out = std::move(it->second);
+    done_.erase(it);
+    return true;
+}
+
+BatchStats BatchEngine::stats() const
+{
+    BatchStats s = st_;
+    s.active = 0;
+    for (const Slot &S : slots_) s.active += S.id >= 0;
+    s.queued = (int)queue_.size();
+    s.capacity = cap_;
+    s.bytes_in_use = in_use_;
+    s.bytes_budget = budget_;
+    s.geometry_bytes = 0;
+    for (const auto &kv : geos_) s.geometry_bytes += kv.second.geo->bytes();
+    s.geometries = (int)geos_.size();
+    s.bundles_per_unit = bpu_;
+    return s;
+}
+
+} // namespace mocgpu

@@ -1,0 +1,149 @@
+// Batched k-eigenvalue engine: many independent 2-D solves (different cross
+// sections, lattice sizes and group counts) advance together, one power
+// iteration of every active solve per replay of a captured CUDA graph.
+//
+// Each solve follows MOCC's EigenSolver::step sequence
+// (src/solvers/eigen_solver.cpp:225-253) with its own k, sources and
+// convergence test; only the launches are shared. Per-solve scalars stay in
+// device memory (StateView::red), so the host reads one small summary per
+// outer iteration. Solves retire as they converge and queued solves take
+// their slots between iterations (continuous batching); admission is gated
+// by a device-memory budget against the solve's segment and state sizes.
+#pragma once
+
+#include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sweeper.hpp"
+
+namespace mocgpu {
+
+struct BatchResult {
+    int64_t id = -1;
+    int error = 0; // 0, or the status code that ended the solve
+    std::string message;
+    double k = 1.0;
+    int iterations = 0;
+    int converged = 0;
+    double error_k = 0.0, error_psi = 0.0;
+    int64_t cmfd_iterations = 0;
+    double t_submit = 0.0, t_admit = 0.0, t_done = 0.0; // seconds on the engine clock
+    std::vector<double> pin_powers;                      // [ny][nx], normalised to the fuel pin count
+};
+
+struct BatchStats {
+    int64_t submitted = 0, completed = 0, outer_iterations = 0, graph_replays = 0, captures = 0;
+    int active = 0, queued = 0, capacity = 0;
+    size_t bytes_in_use = 0, bytes_budget = 0, geometry_bytes = 0;
+    int geometries = 0, bundles_per_unit = 0;
+};
+
+class BatchEngine {
+  public:
+    // capacity: solves advanced together; mem_budget: device bytes the
+    // engine may hold for geometry + solve state (0: 80% of free memory);
+    // bundles_per_unit: sweep work-unit shape (1..4 bundles of 32 tracks).
+    BatchEngine(int precision, int capacity, size_t mem_budget, int bundles_per_unit, cudaStream_t stream = 0);
+    ~BatchEngine();
+    BatchEngine(const BatchEngine &) = delete;
+    BatchEngine &operator=(const BatchEngine &) = delete;
+
+    // Queues one solve of `P` (optionally with other cross sections for the
+    // same materials). `P` stays referenced until the solve is admitted.
+    int64_t submit(std::shared_ptr<const Problem> P, const CrossSections *xs = nullptr);
+    // Admits queued solves that fit, runs one outer iteration of every active
+    // solve and retires the finished ones. Returns the number still active.
+    int step();
+    // Steps until nothing is queued or active.
+    void run();
+    // Finished result of solve `id` (removed from the engine); false if the
+    // solve has not finished.
+    bool take_result(int64_t id, BatchResult &out);
+    BatchStats stats() const;
+    double now() const; // engine clock (s)
+    cudaStream_t stream() const { return stream_; }
+
+  private:
+    struct Pending {
+        int64_t id;
+        std::shared_ptr<const Problem> P;
+        std::unique_ptr<CrossSections> xs;
+        double t_submit;
+        size_t bytes; // state bytes (+ geometry bytes when not yet resident)
+    };
+    struct Slot {
+        int64_t id = -1;
+        std::unique_ptr<Sweeper> sw;
+        std::shared_ptr<const DeviceGeometry> geo;
+        const Problem *key = nullptr;
+        int max_iter = 0, min_iter = 0, iterations = 0;
+        double k_tol = 0.0, psi_tol = 0.0, t_submit = 0.0, t_admit = 0.0;
+        size_t bytes = 0;
+    };
+
+    std::shared_ptr<const DeviceGeometry> geometry_for(const Problem &P);
+    size_t geometry_estimate(const FlatProblem &f) const;
+    bool try_admit(Pending &p);
+    void retire(int slot, int error, const std::string &msg, bool converged, double k, double ek, double ep,
+                int64_t cmfd_its);
+    void rebuild_lists();
+    void capture();
+    void check_config(const Problem &P);
+
+    int precision_, cap_, bpu_;
+    size_t budget_ = 0, in_use_ = 0;
+    cudaStream_t stream_;
+    double t0_;
+    int64_t next_id_ = 0;
+    std::deque<Pending> queue_;
+    std::vector<Slot> slots_;
+    std::map<int64_t, BatchResult> done_;
+    // Resident geometries, keyed by the problem that was traced; the entry
+    // keeps that problem alive so the key is never reused while cached.
+    struct GeoEntry {
+        std::shared_ptr<const Problem> P;
+        std::shared_ptr<const DeviceGeometry> geo;
+        int users = 0;
+    };
+    std::map<const Problem *, GeoEntry> geos_;
+    BatchStats st_{};
+
+    // batch configuration fixed by the first solve
+    bool configured_ = false;
+    int pol_ = 0, n_inner_ = 1;
+    bool cmfd_ = false;
+
+    // device-side views and lists
+    DevBuf<GeomView> d_gv_;
+    DevBuf<StateView> d_sv_;
+    DevBuf<CmfdView> d_cv_;
+    DevBuf<FastView> d_fv_;
+    DevBuf<const double *> d_area_;
+    DevBuf<int> d_act_, d_nact_;
+    DevBuf<int2> d_items_;
+    DevBuf<int> d_nitems_;
+    DevBuf<double> d_sum_;
+    double *h_sum_ = nullptr; // pinned summary
+    std::vector<int> act_;
+    bool lists_dirty_ = true;
+
+    // graph and the sizes it was captured for
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int64_t graph_nodes_ = 0;
+    struct Shape {
+        int max_fsr = 0, max_pin = 0, max_surf = 0, max_cell = 0, max_g = 0, max_local = 0, items_cap = 0;
+        bool operator!=(const Shape &o) const
+        {
+            return max_fsr != o.max_fsr || max_pin != o.max_pin || max_surf != o.max_surf ||
+                   max_cell != o.max_cell || max_g != o.max_g || max_local != o.max_local || items_cap != o.items_cap;
+        }
+    } shape_, captured_;
+    int max_items_phase_ = 0; // capacity of one (group, phase) item list
+};
+
+} // namespace mocgpu

@@ -275,7 +275,7 @@ __device__ double residual_g(const CmfdView &c, Blk &B, const double *m, const d
 
 } // namespace
 
-__global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
+__device__ void cmfd_body(CmfdView c, int vec_in_smem)
 {
     extern __shared__ __align__(16) double sm[];
     Blk B;
@@ -411,13 +411,49 @@ __global__ void k_cmfd_solve(CmfdView c, int vec_in_smem)
     }
 }
 
+__global__ void k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
+
+// One CTA per active solve of a batch; the coarse-current flag and the CMFD
+// iteration count live in each solve's scalar block.
+__global__ void kb_cmfd_solve(BatchViews b, int vec_in_smem)
+{
+    if ((int)blockIdx.x >= *b.n_act) return;
+    const int slot = b.act[blockIdx.x];
+    CmfdView c = b.cv[slot];
+    c.has_radial = (c.red[RED_HAS_RADIAL] != 0.0) ? 1 : 0;
+    if (!vec_in_smem || 10 * c.n_cell + 128 > 10 * b.max_cell + 128) vec_in_smem = 0;
+    cmfd_body(c, vec_in_smem);
+    if (threadIdx.x == 0) c.red[RED_CMFD_ITS] += c.stats[0];
+}
+
 void note_launch_external();
+
+static int cmfd_warps(int n_cell)
+{
+    int nw = (n_cell + 255) / 256;
+    if (n_cell <= 512) nw = 1;
+    return nw < 1 ? 1 : (nw > 16 ? 16 : nw);
+}
+
+void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
+{
+    const int max_cell = b.max_cell;
+    const int nw = cmfd_warps(max_cell);
+    size_t vec_bytes = (size_t)10 * max_cell * sizeof(double);
+    int in_smem = (vec_bytes + 128 * sizeof(double)) <= 200 * 1024 ? 1 : 0;
+    size_t smem = 128 * sizeof(double) + (in_smem ? vec_bytes : 0);
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(kb_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    note_launch_external();
+    kb_cmfd_solve<<<b.cap, 32 * nw, smem, s>>>(b, in_smem);
+}
 
 void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
 {
-    int nw = (c.n_cell + 255) / 256;
-    if (c.n_cell <= 512) nw = 1;
-    nw = nw < 1 ? 1 : (nw > 16 ? 16 : nw);
+    const int nw = cmfd_warps(c.n_cell);
     size_t vec_bytes = (size_t)10 * c.n_cell * sizeof(double);
     int in_smem = (vec_bytes + 128 * sizeof(double)) <= 200 * 1024 ? 1 : 0;
     size_t smem = 128 * sizeof(double) + (in_smem ? vec_bytes : 0);

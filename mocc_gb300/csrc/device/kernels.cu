@@ -16,6 +16,7 @@ static std::atomic<int64_t> g_launches{0};
 static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 int64_t launch_count() { return g_launches.load(); }
 void note_launch_external() { note_launch(); }
+void note_launches(int64_t n) { g_launches += n; }
 
 // ---------------------------------------------------------------------------
 __global__ void k_fill(double *p, double v, int64_t n)
@@ -430,10 +431,9 @@ void launch_set_pin_flux(const GeomView &g, double *phi, const double *cflux, do
 }
 
 // Flux-weighted pin homogenisation (xs_mesh_homogenized.cpp:261-363).
-__global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
+__device__ void homogenize_pin(const GeomView &g, const double *phi, const CmfdView &c, int ip)
 {
     const double *fsr_area = g.fsr_area;
-    int ip = blockIdx.x * blockDim.x + threadIdx.x;
     if (ip >= g.n_pin) return;
     const int G = g.G;
     const int cell = g.pin_cell[ip];
@@ -476,6 +476,10 @@ __global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
     }
     for (int ig = 0; ig < G; ig++)
         c.xsrm[(size_t)cell * G + ig] = c.xstr[(size_t)cell * G + ig] - c.scat[((size_t)cell * G + ig) * G + ig];
+}
+__global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
+{
+    homogenize_pin(g, phi, c, blockIdx.x * blockDim.x + threadIdx.x);
 }
 void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, cudaStream_t s)
 {
@@ -570,6 +574,292 @@ void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStr
 {
     MOCGPU_CUDA(cudaMemsetAsync(pow + g.n_pin, 0, sizeof(double), s));
     { note_launch(); k_pin_power<<<(g.n_pin + 255) / 256, 256, 0, s>>>(g, phi, pow); }
+}
+
+// ===========================================================================
+// Batched forms: the same arithmetic for every active solve of a batch, one
+// solve per blockIdx.y; per-solve scalars (k, total fission, error sums) live
+// in each solve's StateView::red so nothing returns to the host between
+// launches. Solves with fewer groups than the group being processed skip it.
+#define BATCH_SLOT                                                                                                   \
+    if ((int)blockIdx.y >= *b.n_act) return;                                                                         \
+    const int slot = b.act[blockIdx.y];                                                                              \
+    const GeomView &g = b.gv[slot];                                                                                  \
+    const StateView &st = b.sv[slot];
+
+static dim3 bgrid(int n, int block, int cap) { return dim3((unsigned)((n + block - 1) / block), (unsigned)cap); }
+
+__global__ void kb_fission_source(BatchViews b)
+{
+    BATCH_SLOT
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    const double rk = 1.0 / st.red[RED_K];
+    const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * g.G;
+    double f = 0.0;
+    for (int ig = 0; ig < g.G; ig++) f += rk * nf[ig] * st.phi[(size_t)ig * g.n_fsr + r];
+    st.fs[r] = f;
+}
+void launch_b_fission_source(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_fission_source<<<bgrid(b.max_fsr, 256, b.cap), 256, 0, s>>>(b);
+}
+
+__global__ void kb_copy_old(BatchViews b)
+{
+    BATCH_SLOT
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    st.fs_prev[r] = st.fs[r];
+    for (int ig = 0; ig < g.G; ig++) st.phi_old[(size_t)ig * g.n_fsr + r] = st.phi[(size_t)ig * g.n_fsr + r];
+}
+void launch_b_copy_old(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_copy_old<<<bgrid(b.max_fsr, 256, b.cap), 256, 0, s>>>(b);
+}
+
+template <typename Real> __global__ void kb_group_source(BatchViews b, int group)
+{
+    BATCH_SLOT
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr || group >= g.G) return;
+    const int G = g.G;
+    const int m = g.fsr_mat[r];
+    const double *srow = g.scat + ((size_t)m * G + group) * G;
+    double src = g.xsch[(size_t)m * G + group] * st.fs[r];
+    for (int gg = 0; gg < G; gg++)
+        if (gg != group) src += srow[gg] * st.phi[(size_t)gg * g.n_fsr + r];
+    st.src1g[r] = src;
+    double xt = g.xstr[(size_t)m * G + group];
+    double q = (src + st.phi[(size_t)group * g.n_fsr + r] * srow[group]) * (1.0 / (xt * kFpi));
+    ((Real *)st.qbar)[r] = (Real)q;
+    ((Real *)st.sigt)[r] = (Real)xt;
+}
+template <typename Real> void launch_b_group_source(const BatchViews &b, int group, cudaStream_t s)
+{
+    note_launch();
+    kb_group_source<Real><<<bgrid(b.max_fsr, 256, b.cap), 256, 0, s>>>(b, group);
+}
+template void launch_b_group_source<float>(const BatchViews &, int, cudaStream_t);
+template void launch_b_group_source<double>(const BatchViews &, int, cudaStream_t);
+
+template <typename Real> __global__ void kb_epilogue(BatchViews b, int group, int update_q)
+{
+    BATCH_SLOT
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr || group >= g.G) return;
+    Real *tally = (Real *)st.tally;
+    Real *qbar = (Real *)st.qbar;
+    const Real *sigt = (const Real *)st.sigt;
+    double q = (double)qbar[r];
+    double ph = (double)tally[r] / ((double)sigt[r] * g.fsr_vol[r]) + q * kFpi;
+    st.phi[(size_t)group * g.n_fsr + r] = ph;
+    tally[r] = (Real)0;
+    if (update_q) {
+        const int G = g.G, m = g.fsr_mat[r];
+        double sgg = g.scat[((size_t)m * G + group) * G + group];
+        double xt = g.xstr[(size_t)m * G + group];
+        qbar[r] = (Real)((st.src1g[r] + ph * sgg) * (1.0 / (xt * kFpi)));
+    }
+}
+template <typename Real> void launch_b_epilogue(const BatchViews &b, int group, bool update_q, cudaStream_t s)
+{
+    note_launch();
+    kb_epilogue<Real><<<bgrid(b.max_fsr, 256, b.cap), 256, 0, s>>>(b, group, update_q ? 1 : 0);
+}
+template void launch_b_epilogue<float>(const BatchViews &, int, bool, cudaStream_t);
+template void launch_b_epilogue<double>(const BatchViews &, int, bool, cudaStream_t);
+
+__global__ void kb_zero_currents(BatchViews b, int group)
+{
+    BATCH_SLOT
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.n_surf || group >= g.G) return;
+    st.cur[(size_t)group * g.n_surf + i] = 0.0;
+    st.sflux[(size_t)group * g.n_surf + i] = 0.0;
+}
+void launch_b_zero_currents(const BatchViews &b, int group, cudaStream_t s)
+{
+    note_launch();
+    kb_zero_currents<<<bgrid(b.max_surf, 256, b.cap), 256, 0, s>>>(b, group);
+}
+
+// Radial surfaces only: the axial ones are never tallied in 2-D
+// (moc_sweeper.cpp:206-221 normalises every surface; axial entries stay 0).
+__global__ void kb_normalize_currents(BatchViews b, int group)
+{
+    BATCH_SLOT
+    if (group >= g.G) return;
+    const double *area = b.surf_area[slot];
+    int i = g.nx * g.ny + blockIdx.x * blockDim.x + threadIdx.x;
+    int end = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx + g.nx * g.ny;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st.red[RED_HAS_RADIAL] = 1.0;
+    if (i >= end) return;
+    st.cur[(size_t)group * g.n_surf + i] /= area[i];
+    st.sflux[(size_t)group * g.n_surf + i] /= area[i];
+}
+void launch_b_normalize_currents(const BatchViews &b, int group, cudaStream_t s)
+{
+    note_launch();
+    kb_normalize_currents<<<bgrid(b.max_surf, 256, b.cap), 256, 0, s>>>(b, group);
+}
+
+__global__ void kb_pin_flux(BatchViews b)
+{
+    BATCH_SLOT
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.n_pin * g.G) return;
+    int ig = idx / g.n_pin, ip = idx % g.n_pin;
+    double v = 0.0, pf = 0.0;
+    for (int r = g.pin_first_reg[ip]; r < g.pin_first_reg[ip + 1]; r++) {
+        v += g.fsr_vol[r];
+        pf += st.phi[(size_t)ig * g.n_fsr + r] * g.fsr_vol[r];
+    }
+    st.cflux[(size_t)ig * g.n_pin + g.pin_cell[ip]] = pf / v;
+}
+void launch_b_pin_flux(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_pin_flux<<<bgrid(b.max_pin * b.max_g, 256, b.cap), 256, 0, s>>>(b);
+}
+
+__global__ void kb_homogenize(BatchViews b)
+{
+    BATCH_SLOT
+    homogenize_pin(g, st.phi, b.cv[slot], blockIdx.x * blockDim.x + threadIdx.x);
+}
+void launch_b_homogenize(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_homogenize<<<bgrid(b.max_pin, 64, b.cap), 64, 0, s>>>(b);
+}
+
+__global__ void kb_set_pin_flux(BatchViews b)
+{
+    BATCH_SLOT
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= g.n_pin * g.G) return;
+    int ig = idx / g.n_pin, ip = idx % g.n_pin;
+    double c = st.cflux[(size_t)ig * g.n_pin + g.pin_cell[ip]];
+    if (!(c > 0.0)) {
+        atomicOr(st.status, (unsigned)DEV_NONPOSITIVE_PIN_FLUX);
+        return;
+    }
+    double fm = 0.0;
+    int r0 = g.pin_first_reg[ip], r1 = g.pin_first_reg[ip + 1];
+    for (int r = r0; r < r1; r++) fm += st.phi[(size_t)ig * g.n_fsr + r] * g.fsr_area[r];
+    fm /= g.pin_area[ip];
+    double f = c / fm;
+    for (int r = r0; r < r1; r++) st.phi[(size_t)ig * g.n_fsr + r] *= f;
+}
+void launch_b_set_pin_flux(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_set_pin_flux<<<bgrid(b.max_pin * b.max_g, 256, b.cap), 256, 0, s>>>(b);
+}
+
+// Per solve: total fission of the new and the old flux
+// (transport_sweeper.cpp:104-117), k <- k * new / old, then the fission
+// source at the new k (eigen_solver.cpp:242-250). One CTA per solve.
+__global__ void kb_k_update(BatchViews b)
+{
+    __shared__ double scratch[64];
+    if ((int)blockIdx.x >= *b.n_act) return;
+    const int slot = b.act[blockIdx.x];
+    const GeomView &g = b.gv[slot];
+    const StateView &st = b.sv[slot];
+    const int G = g.G;
+    double tn = 0.0, to = 0.0;
+    for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
+        const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * G;
+        double v = g.fsr_vol[r];
+        for (int ig = 0; ig < G; ig++) {
+            tn += st.phi[(size_t)ig * g.n_fsr + r] * v * nf[ig];
+            to += st.phi_old[(size_t)ig * g.n_fsr + r] * v * nf[ig];
+        }
+    }
+    block_sum2(tn, to, scratch);
+    const double k = st.red[RED_K];
+    const double knew = k * tn / to;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st.red[RED_TF_NEW] = tn;
+        st.red[RED_TF_OLD] = to;
+        st.red[RED_K_PREV] = k;
+        st.red[RED_K] = knew;
+    }
+    const double rk = 1.0 / knew;
+    for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
+        const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * G;
+        double f = 0.0;
+        for (int ig = 0; ig < G; ig++) f += rk * nf[ig] * st.phi[(size_t)ig * g.n_fsr + r];
+        st.fs[r] = f;
+    }
+}
+void launch_b_k_update(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_k_update<<<b.cap, 256, 0, s>>>(b);
+}
+
+// Per solve: |k - k_prev| and the fission-source change after MOCC's
+// Normalize() of both sources (eigen_solver.cpp:171-184). One CTA per solve.
+__global__ void kb_errors(BatchViews b)
+{
+    __shared__ double scratch[64];
+    if ((int)blockIdx.x >= *b.n_act) return;
+    const int slot = b.act[blockIdx.x];
+    const GeomView &g = b.gv[slot];
+    const StateView &st = b.sv[slot];
+    double na = 0, sa = 0, nb = 0, sb = 0;
+    for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
+        double a = st.fs[r], c = st.fs_prev[r];
+        if (a > 0.0) na += 1.0;
+        sa += a;
+        if (c > 0.0) nb += 1.0;
+        sb += c;
+    }
+    block_sum2(na, sa, scratch);
+    block_sum2(nb, sb, scratch);
+    const double fa = na / sa, fb = nb / sb;
+    double acc = 0.0, dummy = 0.0;
+    for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
+        double e = st.fs[r] * fa - st.fs_prev[r] * fb;
+        acc += e * e;
+    }
+    block_sum2(acc, dummy, scratch);
+    if (threadIdx.x == 0) {
+        st.red[RED_ERR_K] = fabs(st.red[RED_K] - st.red[RED_K_PREV]);
+        st.red[RED_ERR_PSI] = sqrt(acc / st.red[RED_N_FISSILE]);
+        if (!isfinite(st.red[RED_K])) atomicOr(st.status, (unsigned)DEV_NAN);
+    }
+}
+void launch_b_errors(const BatchViews &b, cudaStream_t s)
+{
+    note_launch();
+    kb_errors<<<b.cap, 256, 0, s>>>(b);
+}
+
+__global__ void kb_summary(BatchViews b, double *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *b.n_act) return;
+    const int slot = b.act[i];
+    const StateView &st = b.sv[slot];
+    double *o = out + (size_t)slot * 6;
+    o[0] = st.red[RED_K];
+    o[1] = st.red[RED_ERR_K];
+    o[2] = st.red[RED_ERR_PSI];
+    o[3] = (double)*st.status;
+    o[4] = st.red[RED_CMFD_ITS];
+    o[5] = st.red[RED_HAS_RADIAL];
+}
+void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s)
+{
+    note_launch();
+    kb_summary<<<(b.cap + 127) / 128, 128, 0, s>>>(b, out);
 }
 
 } // namespace mocgpu

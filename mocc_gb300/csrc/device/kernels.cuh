@@ -50,11 +50,12 @@ struct GeomView {
 };
 
 struct StateView {
-    double *phi, *phi_old, *fs, *src1g;
+    double *phi, *phi_old, *fs, *fs_prev, *src1g;
     void *qbar, *sigt, *tally; // Real
     void *psi_in, *psi_out;    // Real
     double *cur, *sflux;       // [G][n_surf]
-    double *red;               // reduction scratch (64 doubles)
+    double *cflux;             // coarse (pin) flux [G][n_pin]
+    double *red;               // per-solve scalars and reduction scratch (64 doubles)
     unsigned *status;
 };
 
@@ -77,6 +78,7 @@ struct CmfdView {
     double *k;      // in/out
     double *stats;  // [0]=iterations, [1]=r0, [2]=ri/r0, [3]=psi_err, [4]=bicgstab its
     unsigned *status;
+    double *red;    // the solve's scalars (batched path reads RED_HAS_RADIAL here)
 };
 
 // Bundled work-unit layout of the fast sweep (see host/layout.hpp).
@@ -94,6 +96,62 @@ struct FastView {
     int split;            // forward and backward on separate warps
     int max_local;
 };
+
+// Per-solve scalars kept in device memory (StateView::red) so that batched
+// solves advance without host round trips.
+enum RedSlot {
+    RED_TFIS = 8,        // total fission scratch
+    RED_FLUXRES = 9,     // flux residual scratch
+    RED_PINRES = 10,     // set_pin_flux residual scratch
+    RED_K = 16,          // k
+    RED_K_PREV = 17,     // k of the previous outer
+    RED_TF_NEW = 18,     // total fission of the new flux
+    RED_TF_OLD = 19,     // total fission of the old flux
+    RED_PSI = 20,        // 20..24: fission-source change sums
+    RED_ERR_K = 25,      // |k - k_prev|
+    RED_ERR_PSI = 26,    // fission-source L2 change
+    RED_N_FISSILE = 27,  // fissile FSR count
+    RED_HAS_RADIAL = 28, // 1 once the sweep has tallied coarse currents
+    RED_CMFD_ITS = 29    // CMFD iterations accumulated
+};
+
+// Arrays of per-solve views for the batched kernels (device memory), and the
+// list of active solve slots. The active list and its length live in device
+// memory so that one captured graph serves every mix of active solves; grids
+// span `cap` solves and blocks past the active count return at once.
+struct BatchViews {
+    const GeomView *gv;
+    const StateView *sv;
+    const CmfdView *cv;
+    const FastView *fv;
+    const double *const *surf_area; // per slot: coarse surface areas
+    const int *act;                 // active slots
+    const int *n_act;               // number of active slots
+    int cap;                        // grid extent over solves
+    int max_fsr, max_pin, max_surf, max_cell, max_g;
+};
+
+// ---- batched launchers (one solve per blockIdx.y unless noted) ----
+void launch_b_fission_source(const BatchViews &b, cudaStream_t s);
+void launch_b_copy_old(const BatchViews &b, cudaStream_t s); // fs_prev = fs, phi_old = phi
+template <typename Real> void launch_b_group_source(const BatchViews &b, int group, cudaStream_t s);
+template <typename Real> void launch_b_epilogue(const BatchViews &b, int group, bool update_q, cudaStream_t s);
+void launch_b_zero_currents(const BatchViews &b, int group, cudaStream_t s);
+void launch_b_normalize_currents(const BatchViews &b, int group, cudaStream_t s);
+void launch_b_pin_flux(const BatchViews &b, cudaStream_t s);
+void launch_b_homogenize(const BatchViews &b, cudaStream_t s);
+void launch_b_set_pin_flux(const BatchViews &b, cudaStream_t s);
+void launch_b_k_update(const BatchViews &b, cudaStream_t s); // total fission ratio, k, then fs(k)
+void launch_b_errors(const BatchViews &b, cudaStream_t s);   // error_k, error_psi per solve
+// out[slot * 6 + {0..5}] = k, error_k, error_psi, status, CMFD iterations, has_radial
+void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s);
+void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
+template <typename Real>
+void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
+                    bool cur, int pol, int bundles_per_unit, int max_local, cudaStream_t s);
+// Sets the shared-memory limit of the batched sweep ahead of graph capture.
+template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local);
+void note_launches(int64_t n); // adds replayed launches to launch_count()
 
 // ---- launchers (stream-ordered) ----
 template <typename Real>

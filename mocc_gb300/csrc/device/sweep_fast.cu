@@ -10,6 +10,8 @@
 // ring with 16-byte cp.async copies, chunk c+1 landing while chunk c is swept.
 // After the bundles, the unit's tally is added to the global FSR tally with
 // one atomic per touched FSR.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace mocgpu {
@@ -28,9 +30,11 @@ __device__ __forceinline__ double att_fast(double tau, const double *tab)
 }
 __device__ __forceinline__ float att_fast(float tau, const double *)
 {
-    // 4-term Taylor series of 1 - e^{-tau} below 1/64, hardware exponential above
-    if (tau < 0.015625f) return tau * (1.0f - tau * (0.5f - tau * (0.16666667f - tau * 0.041666668f)));
-    return 1.0f - __expf(-tau);
+    // 4-term Taylor series of 1 - e^{-tau} below 1/64, hardware exponential
+    // above; both are evaluated and selected so a warp never diverges here
+    const float poly = tau * (1.0f - tau * (0.5f - tau * (0.16666667f - tau * 0.041666668f)));
+    const float hw = 1.0f - __expf(-tau);
+    return tau < 0.015625f ? poly : hw;
 }
 
 template <typename Real> struct Pair;
@@ -59,12 +63,12 @@ template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
 }
 
 template <typename Real, int NPOL, bool GS, bool CUR>
-__global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, int wu0)
+__device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv, const StateView &st, int group,
+                                           int wu, unsigned char *smem_raw)
 {
     using R2 = typename Pair<Real>::T;
     constexpr int CH = Chunk<Real>::rows;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const WorkUnitDev u = fv.wu[wu0 + blockIdx.x];
+    const WorkUnitDev u = fv.wu[wu];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     // [warp rings][(sigma_t, qbar) pairs][tally]
@@ -189,10 +193,48 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
             const Real *cl = ring_len + (size_t)(c & 1) * CH * 32;
             const uint16_t *cf = ring_fsr + (size_t)(c & 1) * CH * 32;
             const int nr = hi - lo;
-            for (int k = 0; k < nr; k++) {
+            // Four rows per step: the loads, gathers and attenuations of the
+            // four rows are independent and issue back to back; only the psi
+            // recurrence that follows is serial.
+            constexpr int U = 4;
+            int k = 0;
+            for (; k + U <= nr; k += U) {
+                Real L[U], e[U][NPOL];
+                int l[U];
+                R2 sq[U];
+#pragma unroll
+                for (int v = 0; v < U; v++) {
+                    const int j = fwd ? k + v : nr - 1 - (k + v);
+                    L[v] = cl[j * 32 + lane];
+                    l[v] = cf[j * 32 + lane];
+                }
+#pragma unroll
+                for (int v = 0; v < U; v++) sq[v] = s_sq[l[v]];
+#pragma unroll
+                for (int v = 0; v < U; v++) {
+                    const Real tau0 = sq[v].x * L[v];
+#pragma unroll
+                    for (int p = 0; p < NPOL; p++) e[v][p] = att_fast(tau0 * rsin[p], g.exp_tab);
+                }
+#pragma unroll
+                for (int v = 0; v < U; v++) {
+                    if (CUR && t >= 0) {
+                        const int j = fwd ? k + v : nr - 1 - (k + v);
+                        events(fwd ? lo + j : lo + j + 1);
+                    }
+                    Real acc = 0;
+#pragma unroll
+                    for (int p = 0; p < NPOL; p++) {
+                        Real d = (psi[p] - sq[v].y) * e[v][p];
+                        psi[p] -= d;
+                        acc += d * wt[p];
+                    }
+                    if (L[v] > (Real)0) atomicAdd(s_tal + l[v], acc);
+                }
+            }
+            for (; k < nr; k++) {
                 const int j = fwd ? k : nr - 1 - k; // row within the chunk
-                const int row = lo + j;
-                if (CUR && t >= 0) events(fwd ? row : row + 1);
+                if (CUR && t >= 0) events(fwd ? lo + j : lo + j + 1);
                 const Real L = cl[j * 32 + lane];
                 const int l = cf[j * 32 + lane];
                 const R2 sq = s_sq[l];
@@ -230,6 +272,105 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
     }
 }
 
+void note_launch_external();
+
+template <typename Real, int NPOL, bool GS, bool CUR>
+__global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, int wu0)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    sweep_unit<Real, NPOL, GS, CUR>(g, fv, st, group, wu0 + blockIdx.x, smem_raw);
+}
+
+// Persistent batched sweep: a fixed grid walks the (solve slot, work unit)
+// list of every active solve, largest units first.
+template <typename Real, int NPOL, bool GS, bool CUR>
+__global__ void kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = *n_items;
+    for (int it = blockIdx.x; it < n; it += gridDim.x) {
+        const int2 item = items[it];
+        sweep_unit<Real, NPOL, GS, CUR>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y, smem_raw);
+        __syncthreads();
+    }
+}
+
+template <typename Real> static size_t batched_smem(int bundles_per_unit, int max_local)
+{
+    return (size_t)(2 * bundles_per_unit) * ring_bytes<Real>() + (size_t)max_local * (3 * sizeof(Real));
+}
+
+template <typename Real, int NPOL, bool GS, bool CUR> static void prepare_batched(size_t smem)
+{
+    auto k = kb_sweep_fast<Real, NPOL, GS, CUR>;
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+}
+
+template <typename Real, int NPOL, bool GS, bool CUR>
+static void launch_batched(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group,
+                           int bundles_per_unit, int max_local, cudaStream_t s)
+{
+    auto k = kb_sweep_fast<Real, NPOL, GS, CUR>;
+    const int nwarps = 2 * bundles_per_unit;
+    const size_t smem = batched_smem<Real>(bundles_per_unit, max_local);
+    prepare_batched<Real, NPOL, GS, CUR>(smem);
+    int per_sm = 1;
+    MOCGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * nwarps, smem));
+    int dev = 0, sms = 152;
+    MOCGPU_CUDA(cudaGetDevice(&dev));
+    MOCGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int grid = std::max(1, std::min(max_items, sms * std::max(1, per_sm)));
+    k<<<grid, 32 * nwarps, smem, s>>>(b, items, n_items, group);
+}
+
+template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local)
+{
+    const size_t smem = batched_smem<Real>(bundles_per_unit, max_local);
+#define MOCGPU_P(NP)                                                                                                     if (pol == NP) {                                                                                                         prepare_batched<Real, NP, true, false>(smem);                                                                        prepare_batched<Real, NP, true, true>(smem);                                                                         prepare_batched<Real, NP, false, false>(smem);                                                                       prepare_batched<Real, NP, false, true>(smem);                                                                        return;                                                                                                          }
+    MOCGPU_P(1)
+    MOCGPU_P(2)
+    MOCGPU_P(3)
+    MOCGPU_P(4)
+#undef MOCGPU_P
+    throw Error(1, "unsupported number of polar angles per track set");
+}
+template void prepare_b_sweep<float>(int, int, int);
+template void prepare_b_sweep<double>(int, int, int);
+
+template <typename Real>
+void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
+                    bool cur, int pol, int bundles_per_unit, int max_local, cudaStream_t s)
+{
+    if (max_items <= 0) return;
+    note_launch_external();
+#define MOCGPU_B(NP)                                                                                                 \
+    if (pol == NP) {                                                                                                 \
+        if (gs && !cur) launch_batched<Real, NP, true, false>(b, items, n_items, max_items, group, bundles_per_unit,  \
+                                                              max_local, s);                                         \
+        else if (gs && cur) launch_batched<Real, NP, true, true>(b, items, n_items, max_items, group,               \
+                                                                 bundles_per_unit, max_local, s);                     \
+        else if (!gs && !cur) launch_batched<Real, NP, false, false>(b, items, n_items, max_items, group,           \
+                                                                     bundles_per_unit, max_local, s);                 \
+        else launch_batched<Real, NP, false, true>(b, items, n_items, max_items, group, bundles_per_unit, max_local,  \
+                                                   s);                                                               \
+        return;                                                                                                      \
+    }
+    MOCGPU_B(1)
+    MOCGPU_B(2)
+    MOCGPU_B(3)
+    MOCGPU_B(4)
+#undef MOCGPU_B
+    throw Error(1, "unsupported number of polar angles per track set");
+}
+template void launch_b_sweep<float>(const BatchViews &, const int2 *, const int *, int, int, bool, bool, int, int, int,
+                                    cudaStream_t);
+template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int *, int, int, bool, bool, int, int,
+                                     int, cudaStream_t);
+
 template <typename Real> size_t fast_sweep_smem(const FastView &fv)
 {
     int nwarps = 2 * fv.bundles_per_unit;
@@ -262,8 +403,6 @@ static void launch_np(const GeomView &g, const FastView &fv, const StateView &st
     else if (!gs && !cur) launch_one<Real, NPOL, false, false>(g, fv, st, group, wu0, wu1, s);
     else launch_one<Real, NPOL, false, true>(g, fv, st, group, wu0, wu1, s);
 }
-
-void note_launch_external();
 
 template <typename Real>
 void launch_sweep_fast(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,

@@ -5,13 +5,17 @@
 // src/solvers/fixed_source_solver.cpp, src/core/cmfd.cpp) with all arrays in
 // HBM and every per-iteration loop a device kernel. The host only sequences
 // launches and reads back a handful of scalars per outer iteration.
+//
+// A Sweeper owns the per-solve state (cross sections, scalar and angular
+// flux, sources, coarse data, CMFD working set) and shares a DeviceGeometry
+// with every other solve of the same traced lattice shape.
 #pragma once
 
 #include <memory>
 #include <vector>
 
-#include "../host/layout.hpp"
 #include "../host/problem.hpp"
+#include "geometry.hpp"
 #include "kernels.cuh"
 
 namespace mocgpu {
@@ -22,13 +26,16 @@ struct EigenResult {
     int converged = 0;
     double error_k = 0.0, error_psi = 0.0;
     double seconds = 0.0;
-    int64_t sweeps = 0;        // one-group sweeps (inner iterations) performed
+    int64_t sweeps = 0; // one-group sweeps (inner iterations) performed
     int64_t cmfd_iterations = 0;
 };
 
 class Sweeper {
   public:
-    Sweeper(const Problem &P, int precision, cudaStream_t stream = 0);
+    // xs, when given, replaces the problem's own cross sections (same
+    // material assignment, see cross_sections_from_xsl).
+    Sweeper(const Problem &P, int precision, cudaStream_t stream = 0,
+            std::shared_ptr<const DeviceGeometry> geo = nullptr, const CrossSections *xs = nullptr);
     ~Sweeper();
     Sweeper(const Sweeper &) = delete;
     Sweeper &operator=(const Sweeper &) = delete;
@@ -38,6 +45,7 @@ class Sweeper {
     const SolverOptions &options() const { return opts_; }
     SolverOptions &options() { return opts_; }
     cudaStream_t stream() const { return stream_; }
+    const std::shared_ptr<const DeviceGeometry> &geometry() const { return geo_; }
 
     // MoCSweeper / TransportSweeper duties
     void initialize();
@@ -56,6 +64,9 @@ class Sweeper {
     void pin_powers(double *out) const; // [ny][nx], normalised to n_fuel
     void get_currents(double *cur, double *sflux) const;
     void set_coarse_enabled(bool on) { coarse_enabled_ = on; }
+    bool coarse_enabled() const { return coarse_enabled_; }
+    bool has_radial() const { return has_radial_; }
+    void set_has_radial(bool v) { has_radial_ = v; }
 
     // CMFD + eigen solver
     void cmfd_solve(double &k); // EigenSolver::do_cmfd
@@ -73,16 +84,21 @@ class Sweeper {
     // and the number of sweep-kernel launches they took.
     double time_sweep(int g, int reps, int *launches);
 
-    // device memory footprint (bytes)
-    size_t device_bytes() const { return dev_bytes_; }
-    // sweep-only algorithmic traffic per group sweep (bytes)
-    double sweep_bytes() const;
+    // device memory footprint (bytes): per-solve state plus the geometry
+    size_t device_bytes() const { return dev_bytes_ + geo_->bytes(); }
+    size_t state_bytes() const { return dev_bytes_; }
+    // per-solve device bytes of a solve of f on a geometry with the given
+    // boundary-flux entries per group (what the constructor allocates)
+    static size_t state_bytes_for(const FlatProblem &f, int precision, int bc_per_group);
+    double sweep_bytes() const { return geo_->sweep_bytes(); }
+    int n_fissile() const { return n_fissile_; }
 
     const GeomView &geom() const { return gv_; }
     const StateView &state() const { return sv_; }
+    const CmfdView &cmfd_view() const { return cv_; }
+    const FastView &fast_view() const { return geo_->fv; }
 
   private:
-    template <typename Real> void sweep_impl(int g);
     void check_status();
     void launch_phase(int g, int phase, bool gs, bool cur);
     void launch_epilogue(int g, bool update_q);
@@ -91,45 +107,21 @@ class Sweeper {
     SolverOptions opts_;
     int precision_;
     cudaStream_t stream_;
+    std::shared_ptr<const DeviceGeometry> geo_;
     bool coarse_enabled_ = false;
     bool has_radial_ = false;
     int n_fissile_ = 0;
-    int phaseA_end_ = 0; // first track of octant-2 sets
     size_t dev_bytes_ = 0;
 
-    // geometry
-    DevBuf<int64_t> seg_begin_;
-    DevBuf<int> trk_bc0_, trk_bc1_, trk_set_, seg_fsr_, fsr_mat_, bc_off_, set_ny_, wt_tgt_;
-    DevBuf<double> seg_len_d_;
-    DevBuf<float> seg_len_f_;
-    DevBuf<double> fsr_vol_, fsr_area_, xstr_, xsnf_, xsf_, xsch_, scat_, exp_tab_;
-    DevBuf<SetPolar> sp_;
-    DevBuf<int> ev_fw_begin_, ev_fw_pt_, ev_fw_code_, ev_bw_begin_, ev_bw_pt_, ev_bw_code_;
-    DevBuf<int> pin_first_reg_, pin_cell_, pin_fuel_;
-    DevBuf<double> pin_area_, surf_area_, dx_, dy_;
+    // cross sections of this solve
+    DevBuf<double> xstr_, xsnf_, xsf_, xsch_, scat_;
     // state
     DevBuf<double> phi_, phi_old_, fs_, fs_prev_, src1g_, cur_, sflux_, red_;
     DevBuf<unsigned char> qbar_, sigt_, tally_, psi_in_, psi_out_;
     DevBuf<unsigned> status_;
     // CMFD
-    DevBuf<double> cflux_, hxs_, hscat_, dtil_, dhat_, stil_, shat_, cmat_, cfs_, cfs_old_, cvec_, ck_, cstats_;
+    DevBuf<double> cflux_, hxs_, hscat_, dtil_, dhat_, stil_, shat_, cmat_, cfs_, cfs_old_, cvec_, cstats_;
     DevBuf<double> pinbuf_;
-    std::vector<double> psi_init_;
-    // bundled work-unit layout
-    DevBuf<WorkUnitDev> wu_;
-    DevBuf<int64_t> bundle_row_;
-    DevBuf<int> bundle_nrows_, bundle_track_, local_fsr_;
-    DevBuf<float> blen_f_;
-    DevBuf<double> blen_d_;
-    DevBuf<uint16_t> blfsr_;
-    std::vector<int> phase_wu_;
-    FastView fv_{};
-
-  public:
-    double layout_padding = 0.0;
-    int layout_units = 0, layout_max_local = 0, layout_tracks_per_unit = 0;
-
-  private:
 
     GeomView gv_{};
     StateView sv_{};

@@ -218,4 +218,88 @@ std::unique_ptr<Problem> Problem::from_xml(const std::string &xml_text, const st
     return P;
 }
 
+CrossSections cross_sections_of(const FlatProblem &f)
+{
+    CrossSections x;
+    x.ng = f.ng;
+    x.xstr = f.xstr;
+    x.xsnf = f.xsnf;
+    x.xsf = f.xsf;
+    x.xsch = f.xsch;
+    x.scat = f.scat;
+    return x;
+}
+
+CrossSections cross_sections_from_xsl(const Problem &base, const std::string &xsl_text)
+{
+    MaterialLib lib = MaterialLib::from_xsl_text(xsl_text);
+    const MaterialLib &ref = base.mesh->mat_lib;
+    if (lib.ng != ref.ng) MOCGPU_THROW(4, "cross-section library has a different number of groups");
+    CrossSections x;
+    x.ng = lib.ng;
+    const int G = lib.ng;
+    for (const Material &old : ref.assigned) {
+        auto it = lib.by_name.find(old.name);
+        if (it == lib.by_name.end()) MOCGPU_THROW(4, "material not in library: " + old.name);
+        const Material &m = lib.lib[it->second];
+        if (m.fissile != old.fissile) MOCGPU_THROW(4, "library changes whether material " + old.name + " is fissile");
+        for (int g = 0; g < G; g++) {
+            x.xstr.push_back(m.xstr[g]);
+            x.xsnf.push_back(m.xsnf[g]);
+            x.xsf.push_back(m.xsf[g]);
+            x.xsch.push_back(m.xsch[g]);
+        }
+        x.scat.insert(x.scat.end(), m.scat.begin(), m.scat.end());
+    }
+    return x;
+}
+
+FlatProblem flat_without_tracks(const FlatProblem &f)
+{
+    FlatProblem c;
+    c.ng = f.ng;
+    c.n_fsr = f.n_fsr;
+    c.n_mat = f.n_mat;
+    c.ndir_oct = f.ndir_oct;
+    c.n_ang = f.n_ang;
+    c.n_sets = f.n_sets;
+    c.pol_per_set = f.pol_per_set;
+    c.nx = f.nx;
+    c.ny = f.ny;
+    c.n_pin = f.n_pin;
+    c.n_surf = f.n_surf;
+    c.n_fuel_2d = f.n_fuel_2d;
+    c.hz = f.hz;
+    for (int i = 0; i < 6; i++) c.bc[i] = f.bc[i];
+    c.n_tracks = f.n_tracks;
+    c.n_seg = f.n_seg;
+    c.max_seg = f.max_seg;
+    c.xstr = f.xstr;
+    c.xsnf = f.xsnf;
+    c.xsf = f.xsf;
+    c.xsch = f.xsch;
+    c.scat = f.scat;
+    c.fsr_mat = f.fsr_mat;
+    c.fsr_vol = f.fsr_vol;
+    c.fsr_area = f.fsr_area;
+    c.ang_ox = f.ang_ox;
+    c.ang_oy = f.ang_oy;
+    c.ang_oz = f.ang_oz;
+    c.ang_alpha = f.ang_alpha;
+    c.ang_theta = f.ang_theta;
+    c.ang_weight = f.ang_weight;
+    c.ang_rsintheta = f.ang_rsintheta;
+    c.set_nx = f.set_nx;
+    c.set_ny = f.set_ny;
+    c.set_first_track = f.set_first_track;
+    c.set_spacing = f.set_spacing;
+    c.dx = f.dx;
+    c.dy = f.dy;
+    c.pin_first_reg = f.pin_first_reg;
+    c.pin_cell = f.pin_cell;
+    c.pin_fuel = f.pin_fuel;
+    c.pin_area = f.pin_area;
+    return c;
+}
+
 } // namespace mocgpu

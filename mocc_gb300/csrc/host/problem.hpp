@@ -81,4 +81,23 @@ struct Problem {
                                              const std::string &base_dir);
 };
 
+// Macroscopic cross sections of every assigned material, dense order
+// [mat][g] and [mat][to][from] as in FlatProblem.
+struct CrossSections {
+    int ng = 0;
+    std::vector<double> xstr, xsnf, xsf, xsch, scat;
+};
+
+CrossSections cross_sections_of(const FlatProblem &f);
+
+// Cross sections for `base`'s material assignment (the <material id name>
+// list of its input) read from another .xsl library. The library must have
+// the same group count and leave every material's fissile flag unchanged,
+// since the fuel-pin map of the traced geometry depends on it.
+CrossSections cross_sections_from_xsl(const Problem &base, const std::string &xsl_text);
+
+// Copy of f without the per-track and per-segment arrays (what a solve keeps
+// once its geometry lives on the device).
+FlatProblem flat_without_tracks(const FlatProblem &f);
+
 } // namespace mocgpu

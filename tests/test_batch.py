@@ -1,0 +1,159 @@
+"""Batched solves: each solve in a batch gives the result it gives alone.
+
+The batch engine advances many independent eigenvalue solves together; the
+arithmetic of every solve is the single-solve arithmetic, only the launches
+are shared, so:
+
+* FP64 batched solves match the FP64 single-solve path (k to 1e-9 absolute,
+  pin powers to 1e-8 relative; the sums run in another order);
+* mixed-precision batched solves match the FP64 oracle within 10 pcm and
+  0.1 % pin power;
+* a solve's result does not depend on what else is in the batch (the FP32
+  tally's atomic order is the only difference: k within 0.05 pcm, pins 1e-5).
+"""
+import numpy as np
+import pytest
+
+import mocc_gb300 as m
+import oracle
+from mocc_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def pcm(k, k_ref):
+    return 1e5 * abs(k - k_ref) / k_ref
+
+
+def max_pin_err(p, p_ref):
+    p, p_ref = np.ravel(p), np.ravel(p_ref)
+    mask = p_ref > 0
+    return float(np.max(np.abs(p[mask] - p_ref[mask]) / p_ref[mask]))
+
+
+def _cases(n, seed=5, sizes=(1, 3, 7), precision="double"):
+    """Seeded lattice cases of mixed sizes and cross-section perturbations."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        size = int(sizes[i % len(sizes)])
+        out.append(W.lattice_case(size, 8, 0.05, precision, seed=1000 + i,
+                                  mod_factor=float(rng.uniform(0.9, 1.1)),
+                                  fuel_nf_factor=float(rng.uniform(0.95, 1.05))))
+    return out
+
+
+def _run(engine, problems, xsls=None):
+    ids = [engine.submit(P, x) for P, x in zip(problems, xsls or [None] * len(problems))]
+    engine.run()
+    res = [engine.take(i) for i in ids]
+    assert all(r is not None for r in res)
+    return res
+
+
+def test_fp64_batch_matches_single_solves():
+    cases = _cases(6)
+    probs = [m.Problem(x, s) for x, s in cases]
+    E = m.BatchEngine(precision=0, capacity=8, bundles_per_unit=1)
+    res = _run(E, probs)
+    for P, r in zip(probs, res):
+        assert r["error"] == 0, r["message"]
+        S = m.EigenSolver(P, 0)
+        ref = S.solve()
+        assert r["iterations"] == ref["iterations"]
+        assert r["converged"] == ref["converged"] == 1
+        assert abs(r["k"] - ref["k"]) < 1e-9
+        assert max_pin_err(r["pin_powers"], S.pin_powers()) < 1e-8
+
+
+def test_mixed_batch_matches_oracle():
+    cases = _cases(5, seed=9, precision="mixed")
+    probs = [m.Problem(x, s) for x, s in cases]
+    E = m.BatchEngine(precision=1, capacity=8, bundles_per_unit=2)
+    res = _run(E, probs)
+    for P, r in zip(probs, res):
+        assert r["error"] == 0, r["message"]
+        O = oracle.OracleSolver(P)
+        ref = O.solve()
+        assert r["converged"] == 1
+        assert pcm(r["k"], ref["k"]) < 10.0
+        assert max_pin_err(r["pin_powers"], O.pin_powers()) < 1e-3
+
+
+@pytest.mark.parametrize("precision,k_tol,pin_tol", [(0, 1e-11, 1e-10), (1, 5e-7, 1e-5)])
+def test_result_same_alone_and_in_the_mix(precision, k_tol, pin_tol):
+    pstr = "double" if precision == 0 else "mixed"
+    target = W.lattice_case(7, 8, 0.05, pstr, seed=77, mod_factor=1.03)
+    mix = _cases(11, seed=3, sizes=(1, 3, 7, 5), precision=pstr)
+    P = m.Problem(*target)
+    alone = _run(m.BatchEngine(precision=precision, capacity=4), [P])[0]
+    probs = [m.Problem(x, s) for x, s in mix[:5]] + [P] + [m.Problem(x, s) for x, s in mix[5:]]
+    E = m.BatchEngine(precision=precision, capacity=6)  # fewer slots than solves: continuous batching
+    res = _run(E, probs)
+    inmix = res[5]
+    assert alone["error"] == inmix["error"] == 0
+    if precision == 0:
+        assert alone["iterations"] == inmix["iterations"]
+    assert abs(alone["k"] - inmix["k"]) < k_tol
+    assert max_pin_err(inmix["pin_powers"], alone["pin_powers"]) < pin_tol
+    st = E.stats()
+    assert st["completed"] == len(probs) and st["active"] == 0 and st["queued"] == 0
+
+
+def test_shared_geometry_with_other_cross_sections():
+    xml, xsl = W.lattice_case(3, 8, 0.05, "double", seed=1)
+    base = m.Problem(xml, xsl)
+    xsl2 = W.lattice_case(3, 8, 0.05, "double", seed=1, mod_factor=1.07, fuel_nf_factor=0.97)[1]
+    E = m.BatchEngine(precision=0, capacity=4)
+    r = _run(E, [base, base], [None, xsl2])
+    assert E.stats()["geometries"] == 1
+    ref1 = m.EigenSolver(base, 0).solve()
+    ref2 = m.EigenSolver(m.Problem(xml, xsl2), 0).solve()
+    assert abs(r[0]["k"] - ref1["k"]) < 1e-9
+    assert abs(r[1]["k"] - ref2["k"]) < 1e-9
+    assert abs(ref1["k"] - ref2["k"]) > 1e-4  # the cross sections did change
+
+
+def test_memory_budget_gates_admission():
+    cases = _cases(4, sizes=(3,))
+    probs = [m.Problem(x, s) for x, s in cases]
+    E = m.BatchEngine(precision=0, capacity=8)
+    E.submit(probs[0])
+    E.step()
+    st = E.stats()
+    geom = st["geometry_bytes"]
+    state = st["bytes_in_use"] - geom
+    E.run()
+    assert geom > 0 and state > 0
+    # room for the geometry and about one and a half solves
+    E2 = m.BatchEngine(precision=0, capacity=8, mem_budget=2 * geom + 1.5 * state)
+    ids = [E2.submit(P) for P in probs]
+    peak = 0
+    while True:
+        n = E2.step()
+        peak = max(peak, n)
+        s2 = E2.stats()
+        assert s2["bytes_in_use"] <= s2["bytes_budget"]
+        if n == 0 and s2["queued"] == 0:
+            break
+    res = [E2.take(i) for i in ids]
+    assert all(r["error"] == 0 and r["converged"] == 1 for r in res)
+    assert 1 <= peak < len(probs)
+
+
+def test_solve_larger_than_budget_is_refused():
+    P = m.Problem(*W.lattice_case(7, 8, 0.05, "double", seed=2))
+    E = m.BatchEngine(precision=0, capacity=2, mem_budget=64 * 1024)
+    r = _run(E, [P])[0]
+    assert r["error"] == 21 and "budget" in r["message"]
+
+
+def test_batch_rejects_mismatched_configuration():
+    a = m.Problem(*W.pin3x3())
+    b = m.Problem(*W.pin3x3())
+    b.set_options(n_inner=2)
+    E = m.BatchEngine(precision=0, capacity=2)
+    E.submit(a)
+    with pytest.raises(m.MocgpuError) as e:
+        E.submit(b)
+    assert e.value.code == 1

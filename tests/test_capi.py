@@ -74,3 +74,12 @@ def test_sweeper_requires_a_gpu():
     with pytest.raises(m.MocgpuError) as e:
         m.MoCSweeper(P)
     assert e.value.code == 20
+
+
+def test_batch_engine_requires_a_gpu():
+    from conftest import has_gpu
+    if has_gpu():
+        pytest.skip("GPU present")
+    with pytest.raises(m.MocgpuError) as e:
+        m.BatchEngine(precision=1, capacity=4)
+    assert e.value.code == 20
