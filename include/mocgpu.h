@@ -34,7 +34,7 @@ extern "C" {
 #define MOCGPU_ERR_NAN 12           /* eigenvalue became NaN */
 #define MOCGPU_ERR_NOT_CONVERGED 13 /* iteration limit reached (result still valid) */
 #define MOCGPU_ERR_CUDA 20          /* CUDA runtime error (out of memory included) */
-#define MOCGPU_ERR_CAPACITY 21      /* serving admission: over the memory budget */
+#define MOCGPU_ERR_CAPACITY 21      /* over a memory budget or a fixed scratch size */
 #define MOCGPU_ERR_INTERNAL 99
 
 typedef struct mocgpu_problem mocgpu_problem; /* traced problem (host) */
@@ -156,6 +156,16 @@ int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surfa
 /* EigenSolver::do_cmfd (eigen_solver.cpp:263-291) incl. CMFD::solve
  * (cmfd.cpp:171-279); k is read and updated */
 int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
+/* mocgpu_cmfd_solve without allocation (no MOCC counterpart). The CMFD work
+ * vectors live in a fixed array inside the library (10 x 8192 doubles, 640
+ * KiB per device) instead of a buffer of the handle, so no call allocates
+ * device memory. The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. Meshes over 8192 coarse cells fail with
+ * MOCGPU_ERR_CAPACITY. Nothing in the array needs to start at zero. The
+ * array is shared by every handle in the process: calls that overlap in time
+ * on one device race on it and must be serialised by the caller. */
+int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k);
 /* EigenSolver::solve (eigen_solver.cpp:131-223): the whole power iteration.
  * max_outer < 0 uses <solver max_iter>. */
 int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);

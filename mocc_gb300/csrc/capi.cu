@@ -444,6 +444,13 @@ int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k)
         sw(s).cmfd_solve(*k);
     });
 }
+int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k)
+{
+    return guarded([&] {
+        REQUIRE(k, "null argument");
+        sw(s).cmfd_solve_static(*k);
+    });
+}
 int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out)
 {
     return guarded([&] {

@@ -6,6 +6,9 @@
 // single warp, so every reduction is a shuffle tree and every barrier a warp
 // barrier; larger meshes use up to 16 warps with one block barrier per
 // reduction. Work vectors live in shared memory when they fit.
+#include <mutex>
+#include <string>
+
 #include "kernels.cuh"
 
 namespace mocgpu {
@@ -464,6 +467,58 @@ void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
     }
     note_launch_external();
     k_cmfd_solve<<<1, 32 * nw, smem, s>>>(c, in_smem);
+}
+
+} // namespace mocgpu
+
+// ---------------------------------------------------------------------------
+// CMFD solve with its work vectors in a fixed module-scope array instead of
+// the handle's buffer: no allocation happens on any call. The array holds the
+// ten work vectors (right-hand side, group flux copy, eight BiCGSTAB vectors)
+// of meshes up to kStaticCmfdMaxCells coarse cells. The kernel writes every
+// entry it reads (BiCGSTAB zeroes its p and v itself), so nothing in the
+// array has to start at zero. All calls in the process share the array:
+// calls that overlap in time on the same device race on it.
+namespace mocgpu {
+
+constexpr int kStaticCmfdMaxCells = 8192;
+static __device__ __align__(256) double g_cmfd_static_scratch[10 * kStaticCmfdMaxCells];
+
+__global__ void k_cmfd_solve_static(CmfdView c) { cmfd_body(c, 0); }
+
+// Device address of the array, looked up once per device (with that device
+// current) on the first call that runs there.
+static double *static_scratch_address()
+{
+    static std::mutex mu;
+    static double *addr[64] = {nullptr};
+    int dev = 0;
+    MOCGPU_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error(20, "device ordinal out of range for the static CMFD scratch");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_cmfd_static_scratch);
+        if (e != cudaSuccess)
+            throw Error(20, std::string("cudaGetSymbolAddress of the static CMFD scratch failed: ") +
+                                cudaGetErrorString(e));
+        addr[dev] = static_cast<double *>(p);
+    }
+    return addr[dev];
+}
+
+int static_cmfd_max_cells() { return kStaticCmfdMaxCells; }
+
+void launch_cmfd_solve_static(const CmfdView &c, cudaStream_t s)
+{
+    if (c.n_cell > kStaticCmfdMaxCells)
+        throw Error(21, "coarse mesh has " + std::to_string(c.n_cell) + " cells; the static CMFD scratch holds " +
+                            std::to_string(kStaticCmfdMaxCells));
+    CmfdView v = c;
+    v.vec = static_scratch_address();
+    const int nw = cmfd_warps(c.n_cell);
+    note_launch_external();
+    k_cmfd_solve_static<<<1, 32 * nw, 128 * sizeof(double), s>>>(v);
 }
 
 } // namespace mocgpu

@@ -177,6 +177,11 @@ void launch_set_pin_flux(const GeomView &g, double *phi, const double *cflux, do
                          cudaStream_t s);
 void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, cudaStream_t s);
 void launch_cmfd_solve(const CmfdView &c, cudaStream_t s);
+// Same solve with the work vectors in a fixed module-scope array (no
+// allocation); meshes up to static_cmfd_max_cells() cells, calls must not
+// overlap in time on one device.
+void launch_cmfd_solve_static(const CmfdView &c, cudaStream_t s);
+int static_cmfd_max_cells();
 void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev, double *red, cudaStream_t s);
 void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s);
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);

@@ -415,6 +415,25 @@ void Sweeper::cmfd_solve(double &k)
     cmfd_iters += (int64_t)cmfd_stats[0];
 }
 
+void Sweeper::cmfd_solve_static(double &k)
+{
+    launch_pin_flux(gv_, phi_.p, cflux_.p, stream_);
+    launch_homogenize(gv_, phi_.p, cv_, stream_);
+    cv_.has_radial = has_radial_ ? 1 : 0;
+    cv_.k_tol = opts_.cmfd_k_tol;
+    cv_.psi_tol = opts_.cmfd_psi_tol;
+    cv_.resid_reduction = opts_.cmfd_resid_reduction;
+    cv_.max_iter = opts_.cmfd_max_iter;
+    cv_.fixup = opts_.cmfd_negative_fixup ? 1 : 0;
+    MOCGPU_CUDA(cudaMemcpyAsync(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_cmfd_solve_static(cv_, stream_);
+    launch_set_pin_flux(gv_, phi_.p, cflux_.p, nullptr, status_.p, stream_);
+    MOCGPU_CUDA(cudaMemcpyAsync(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(cudaMemcpyAsync(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
+    check_status();
+    cmfd_iters += (int64_t)cmfd_stats[0];
+}
+
 double Sweeper::psi_error()
 {
     launch_psi_error(gv_, fs_.p, fs_prev_.p, red_.p + RED_PSI, stream_);

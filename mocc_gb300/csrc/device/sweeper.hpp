@@ -70,6 +70,9 @@ class Sweeper {
 
     // CMFD + eigen solver
     void cmfd_solve(double &k); // EigenSolver::do_cmfd
+    // cmfd_solve with the CMFD work vectors in the library's fixed scratch
+    // array instead of this handle's buffer
+    void cmfd_solve_static(double &k);
     EigenResult eigen_solve(int max_outer = -1);
     void eigen_step(double &k, double &k_prev);
     double psi_error();
