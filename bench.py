@@ -1,28 +1,40 @@
 """Benchmark: k-eigenvalue MoC solves per second on one GB300.
 
-Default workload: the 17x17 pin assembly (264 fuel + 25 guide-tube cells,
-24 FSR/pin, 7 groups, 16 azimuths/octant, 3 polar, 0.03 cm spacing) solved
-with the mixed-precision path (FP32 sweep, FP64 k/fission source/CMFD), CMFD
-on, k_tol 1e-6, psi_tol 1e-5. One step = one full eigenvalue solve (flux
-initialisation through convergence). Cross sections are the seeded synthetic
-library (no benchmark data is used).
+Default workload (``--workload branch256``): 256 independent branch-case
+eigenvalue solves of uneven size, lattices drawn uniformly from {1x1, 3x3,
+7x7, 17x17} pins (24 FSR/pin), each perturbing moderator Sigma_t/scattering
+by U[0.9, 1.1] and fuel nu-Sigma_f by U[0.95, 1.05] of a seeded synthetic
+7-group library; 8 azimuths/octant (32 over 2pi), 3 Tabuchi-Yamamoto polar
+angles, 0.05 cm spacing, CMFD on the pin mesh, k_tol 1e-6, psi_tol 1e-5,
+n_inner 5, reflective boundaries. FP32 sweep, FP64 k/fission source/CMFD.
+One step = all 256 solves from flat-flux start to convergence through the
+batch engine (continuous batching, one captured CUDA graph per outer
+iteration, work-unit shape chosen by the autotuner).
 
 Printed JSON (one line, rank 0):
-  value        solves/s with the traced problem resident in HBM
-  e2e          solves/s through the C ABI from host buffers: sweeper creation
-               (host->device upload of tracks, cross sections, geometry),
-               the solve, and the device->host read of the pin powers
-  roofline     the sweep kernel: algorithmic bytes per launch / CUDA-event
-               duration, against the measured HBM copy bandwidth
-  cpu_baseline the CPU oracle (FP64 OpenMP restatement of MOCC's sweep) on the
-               same workload, all host threads
-The segment stream of this workload (~23 MB) fits in L2; L2 is flushed
-(256 MB write) before every timed solve.
+  value          solves/s: solves / device time of the graph replays (CUDA
+                 events on the engine's stream), inputs resident in HBM
+  e2e            solves/s through the public API from host buffers: submit
+                 (cross-section parse + upload, state initialisation), the
+                 solves, and the device->host read of k and pin powers
+  plain          the plain single-solve GPU path (one EigenSolver per case,
+                 same precision) over the same 256 cases, and the speed-up
+  serving        a Poisson request stream (lattice sizes weighted
+                 0.4/0.3/0.2/0.1, 7 or 23 groups): solves/s, p50/p99 latency
+  accuracy       k error (pcm) and max fuel-pin power error of the batched
+                 solves against the FP64 CPU oracle on one case per size
+  roofline       the batched sweep kernel: algorithmic bytes of its launches /
+                 their CUDA-event device time, against the measured HBM copy
+                 bandwidth
+  cpu_baseline   the CPU oracle (FP64 OpenMP restatement of MOCC) solving one
+                 case of each size with all host threads
+The segment streams of the 256 cases (about 0.4 GB) exceed the 129 MB L2,
+so no explicit L2 flush is needed between steps.
 
---impl reference times the reference's CPU algorithm (the oracle port, since
-MOCC itself cannot be built without its third-party dependencies) with all
-host threads on the same workload: each step is one outer iteration, scaled to
-solves/s by the outer-iteration count of a full solve.
+--impl reference times the reference's CPU algorithm (the oracle port:
+MOCC itself cannot be built without Blitz++, Eigen, pugixml and HDF5) with
+all host threads on the same workload: each step solves one case of each
+lattice size, reported as solves/s of that mixture.
 """
 from __future__ import annotations
 
@@ -39,6 +51,9 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+N_CASES = 256
+SIZES = (1, 3, 7, 17)
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -46,21 +61,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="assembly17", choices=["assembly17", "pin3x3", "minicore"])
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--workload", default="branch256", choices=["branch256", "assembly17"])
+    ap.add_argument("--cases", type=int, default=N_CASES)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle legs")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
     return ap.parse_args()
-
-
-def workload(name):
-    from mocc_gb300 import workloads as W
-    if name == "assembly17":
-        return W.assembly17(precision="mixed"), {"pins": "17x17 (264 fuel + 25 guide tube)", "groups": 7,
-                                                   "azimuthal_per_octant": 16, "polar": 3, "spacing_cm": 0.03}
-    if name == "pin3x3":
-        return W.pin3x3(precision="mixed"), {"pins": "3x3", "groups": 7, "azimuthal_per_octant": 8, "polar": 3,
-                                               "spacing_cm": 0.05}
-    return W.minicore(precision="mixed"), {"pins": "68x68 (3x3 fuel assemblies + reflector row)", "groups": 7,
-                                             "azimuthal_per_octant": 16, "polar": 3, "spacing_cm": 0.03}
 
 
 def dist_init(args):
@@ -91,6 +96,8 @@ def max_over_ranks(v, world):
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
     def __init__(self):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -108,12 +115,13 @@ class Clocks:
         self.p.terminate()
         self.p.wait()
         self.f.flush()
-        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        rows = [[c.strip() for c in r.split(",")] for r in Path(self.f.name).read_text().strip().splitlines()
+                if r.strip()]
         os.unlink(self.f.name)
-        sm = [float(r[1]) for r in rows if len(r) > 8 and r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if len(r) > 8 and r[2].strip().replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({n for r in rows if len(r) > 8 for n, v in zip(names, r[5:9]) if "Active" in v})
+        rows = [r for r in rows if len(r) > 8]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = sorted({n for r in rows for n, v in zip(self.NAMES, r[5:9]) if v == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
 
@@ -126,130 +134,264 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def pcm(k, k_ref):
+    return 1e5 * abs(k - k_ref) / k_ref
+
+
+def max_pin_err(p, p_ref):
+    import numpy as np
+    p, p_ref = np.ravel(p), np.ravel(p_ref)
+    mask = p_ref > 0
+    return float(np.max(np.abs(p[mask] - p_ref[mask]) / p_ref[mask]))
+
+
+def branch_workload(n_cases, seed=7):
+    """256 seeded branch cases; one traced base problem per lattice size."""
+    import mocc_gb300 as m
+    from mocc_gb300 import workloads as W
+    cases = W.branch_cases(n_cases, seed=seed)
+    bases = {}
+    for size, ng, xml, xsl in cases:
+        if (size, ng) not in bases:
+            bases[(size, ng)] = (m.Problem(xml, xsl), xml)
+    reqs = [(bases[(size, ng)][0], xsl) for size, ng, xml, xsl in cases]
+    return cases, bases, reqs
+
+
+CONFIG = {"workload": "branch256: 256 eigenvalue solves, lattices uniform over 1x1/3x3/7x7/17x17 pins",
+          "fsr_per_pin": 24, "groups": 7, "azimuthal": "32 over 2pi", "polar": "3 (Tabuchi-Yamamoto)",
+          "spacing_cm": 0.05, "perturbation": "moderator x U[0.9,1.1], fuel nu-Sigma_f x U[0.95,1.05]",
+          "cmfd": "pin mesh, BiCGSTAB", "tolerances": "k 1e-6, psi 1e-5", "n_inner": 5,
+          "precision": "FP32 sweep, FP64 k/fission source/CMFD",
+          "l2": "no flush: the 256 segment streams (~0.4 GB) exceed the 129 MB L2"}
+
+
+def oracle_sample(cases, per_size=1):
+    """(index, xml, xsl) of the first `per_size` cases of each lattice size."""
+    out, seen = [], {}
+    for i, (size, ng, xml, xsl) in enumerate(cases):
+        if seen.get(size, 0) < per_size:
+            seen[size] = seen.get(size, 0) + 1
+            out.append((i, xml, xsl))
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     import oracle
     import mocc_gb300 as m
-    (xml, xsl), cfg = workload(args.workload)
-    P = m.Problem(xml, xsl)
-    O = oracle.OracleSolver(P)
-    full = O.solve()  # outer-iteration count of a full solve (untimed)
-    n_outer = full["iterations"]
+    from mocc_gb300 import workloads as W
+    cases = W.branch_cases(args.cases, seed=7)
+    sample = oracle_sample(cases)
+    solvers = [oracle.OracleSolver(m.Problem(xml, xsl)) for _, xml, xsl in sample]
+
+    def step():
+        for O in solvers:
+            O.solve()
+
     for _ in range(args.warmup):
-        O.solve(max_outer=1)
+        step()
     times = []
     for _ in range(args.steps):
         t = time.perf_counter()
-        O.solve(max_outer=1)
+        step()
         times.append(time.perf_counter() - t)
-    t_outer = statistics.median(times)
-    v = 1.0 / (t_outer * n_outer)
+    t_step = statistics.median(times)
+    v = len(solvers) / t_step
     line = {"impl": "reference", "metric": "solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_outer,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, **cfg},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": O.threads, "kind": "port",
-                             "sample": f"one outer iteration per step x {n_outer} outers per solve"},
+            "config": CONFIG,
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": solvers[0].threads, "kind": "port",
+                             "sample": "each step: one full FP64 solve of one case of each lattice size "
+                                       "(1x1, 3x3, 7x7, 17x17)"},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, rank, world):
+def run_branch(args, rank, world):
     import numpy as np
     import torch
 
     import mocc_gb300 as m
+    from mocc_gb300 import workloads as W
+    from mocc_gb300.serve import Request, poisson_arrivals, serve
+    from mocc_gb300.tune import tune_bundles_per_unit
     m.load_library()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    (xml, xsl), cfg = workload(args.workload)
+    cases, bases, reqs = branch_workload(args.cases)
+    n = len(reqs)
+    n_pin_max = max(P.sizes["npin"] for P, _ in bases.values())
+
+    # work-unit shape: autotuned on a 64-case sample
+    tune = tune_bundles_per_unit(lambda b: m.BatchEngine(precision=1, capacity=64, bundles_per_unit=b),
+                                 reqs[:64])
+    bpu = tune["best"]
+    E = m.BatchEngine(precision=1, capacity=n, bundles_per_unit=bpu)
+
+    def batch():
+        ids = [E.submit(P, x) for P, x in reqs]
+        E.run()
+        return [E.take(i, n_pin_max) for i in ids]
+
+    for _ in range(args.warmup):
+        batch()
+    E.set_timing(True)
+    batch()  # capture the timing graph outside the timed region
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks = Clocks()
+    s0 = E.stats()
+    l0 = m.launch_count()
+    h0, d0 = m.copy_bytes()
+    t0 = time.perf_counter()
+    results = None
+    for _ in range(args.steps):
+        results = batch()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = m.launch_count() - l0
+    h1, d1 = m.copy_bytes()
+    s1 = E.stats()
+    barrier(world)
+    clk = clocks.stop()
+    replay_ms = max_over_ranks(s1["replay_ms"] - s0["replay_ms"], world)
+    wall = max_over_ranks(wall, world)
+    value = world * n * args.steps / (replay_ms / 1e3)
+    e2e = world * n * args.steps / wall
+    assert all(r["error"] == 0 and r["converged"] == 1 for r in results), [r for r in results if r["error"]][:2]
+    sweep_ms = s1["sweep_ms"] - s0["sweep_ms"]
+    sweep_launches = s1["sweep_launches"] - s0["sweep_launches"]
+    sweep_bytes = s1["sweep_bytes"] - s0["sweep_bytes"]
+    sgu = s1["sweep_sgu"] - s0["sweep_sgu"]
+    peak, peak_kind = measured_peaks()
+    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
+
+    # plain single-solve GPU path on the same cases (sequential, one handle each)
+    E.set_timing(False)
+    plain_t, plain_k = [], []
+    for P, x in reqs:
+        S = m.MoCSweeper(P, 1, xsl=x)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = m.EigenSolver(P, sweeper=S).solve()
+        torch.cuda.synchronize()
+        plain_t.append(time.perf_counter() - t)
+        plain_k.append(r["k"])
+        S.close()
+    plain = n / sum(plain_t)
+    k_vs_plain = max(pcm(r["k"], k) for r, k in zip(results, plain_k))
+
+    line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": replay_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {**CONFIG, "cases": n, "bundles_per_unit": bpu, "replicas": world},
+            "sgu_per_s": sgu / (sweep_ms / 1e3), "sgu_per_s_whole_replay": world * sgu / (replay_ms / 1e3),
+            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int((h1 - h0) / args.steps),
+                    "d2h_bytes_per_step": int((d1 - d0) / args.steps)},
+            "plain": {"value": plain, "unit": "solves/s", "speedup": value / plain, "speedup_e2e": e2e / plain,
+                      "k_max_diff_pcm_vs_batched": k_vs_plain,
+                      "what": "sequential EigenSolver solves of the same cases, FP32 sweep, one handle each"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "kb_sweep_fast",
+                         "bytes_per_launch": sweep_bytes / max(sweep_launches, 1),
+                         "ms_per_launch": sweep_ms / max(sweep_launches, 1), "peak_source": peak_kind,
+                         "sweep_share_of_replay": sweep_ms / (s1["replay_ms"] - s0["replay_ms"])},
+            "tuning": tune, "clocks": clk, "gpu_launches": int(launches),
+            "outer_iterations": int(sum(r["iterations"] for r in results))}
+
+    # served request stream
+    if not args.no_serve:
+        scases = W.branch_cases(512, seed=11, weights=(0.4, 0.3, 0.2, 0.1), groups=(7, 23))
+        sb = {}
+        for size, ng, xml, xsl in scases:
+            if (size, ng) not in sb:
+                sb[(size, ng)] = m.Problem(xml, xsl)
+        rate = 1000.0
+        arr = poisson_arrivals(len(scases), rate, seed=5)
+        rq = [Request(sb[(size, ng)], xsl, float(a)) for (size, ng, xml, xsl), a in zip(scases, arr)]
+        SE = m.BatchEngine(precision=1, capacity=256, bundles_per_unit=bpu)
+        serve(SE, rq[:64], n_pin_max)  # warm-up: captures
+        rep = serve(SE, rq, n_pin_max)
+        ok = all(r is not None and r["error"] == 0 for r in rep.results)
+        line["serving"] = {"rate_req_per_s": rate, "requests": len(rq), "solves_per_s": rep.solves_per_s,
+                           "p50_ms": rep.percentile_ms(50), "p99_ms": rep.percentile_ms(99), "all_ok": ok,
+                           "mix": "sizes 1/3/7/17 weighted 0.4/0.3/0.2/0.1, groups 7 or 23",
+                           "budget": "80% of free device memory"}
+        SE.close()
+
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        sample = oracle_sample(cases)
+        errs, tcpu, cores = [], 0.0, None
+        for i, xml, xsl in sample:
+            O = oracle.OracleSolver(m.Problem(xml, xsl))
+            t = time.perf_counter()
+            ro = O.solve()
+            tcpu += time.perf_counter() - t
+            cores = O.threads
+            errs.append((cases[i][0], pcm(results[i]["k"], ro["k"]), max_pin_err(results[i]["pin_powers"],
+                                                                                  O.pin_powers())))
+        line["accuracy"] = {"vs": "FP64 CPU oracle, same inputs", "cases": [
+            {"size": s, "k_err_pcm": e, "max_pin_err": p} for s, e, p in errs],
+            "k_err_pcm_max": max(e for _, e, _ in errs), "max_pin_err": max(p for _, _, p in errs),
+            "tolerance": {"k_pcm": 10.0, "pin": 1e-3}}
+        line["cpu_baseline"] = {"value": len(sample) / tcpu, "unit": "solves/s", "cores": cores, "kind": "port",
+                                "sample": "one full FP64 solve of one case of each lattice size (1x1, 3x3, 7x7, "
+                                          "17x17) with all host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_assembly17(args, rank, world):
+    """Single 17x17 assembly solve per step (mixed precision)."""
+    import numpy as np
+    import torch
+
+    import mocc_gb300 as m
+    from mocc_gb300 import workloads as W
+    m.load_library()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    xml, xsl = W.assembly17(precision="mixed")
     P = m.Problem(xml, xsl)
     S = m.MoCSweeper(P, 1)
     E = m.EigenSolver(P, sweeper=S)
     stream = torch.cuda.ExternalStream(S.stream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def solve_once():
-        r = E.solve()
-        assert r["converged"], r
-        return r
-
     for _ in range(args.warmup):
-        solve_once()
-    barrier(world)
+        E.solve()
     torch.cuda.synchronize()
     clocks = Clocks()
     l0 = m.launch_count()
-    ms_steps, results = [], []
+    ms_steps, r = [], None
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        results.append(solve_once())
+        r = E.solve()
         e1.record(stream)
         e1.synchronize()
         ms_steps.append(e0.elapsed_time(e1))
-    torch.cuda.synchronize()
     launches = m.launch_count() - l0
-    barrier(world)
     clk = clocks.stop()
-    total_ms = max_over_ranks(sum(ms_steps), world)
-    value = world * args.steps / (total_ms / 1e3)
-    r0 = results[-1]
-    sgu = P.sizes["nseg"] * r0["sweeps"] / (statistics.median(ms_steps) / 1e3)
-
-    # end to end through the C ABI from host buffers
+    value = args.steps / (sum(ms_steps) / 1e3)
     db, sweep_bytes = S.bytes()
-    pins = None
-    e2e_t = []
-    for i in range(max(2, args.steps)):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        S2 = m.MoCSweeper(P, 1)
-        r = m.EigenSolver(P, sweeper=S2).solve()
-        pins = S2.pin_powers()
-        S2.close()
-        torch.cuda.synchronize()
-        e2e_t.append(time.perf_counter() - t)
-    e2e_v = world / max_over_ranks(statistics.median(e2e_t), world)
-    h2d = db  # device arrays uploaded or initialised at creation
-    d2h = pins.nbytes + 8 * 8
-
-    # sweep-kernel roofline (CUDA events around the sweep launches only)
-    reps = 20
-    ms, nl = S.time_sweep(0, reps)
-    per_launch_ms = ms / nl
-    bytes_per_launch = sweep_bytes / (nl / reps)
-    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    ms, nl = S.time_sweep(0, 20)
+    achieved = sweep_bytes / (ms / nl * 2 / 1e3) / 1e9 if nl else None
     peak, peak_kind = measured_peaks()
-
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.median(ms_steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": args.workload, **cfg, "precision": "FP32 sweep, FP64 k/fs/CMFD",
-                       "l2": "flushed (256 MB write) before each timed solve", "replicas": world},
-            "sgu_per_s": sgu, "outer_iterations": r0["iterations"], "sweeps_per_solve": r0["sweeps"],
-            "k": r0["k"],
-            "e2e": {"value": e2e_v, "unit": "solves/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_sweep", "bytes_per_launch": bytes_per_launch,
-                         "ms_per_launch": per_launch_ms, "peak_source": peak_kind},
+            "config": {"workload": "assembly17: 17x17 assembly, 16 azimuths/octant, 3 polar, 0.03 cm",
+                       "l2": "flushed (256 MB write) before each timed solve"},
+            "k": r["k"], "outer_iterations": r["iterations"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": None, "kernel": "k_sweep_fast",
+                         "peak_source": peak_kind},
             "clocks": clk, "gpu_launches": int(launches)}
-    if rank == 0 and not args.no_cpu:
-        import oracle
-        O = oracle.OracleSolver(P)
-        t = time.perf_counter()
-        ro = O.solve()
-        tc = time.perf_counter() - t
-        line["cpu_baseline"] = {"value": 1.0 / tc, "unit": "solves/s", "cores": O.threads, "kind": "port",
-                                "sample": "one full FP64 solve of the same workload"}
-        po = O.pin_powers()
-        pg = S.pin_powers() if pins is None else pins
-        mask = po > 0
-        line["k_err_pcm"] = 1e5 * abs(r0["k"] - ro["k"]) / ro["k"]
-        line["max_pin_err"] = float(np.max(np.abs(pg[mask] - po[mask]) / po[mask]))
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -259,8 +401,10 @@ def main():
     rank, world = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "assembly17":
+        run_assembly17(args, rank, world)
     else:
-        run_ours(args, rank, world)
+        run_branch(args, rank, world)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

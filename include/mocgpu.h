@@ -121,6 +121,11 @@ int mocgpu_trace_ray(const char *xml_text, const char *xsl_text, double x1, doub
  * precision: 0 = FP64 sweep, 1 = FP32 sweep with FP64 reductions and CMFD,
  *            -1 = the <sweeper precision> of the input (default FP64). ---- */
 int mocgpu_sweeper_create(const mocgpu_problem *p, int precision, mocgpu_sweeper **out);
+/* mocgpu_sweeper_create with the cross sections of another .xsl library
+ * for p's materials (same names, groups and fissile flags); NULL or empty
+ * xsl_text uses p's own. No MOCC counterpart (MOCC reads one library per
+ * input). */
+int mocgpu_sweeper_create_xsl(const mocgpu_problem *p, int precision, const char *xsl_text, mocgpu_sweeper **out);
 void mocgpu_sweeper_destroy(mocgpu_sweeper *s);
 int mocgpu_sweeper_set_options(mocgpu_sweeper *s, const mocgpu_options *in);
 /* MoCSweeper::initialize (moc_sweeper.cpp:234-253): phi = 1, psi = 1/4pi */
@@ -221,7 +226,12 @@ typedef struct mocgpu_batch_stats {
     int64_t submitted, completed, outer_iterations, graph_replays, captures;
     int active, queued, capacity, geometries, bundles_per_unit;
     double bytes_in_use, bytes_budget, geometry_bytes;
-    double now; /* engine clock, seconds */
+    double now;           /* engine clock, seconds */
+    double replay_ms;     /* device time of all graph replays */
+    double sweep_ms;      /* device time of the sweep launches in them (timing on) */
+    int64_t sweep_launches;
+    double sweep_bytes;   /* algorithmic bytes of the timed sweep launches */
+    int64_t sweep_sgu;    /* segment-group updates of the timed sweep launches */
 } mocgpu_batch_stats;
 
 /* precision: 0 FP64 sweep, 1 FP32 sweep (mixed); capacity: solves advanced
@@ -247,6 +257,11 @@ int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_resu
 int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out);
 /* The CUDA stream (cudaStream_t) of the engine's launches. */
 int mocgpu_batch_stream(mocgpu_batch *b, void **stream);
+/* on != 0: CUDA events around every sweep launch of the graph (re-captured),
+ * so the stats report the sweep kernels' device time and bytes. */
+int mocgpu_batch_set_timing(mocgpu_batch *b, int on);
+/* Host<->device bytes the library has copied in this process so far. */
+int mocgpu_copy_bytes(int64_t *h2d, int64_t *d2h);
 
 #ifdef __cplusplus
 }

@@ -64,7 +64,8 @@ class _BatchStats(C.Structure):
                 ("graph_replays", C.c_int64), ("captures", C.c_int64), ("active", C.c_int), ("queued", C.c_int),
                 ("capacity", C.c_int), ("geometries", C.c_int), ("bundles_per_unit", C.c_int),
                 ("bytes_in_use", C.c_double), ("bytes_budget", C.c_double), ("geometry_bytes", C.c_double),
-                ("now", C.c_double)]
+                ("now", C.c_double), ("replay_ms", C.c_double), ("sweep_ms", C.c_double),
+                ("sweep_launches", C.c_int64), ("sweep_bytes", C.c_double), ("sweep_sgu", C.c_int64)]
 
 
 def library_path() -> Path:
@@ -99,6 +100,7 @@ def load_library(build: bool = True):
         "mocgpu_synthetic_xsl": (I, [C.c_uint64, I, I, DP, D, D, C.c_char_p, C.c_int64, I64P]),
         "mocgpu_trace_ray": (I, [CP, CP, D, D, D, D, IP, DP, IP, I, IP, IP, IP, I]),
         "mocgpu_sweeper_create": (I, [P, I, C.POINTER(P)]),
+        "mocgpu_sweeper_create_xsl": (I, [P, I, CP, C.POINTER(P)]),
         "mocgpu_sweeper_destroy": (None, [P]),
         "mocgpu_sweeper_set_options": (I, [P, C.POINTER(_Options)]),
         "mocgpu_initialize": (I, [P]),
@@ -131,6 +133,8 @@ def load_library(build: bool = True):
         "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
         "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
         "mocgpu_batch_stream": (I, [P, C.POINTER(C.c_void_p)]),
+        "mocgpu_batch_set_timing": (I, [P, I]),
+        "mocgpu_copy_bytes": (I, [I64P, I64P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -254,14 +258,19 @@ class MoCSweeper:
     """Device-resident MoC sweeper (MOCC's MoCSweeper API).
 
     ``precision``: 0 = FP64 sweep, 1 = FP32 sweep with FP64 reductions and
-    CMFD, -1 = the ``<sweeper precision>`` of the input.
+    CMFD, -1 = the ``<sweeper precision>`` of the input. ``xsl``: another
+    cross-section library for the problem's materials (the traced geometry
+    is reused).
     """
 
-    def __init__(self, problem: Problem, precision: int = -1):
+    def __init__(self, problem: Problem, precision: int = -1, xsl: str | None = None):
         self.problem = problem
         self._lib = load_library()
         h = C.c_void_p()
-        _check(self._lib.mocgpu_sweeper_create(problem.handle, precision, C.byref(h)))
+        if xsl:
+            _check(self._lib.mocgpu_sweeper_create_xsl(problem.handle, precision, xsl.encode(), C.byref(h)))
+        else:
+            _check(self._lib.mocgpu_sweeper_create(problem.handle, precision, C.byref(h)))
         self._h = h
         s = problem.sizes
         self.n_group, self.n_reg, self.n_pin = s["ngroup"], s["nfsr"], s["npin"]
@@ -373,6 +382,13 @@ class MoCSweeper:
         return ms.value, nl.value
 
 
+def copy_bytes() -> tuple[int, int]:
+    """(host->device, device->host) bytes the library has copied so far."""
+    h, d = C.c_int64(), C.c_int64()
+    _check(load_library().mocgpu_copy_bytes(C.byref(h), C.byref(d)))
+    return h.value, d.value
+
+
 def launch_count() -> int:
     n = C.c_int64()
     _check(load_library().mocgpu_launch_count(C.byref(n)))
@@ -458,3 +474,6 @@ class BatchEngine:
         p = C.c_void_p()
         _check(self._lib.mocgpu_batch_stream(self._h, C.byref(p)))
         return p.value or 0
+
+    def set_timing(self, on: bool = True):
+        _check(self._lib.mocgpu_batch_set_timing(self._h, 1 if on else 0))

@@ -307,6 +307,29 @@ int mocgpu_sweeper_create(const mocgpu_problem *p, int precision, mocgpu_sweeper
     });
 }
 
+int mocgpu_sweeper_create_xsl(const mocgpu_problem *p, int precision, const char *xsl_text, mocgpu_sweeper **out)
+{
+    return guarded([&] {
+        REQUIRE(p && out, "null argument");
+        REQUIRE(precision >= -1 && precision <= 1, "precision must be -1, 0 or 1");
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+            throw mocgpu::Error(MOCGPU_ERR_CUDA, "no CUDA device available: the sweeper runs on the GPU only");
+        std::unique_ptr<mocgpu::CrossSections> xs;
+        if (xsl_text && *xsl_text)
+            xs = std::make_unique<mocgpu::CrossSections>(mocgpu::cross_sections_from_xsl(*p->P, xsl_text));
+        auto h = std::make_unique<mocgpu_sweeper>();
+        MOCGPU_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        try {
+            h->S = std::make_unique<mocgpu::Sweeper>(*p->P, precision, h->stream, nullptr, xs.get());
+        } catch (...) {
+            cudaStreamDestroy(h->stream);
+            throw;
+        }
+        *out = h.release();
+    });
+}
+
 void mocgpu_sweeper_destroy(mocgpu_sweeper *s)
 {
     if (!s) return;
@@ -661,6 +684,24 @@ int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out)
         out->bytes_budget = (double)s.bytes_budget;
         out->geometry_bytes = (double)s.geometry_bytes;
         out->now = E.now();
+        out->replay_ms = s.replay_ms;
+        out->sweep_ms = s.sweep_ms;
+        out->sweep_launches = s.sweep_launches;
+        out->sweep_bytes = s.sweep_bytes;
+        out->sweep_sgu = s.sweep_sgu;
+    });
+}
+
+int mocgpu_batch_set_timing(mocgpu_batch *b, int on)
+{
+    return guarded([&] { eng(b).set_timing(on != 0); });
+}
+
+int mocgpu_copy_bytes(int64_t *h2d, int64_t *d2h)
+{
+    return guarded([&] {
+        REQUIRE(h2d && d2h, "null argument");
+        mocgpu::copy_bytes(h2d, d2h);
     });
 }
 

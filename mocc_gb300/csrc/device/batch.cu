@@ -36,7 +36,20 @@ BatchEngine::BatchEngine(int precision, int capacity, size_t mem_budget, int bun
     d_nact_.zero(stream_);
     d_sum_.alloc((size_t)cap_ * 6);
     MOCGPU_CUDA(cudaMallocHost((void **)&h_sum_, sizeof(double) * 6 * (size_t)cap_));
+    MOCGPU_CUDA(cudaEventCreate(&rep0_));
+    MOCGPU_CUDA(cudaEventCreate(&rep1_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void BatchEngine::set_timing(bool on)
+{
+    if (on == timing_) return;
+    timing_ = on;
+    captured_ = Shape{}; // force a new capture
+    if (exec_) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
 }
 
 BatchEngine::~BatchEngine()
@@ -44,6 +57,9 @@ BatchEngine::~BatchEngine()
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (h_sum_) cudaFreeHost(h_sum_);
+    for (cudaEvent_t e : tev_) cudaEventDestroy(e);
+    if (rep0_) cudaEventDestroy(rep0_);
+    if (rep1_) cudaEventDestroy(rep1_);
 }
 
 double BatchEngine::now() const { return wall_seconds() - t0_; }
@@ -173,7 +189,7 @@ bool BatchEngine::try_admit(Pending &p)
     init[RED_K - RED_K] = 1.0;                          // RED_K
     init[RED_K_PREV - RED_K] = 1.0;                     // RED_K_PREV
     init[RED_N_FISSILE - RED_K] = (double)sw.n_fissile(); // RED_N_FISSILE
-    MOCGPU_CUDA(cudaMemcpyAsync(sw.state().red + RED_K, init, sizeof(double) * 14, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(sw.state().red + RED_K, init, sizeof(double) * 14, cudaMemcpyHostToDevice, stream_));
     sw.calc_fission_source(1.0);
 
     // shape of the captured graph
@@ -271,21 +287,21 @@ void BatchEngine::rebuild_lists()
             nitems[(size_t)g * 2 + ph] = n;
         }
     }
-    MOCGPU_CUDA(cudaMemcpyAsync(d_gv_.p, gv.data(), sizeof(GeomView) * cap_, cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(d_sv_.p, sv.data(), sizeof(StateView) * cap_, cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(d_cv_.p, cv.data(), sizeof(CmfdView) * cap_, cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(d_fv_.p, fv.data(), sizeof(FastView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(d_gv_.p, gv.data(), sizeof(GeomView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(d_sv_.p, sv.data(), sizeof(StateView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(d_cv_.p, cv.data(), sizeof(CmfdView) * cap_, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(d_fv_.p, fv.data(), sizeof(FastView) * cap_, cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(
-        cudaMemcpyAsync(d_area_.p, area.data(), sizeof(const double *) * cap_, cudaMemcpyHostToDevice, stream_));
+        copy_async(d_area_.p, area.data(), sizeof(const double *) * cap_, cudaMemcpyHostToDevice, stream_));
     int nact = (int)act_.size();
     if (nact)
-        MOCGPU_CUDA(cudaMemcpyAsync(d_act_.p, act_.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(d_nact_.p, &nact, sizeof(int), cudaMemcpyHostToDevice, stream_));
+        MOCGPU_CUDA(copy_async(d_act_.p, act_.data(), sizeof(int) * nact, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(d_nact_.p, &nact, sizeof(int), cudaMemcpyHostToDevice, stream_));
     for (int ph = 0; ph < 2; ph++)
         if (!items[ph].empty())
-            MOCGPU_CUDA(cudaMemcpyAsync(d_items_.p + (size_t)ph * shape_.items_cap, items[ph].data(),
+            MOCGPU_CUDA(copy_async(d_items_.p + (size_t)ph * shape_.items_cap, items[ph].data(),
                                         sizeof(int2) * items[ph].size(), cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(d_nitems_.p, nitems.data(), sizeof(int) * nitems.size(), cudaMemcpyHostToDevice,
+    MOCGPU_CUDA(copy_async(d_nitems_.p, nitems.data(), sizeof(int) * nitems.size(), cudaMemcpyHostToDevice,
                                 stream_));
     // pageable sources: wait for the copies before the host vectors go away
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
@@ -321,6 +337,14 @@ void BatchEngine::capture()
     if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local);
     else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local);
 
+    const int n_sweeps = shape_.max_g * n_inner_ * 2;
+    if (timing_)
+        while ((int)tev_.size() < 2 * n_sweeps) {
+            cudaEvent_t e;
+            MOCGPU_CUDA(cudaEventCreate(&e));
+            tev_.push_back(e);
+        }
+    tev_used_ = 0;
     const int64_t l0 = launch_count();
     MOCGPU_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     try {
@@ -342,12 +366,19 @@ void BatchEngine::capture()
                 for (int ph = 0; ph < 2; ph++) {
                     const int2 *items = d_items_.p + (size_t)ph * shape_.items_cap;
                     const int *nit = d_nitems_.p + (size_t)g * 2 + ph;
+                    if (timing_)
+                        MOCGPU_CUDA(cudaEventRecordWithFlags(tev_[2 * tev_used_], stream_, cudaEventRecordExternal));
                     if (precision_ == 0)
                         launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
                                                shape_.max_local, stream_);
                     else
                         launch_b_sweep<float>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
                                               shape_.max_local, stream_);
+                    if (timing_) {
+                        MOCGPU_CUDA(
+                            cudaEventRecordWithFlags(tev_[2 * tev_used_ + 1], stream_, cudaEventRecordExternal));
+                        tev_used_++;
+                    }
                 }
                 if (precision_ == 0) launch_b_epilogue<double>(b, g, !last, stream_);
                 else launch_b_epilogue<float>(b, g, !last, stream_);
@@ -398,12 +429,32 @@ int BatchEngine::step()
     if (act_.empty()) return 0;
     if (!exec_ || shape_ != captured_) capture();
 
+    MOCGPU_CUDA(cudaEventRecord(rep0_, stream_));
     MOCGPU_CUDA(cudaGraphLaunch(exec_, stream_));
+    MOCGPU_CUDA(cudaEventRecord(rep1_, stream_));
     note_launches(graph_nodes_);
-    MOCGPU_CUDA(cudaMemcpyAsync(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     st_.graph_replays++;
     st_.outer_iterations += (int64_t)act_.size();
+    {
+        float ms = 0.f;
+        MOCGPU_CUDA(cudaEventElapsedTime(&ms, rep0_, rep1_));
+        st_.replay_ms += ms;
+    }
+    if (timing_) {
+        for (int i = 0; i < tev_used_; i++) {
+            float ms = 0.f;
+            MOCGPU_CUDA(cudaEventElapsedTime(&ms, tev_[2 * i], tev_[2 * i + 1]));
+            st_.sweep_ms += ms;
+        }
+        st_.sweep_launches += tev_used_;
+        for (int s : act_) {
+            const DeviceGeometry &geo = *slots_[s].geo;
+            st_.sweep_bytes += (double)geo.G * n_inner_ * geo.sweep_bytes();
+            st_.sweep_sgu += (int64_t)geo.G * n_inner_ * geo.n_seg;
+        }
+    }
 
     const std::vector<int> act = act_;
     for (int s : act) {

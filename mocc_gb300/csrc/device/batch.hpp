@@ -40,6 +40,11 @@ struct BatchStats {
     int active = 0, queued = 0, capacity = 0;
     size_t bytes_in_use = 0, bytes_budget = 0, geometry_bytes = 0;
     int geometries = 0, bundles_per_unit = 0;
+    double replay_ms = 0.0;      // device time of all graph replays (CUDA events on the engine stream)
+    double sweep_ms = 0.0;       // device time of the sweep launches inside them (timing on)
+    int64_t sweep_launches = 0;  // sweep launches timed
+    double sweep_bytes = 0.0;    // algorithmic bytes of the timed sweep launches
+    int64_t sweep_sgu = 0;       // segment-group updates of the timed sweep launches
 };
 
 class BatchEngine {
@@ -65,6 +70,9 @@ class BatchEngine {
     bool take_result(int64_t id, BatchResult &out);
     BatchStats stats() const;
     double now() const; // engine clock (s)
+    // Records CUDA events around every sweep launch of the captured graph so
+    // that stats() reports the sweep kernels' own device time.
+    void set_timing(bool on);
     cudaStream_t stream() const { return stream_; }
 
   private:
@@ -132,6 +140,10 @@ class BatchEngine {
     bool lists_dirty_ = true;
 
     // graph and the sizes it was captured for
+    bool timing_ = false;
+    std::vector<cudaEvent_t> tev_; // before/after pairs around sweep launches
+    int tev_used_ = 0;
+    cudaEvent_t rep0_ = nullptr, rep1_ = nullptr;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     int64_t graph_nodes_ = 0;

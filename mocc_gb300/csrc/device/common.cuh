@@ -27,6 +27,14 @@ enum DeviceStatus : unsigned {
     DEV_CMFD_NOT_CONVERGED = 1u << 3,
 };
 
+// Host<->device bytes moved by the library (reported by the C ABI).
+void note_copy_bytes(cudaMemcpyKind kind, size_t bytes);
+inline cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s)
+{
+    note_copy_bytes(kind, bytes);
+    return cudaMemcpyAsync(dst, src, bytes, kind, s);
+}
+
 template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
@@ -49,7 +57,10 @@ template <typename T> struct DevBuf {
     void upload(const T *h, size_t count)
     {
         alloc(count);
-        if (count) MOCGPU_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+        if (count) {
+            note_copy_bytes(cudaMemcpyHostToDevice, count * sizeof(T));
+            MOCGPU_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+        }
     }
     template <typename V> void upload(const V &v) { upload(v.data(), v.size()); }
     void zero(cudaStream_t s = 0)

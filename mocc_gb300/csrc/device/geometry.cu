@@ -319,13 +319,15 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
 
 double DeviceGeometry::sweep_bytes() const
 {
-    // one group sweep: segment stream read once (length + 16-bit unit-local
-    // FSR id in the bundled layout), Sigma_t/qbar read and phi written per FSR,
-    // boundary psi in and out for every polar angle of every track
+    // one group sweep, algorithmic: the segment stream read once (length +
+    // int32 FSR id), Sigma_t/qbar read and phi written per FSR, boundary psi
+    // in and out for every polar angle of every track. (The bundled layout
+    // stores a 16-bit unit-local FSR id, so it moves fewer bytes per segment
+    // but adds padding rows.)
     const double rb = precision == 0 ? 8.0 : 4.0;
     double psi = 0.0;
     for (int s = 0; s < n_sets; s++) psi += (double)(set_nx[s] + set_ny[s]) * pol * 2;
-    return (rb + 2.0) * (double)n_seg + 3.0 * rb * n_fsr + 2.0 * rb * psi;
+    return (rb + 4.0) * (double)n_seg + 3.0 * rb * n_fsr + 2.0 * rb * psi;
 }
 
 } // namespace mocgpu

@@ -17,6 +17,17 @@ static inline void note_launch() { g_launches.fetch_add(1, std::memory_order_rel
 int64_t launch_count() { return g_launches.load(); }
 void note_launch_external() { note_launch(); }
 void note_launches(int64_t n) { g_launches += n; }
+static std::atomic<int64_t> g_h2d{0}, g_d2h{0};
+void note_copy_bytes(cudaMemcpyKind kind, size_t bytes)
+{
+    if (kind == cudaMemcpyHostToDevice) g_h2d += (int64_t)bytes;
+    else if (kind == cudaMemcpyDeviceToHost) g_d2h += (int64_t)bytes;
+}
+void copy_bytes(int64_t *h2d, int64_t *d2h)
+{
+    *h2d = g_h2d.load();
+    *d2h = g_d2h.load();
+}
 
 // ---------------------------------------------------------------------------
 __global__ void k_fill(double *p, double v, int64_t n)

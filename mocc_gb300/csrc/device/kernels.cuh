@@ -187,5 +187,6 @@ void launch_flux_residual(const GeomView &g, const StateView &st, double *out, c
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);
 void set_exp_constants(double min, double space, double rspace);
 int64_t launch_count();
+void copy_bytes(int64_t *h2d, int64_t *d2h); // host<->device bytes moved so far
 
 } // namespace mocgpu

@@ -156,7 +156,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
 
     dev_bytes_ = state_bytes_for(f, precision_, bcpg);
     double nfis = n_fissile_;
-    MOCGPU_CUDA(cudaMemcpyAsync(red_.p + RED_N_FISSILE, &nfis, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(red_.p + RED_N_FISSILE, &nfis, sizeof(double), cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -165,7 +165,7 @@ Sweeper::~Sweeper() = default;
 void Sweeper::check_status()
 {
     unsigned st = 0;
-    MOCGPU_CUDA(cudaMemcpyAsync(&st, status_.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&st, status_.p, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     if (st & DEV_NONPOSITIVE_PIN_FLUX) {
         status_.zero(stream_);
@@ -190,11 +190,11 @@ void Sweeper::initialize()
     std::vector<double> init((size_t)G * bcpg);
     for (int g = 0; g < G; g++) std::copy(pi.begin(), pi.end(), init.begin() + (size_t)g * bcpg);
     if (precision_ == 0) {
-        MOCGPU_CUDA(cudaMemcpyAsync(psi_in_.p, init.data(), init.size() * 8, cudaMemcpyHostToDevice, stream_));
+        MOCGPU_CUDA(copy_async(psi_in_.p, init.data(), init.size() * 8, cudaMemcpyHostToDevice, stream_));
         MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     } else {
         std::vector<float> fi(init.begin(), init.end());
-        MOCGPU_CUDA(cudaMemcpyAsync(psi_in_.p, fi.data(), fi.size() * 4, cudaMemcpyHostToDevice, stream_));
+        MOCGPU_CUDA(copy_async(psi_in_.p, fi.data(), fi.size() * 4, cudaMemcpyHostToDevice, stream_));
         MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     }
     tally_.zero(stream_);
@@ -210,18 +210,18 @@ void Sweeper::calc_fission_source(double k) { launch_fission_source(gv_, sv_, k,
 
 void Sweeper::set_fission_source(const double *h)
 {
-    MOCGPU_CUDA(cudaMemcpyAsync(fs_.p, h, sizeof(double) * f_.n_fsr, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(fs_.p, h, sizeof(double) * f_.n_fsr, cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 void Sweeper::get_fission_source(double *h)
 {
-    MOCGPU_CUDA(cudaMemcpyAsync(h, fs_.p, sizeof(double) * f_.n_fsr, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(h, fs_.p, sizeof(double) * f_.n_fsr, cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void Sweeper::store_old_flux()
 {
-    MOCGPU_CUDA(cudaMemcpyAsync(phi_old_.p, phi_.p, phi_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    MOCGPU_CUDA(copy_async(phi_old_.p, phi_.p, phi_.bytes(), cudaMemcpyDeviceToDevice, stream_));
 }
 
 void Sweeper::group_source(int g)
@@ -318,7 +318,7 @@ double Sweeper::total_fission(bool old)
 {
     launch_total_fission(gv_, old ? phi_old_.p : phi_.p, red_.p + RED_TFIS, stream_);
     double v = 0.0;
-    MOCGPU_CUDA(cudaMemcpyAsync(&v, red_.p + RED_TFIS, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&v, red_.p + RED_TFIS, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     return v;
 }
@@ -327,7 +327,7 @@ double Sweeper::flux_residual()
 {
     launch_flux_residual(gv_, sv_, red_.p + RED_FLUXRES, stream_);
     double v = 0.0;
-    MOCGPU_CUDA(cudaMemcpyAsync(&v, red_.p + RED_FLUXRES, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&v, red_.p + RED_FLUXRES, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     return std::sqrt(v);
 }
@@ -336,7 +336,7 @@ void Sweeper::get_flux(double *h) const
 {
     const int G = f_.ng, n = f_.n_fsr;
     std::vector<double> tmp((size_t)G * n);
-    MOCGPU_CUDA(cudaMemcpyAsync(tmp.data(), phi_.p, phi_.bytes(), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(tmp.data(), phi_.p, phi_.bytes(), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     for (int r = 0; r < n; r++)
         for (int g = 0; g < G; g++) h[(size_t)r * G + g] = tmp[(size_t)g * n + r];
@@ -348,14 +348,14 @@ void Sweeper::set_flux(const double *h)
     std::vector<double> tmp((size_t)G * n);
     for (int r = 0; r < n; r++)
         for (int g = 0; g < G; g++) tmp[(size_t)g * n + r] = h[(size_t)r * G + g];
-    MOCGPU_CUDA(cudaMemcpyAsync(phi_.p, tmp.data(), phi_.bytes(), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(phi_.p, tmp.data(), phi_.bytes(), cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
 void Sweeper::get_pin_flux(int g, double *out) const
 {
     launch_pin_flux(gv_, phi_.p, cflux_.p, stream_);
-    MOCGPU_CUDA(cudaMemcpyAsync(out, cflux_.p + (size_t)g * f_.n_pin, sizeof(double) * f_.n_pin,
+    MOCGPU_CUDA(copy_async(out, cflux_.p + (size_t)g * f_.n_pin, sizeof(double) * f_.n_pin,
                                 cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
@@ -368,11 +368,11 @@ double Sweeper::set_pin_flux(int g, const double *in)
     GeomView one = gv_;
     one.G = 1;
     double *phig = phi_.p + (size_t)g * f_.n_fsr;
-    MOCGPU_CUDA(cudaMemcpyAsync(pinbuf_.p, in, sizeof(double) * f_.n_pin, cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(pinbuf_.p, in, sizeof(double) * f_.n_pin, cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(cudaMemsetAsync(red_.p + RED_PINRES, 0, sizeof(double), stream_));
     launch_set_pin_flux(one, phig, pinbuf_.p, red_.p + RED_PINRES, status_.p, stream_);
     double e2 = 0.0;
-    MOCGPU_CUDA(cudaMemcpyAsync(&e2, red_.p + RED_PINRES, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&e2, red_.p + RED_PINRES, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     check_status();
     return std::sqrt(e2) / f_.n_pin;
 }
@@ -381,7 +381,7 @@ void Sweeper::pin_powers(double *out) const
 {
     launch_pin_power(gv_, phi_.p, pinbuf_.p, stream_);
     std::vector<double> p(f_.n_pin + 1);
-    MOCGPU_CUDA(cudaMemcpyAsync(p.data(), pinbuf_.p, sizeof(double) * (f_.n_pin + 1), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(p.data(), pinbuf_.p, sizeof(double) * (f_.n_pin + 1), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     double scale = f_.n_fuel_2d / p[f_.n_pin];
     for (int i = 0; i < f_.n_pin; i++) out[i] = p[i] * scale;
@@ -389,8 +389,8 @@ void Sweeper::pin_powers(double *out) const
 
 void Sweeper::get_currents(double *cur, double *sfl) const
 {
-    MOCGPU_CUDA(cudaMemcpyAsync(cur, cur_.p, cur_.bytes(), cudaMemcpyDeviceToHost, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(sfl, sflux_.p, sflux_.bytes(), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(cur, cur_.p, cur_.bytes(), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(sfl, sflux_.p, sflux_.bytes(), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
@@ -406,11 +406,11 @@ void Sweeper::cmfd_solve(double &k)
     cv_.resid_reduction = opts_.cmfd_resid_reduction;
     cv_.max_iter = opts_.cmfd_max_iter;
     cv_.fixup = opts_.cmfd_negative_fixup ? 1 : 0;
-    MOCGPU_CUDA(cudaMemcpyAsync(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
     launch_cmfd_solve(cv_, stream_);
     launch_set_pin_flux(gv_, phi_.p, cflux_.p, nullptr, status_.p, stream_);
-    MOCGPU_CUDA(cudaMemcpyAsync(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
     check_status();
     cmfd_iters += (int64_t)cmfd_stats[0];
 }
@@ -425,11 +425,11 @@ void Sweeper::cmfd_solve_static(double &k)
     cv_.resid_reduction = opts_.cmfd_resid_reduction;
     cv_.max_iter = opts_.cmfd_max_iter;
     cv_.fixup = opts_.cmfd_negative_fixup ? 1 : 0;
-    MOCGPU_CUDA(cudaMemcpyAsync(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(copy_async(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
     launch_cmfd_solve_static(cv_, stream_);
     launch_set_pin_flux(gv_, phi_.p, cflux_.p, nullptr, status_.p, stream_);
-    MOCGPU_CUDA(cudaMemcpyAsync(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
-    MOCGPU_CUDA(cudaMemcpyAsync(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
     check_status();
     cmfd_iters += (int64_t)cmfd_stats[0];
 }
@@ -438,7 +438,7 @@ double Sweeper::psi_error()
 {
     launch_psi_error(gv_, fs_.p, fs_prev_.p, red_.p + RED_PSI, stream_);
     double r[5];
-    MOCGPU_CUDA(cudaMemcpyAsync(r, red_.p + RED_PSI, sizeof(r), cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(r, red_.p + RED_PSI, sizeof(r), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
     return std::sqrt(r[4] / n_fissile_);
 }
@@ -448,7 +448,7 @@ void Sweeper::eigen_step(double &k, double &k_prev)
 {
     if (opts_.cmfd && opts_.cmfd_enabled) cmfd_solve(k);
     calc_fission_source(k);
-    MOCGPU_CUDA(cudaMemcpyAsync(fs_prev_.p, fs_.p, fs_.bytes(), cudaMemcpyDeviceToDevice, stream_));
+    MOCGPU_CUDA(copy_async(fs_prev_.p, fs_.p, fs_.bytes(), cudaMemcpyDeviceToDevice, stream_));
     store_old_flux();
     for (int g = 0; g < f_.ng; g++) {
         group_source(g);
