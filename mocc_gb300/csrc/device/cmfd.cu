@@ -2,9 +2,9 @@
 // the 5-point operator per group, then the CMFD power iteration with one
 // preconditioned BiCGSTAB solve per group.
 //
-// One CTA runs a whole CMFD solve. Small meshes (up to 512 cells) run on a
+// One CTA runs a whole CMFD solve. Tiny meshes (up to 64 cells) run on a
 // single warp, so every reduction is a shuffle tree and every barrier a warp
-// barrier; larger meshes use up to 16 warps with one block barrier per
+// barrier; larger meshes use 4 to 16 warps with one block barrier per
 // reduction. Work vectors live in shared memory when they fit.
 #include <mutex>
 #include <string>
@@ -431,11 +431,15 @@ __global__ void kb_cmfd_solve(BatchViews b, int vec_in_smem)
 
 void note_launch_external();
 
+// Warps per CMFD CTA. One warp reaches only about a quarter of an SM's FP64
+// rate (one of four schedulers issues), so meshes with work for more than
+// one warp get at least four; tiny meshes stay on one warp, where every
+// reduction is a shuffle tree.
 static int cmfd_warps(int n_cell)
 {
+    if (n_cell <= 64) return 1;
     int nw = (n_cell + 255) / 256;
-    if (n_cell <= 512) nw = 1;
-    return nw < 1 ? 1 : (nw > 16 ? 16 : nw);
+    return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
 
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s)

@@ -442,51 +442,54 @@ void launch_set_pin_flux(const GeomView &g, double *phi, const double *cflux, do
 }
 
 // Flux-weighted pin homogenisation (xs_mesh_homogenized.cpp:261-363).
-__device__ void homogenize_pin(const GeomView &g, const double *phi, const CmfdView &c, int ip)
+__device__ void homogenize_pin(const GeomView &g, const double *phi, const CmfdView &c, int idx)
 {
+    // one (pin, group) pair per thread: the group's flux-weighted XS, its
+    // fission-source-weighted chi and its scattering row
     const double *fsr_area = g.fsr_area;
-    if (ip >= g.n_pin) return;
     const int G = g.G;
+    if (idx >= g.n_pin * G) return;
+    const int ip = idx / G, ig = idx % G;
     const int cell = g.pin_cell[ip];
     const int r0 = g.pin_first_reg[ip], r1 = g.pin_first_reg[ip + 1];
     double fs_sum = 0.0;
     for (int r = r0; r < r1; r++) {
         const double *nf = g.xsnf + (size_t)g.fsr_mat[r] * G;
         double f = 0.0;
-        for (int ig = 0; ig < G; ig++) f += nf[ig] * phi[(size_t)ig * g.n_fsr + r] * fsr_area[r];
+        for (int gg = 0; gg < G; gg++) f += nf[gg] * phi[(size_t)gg * g.n_fsr + r] * fsr_area[r];
         fs_sum += f;
     }
-    for (int ig = 0; ig < G; ig++) {
-        double fvs = 0.0, xt = 0.0, xnf = 0.0, xf = 0.0, xch = 0.0;
+    double fvs = 0.0, xt = 0.0, xnf = 0.0, xf = 0.0, xch = 0.0;
+    for (int r = r0; r < r1; r++) {
+        int m = g.fsr_mat[r];
+        double v = fsr_area[r], fl = phi[(size_t)ig * g.n_fsr + r];
+        fvs += v * fl;
+        xt += v * fl * g.xstr[(size_t)m * G + ig];
+        xnf += v * fl * g.xsnf[(size_t)m * G + ig];
+        xf += v * fl * g.xsf[(size_t)m * G + ig];
+        double fsr_fs = 0.0;
+        for (int gg = 0; gg < G; gg++) fsr_fs += g.xsnf[(size_t)m * G + gg] * phi[(size_t)gg * g.n_fsr + r] * v;
+        xch += fsr_fs * g.xsch[(size_t)m * G + ig];
+    }
+    double self = 0.0;
+    for (int gg = 0; gg < G; gg++) {
+        double num = 0.0, den = 0.0;
         for (int r = r0; r < r1; r++) {
             int m = g.fsr_mat[r];
-            double v = fsr_area[r], fl = phi[(size_t)ig * g.n_fsr + r];
-            fvs += v * fl;
-            xt += v * fl * g.xstr[(size_t)m * G + ig];
-            xnf += v * fl * g.xsnf[(size_t)m * G + ig];
-            xf += v * fl * g.xsf[(size_t)m * G + ig];
-            double fsr_fs = 0.0;
-            for (int gg = 0; gg < G; gg++) fsr_fs += g.xsnf[(size_t)m * G + gg] * phi[(size_t)gg * g.n_fsr + r] * v;
-            xch += fsr_fs * g.xsch[(size_t)m * G + ig];
+            double v = fsr_area[r], fl = phi[(size_t)gg * g.n_fsr + r];
+            den += fl * v;
+            num += g.scat[((size_t)m * G + ig) * G + gg] * v * fl;
         }
-        for (int gg = 0; gg < G; gg++) {
-            double num = 0.0, den = 0.0;
-            for (int r = r0; r < r1; r++) {
-                int m = g.fsr_mat[r];
-                double v = fsr_area[r], fl = phi[(size_t)gg * g.n_fsr + r];
-                den += fl * v;
-                num += g.scat[((size_t)m * G + ig) * G + gg] * v * fl;
-            }
-            if (num > 0.0) num /= den;
-            c.scat[((size_t)cell * G + ig) * G + gg] = num;
-        }
-        c.xstr[(size_t)cell * G + ig] = xt / fvs;
-        c.xsnf[(size_t)cell * G + ig] = xnf / fvs;
-        c.xsf[(size_t)cell * G + ig] = xf / fvs;
-        c.xsch[(size_t)cell * G + ig] = (fs_sum > 0.0) ? xch / fs_sum : xch;
+        if (num > 0.0) num /= den;
+        c.scat[((size_t)cell * G + ig) * G + gg] = num;
+        if (gg == ig) self = num;
     }
-    for (int ig = 0; ig < G; ig++)
-        c.xsrm[(size_t)cell * G + ig] = c.xstr[(size_t)cell * G + ig] - c.scat[((size_t)cell * G + ig) * G + ig];
+    const double xs_tr = xt / fvs;
+    c.xstr[(size_t)cell * G + ig] = xs_tr;
+    c.xsnf[(size_t)cell * G + ig] = xnf / fvs;
+    c.xsf[(size_t)cell * G + ig] = xf / fvs;
+    c.xsch[(size_t)cell * G + ig] = (fs_sum > 0.0) ? xch / fs_sum : xch;
+    c.xsrm[(size_t)cell * G + ig] = xs_tr - self;
 }
 __global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
 {
@@ -494,7 +497,7 @@ __global__ void k_homogenize(GeomView g, const double *phi, CmfdView c)
 }
 void launch_homogenize(const GeomView &g, const double *phi, const CmfdView &c, cudaStream_t s)
 {
-    { note_launch(); k_homogenize<<<(g.n_pin + 127) / 128, 128, 0, s>>>(g, phi, c); }
+    { note_launch(); k_homogenize<<<(g.n_pin * g.G + 127) / 128, 128, 0, s>>>(g, phi, c); }
 }
 
 // ---------------------------------------------------------------------------
@@ -744,7 +747,7 @@ __global__ void kb_homogenize(BatchViews b)
 void launch_b_homogenize(const BatchViews &b, cudaStream_t s)
 {
     note_launch();
-    kb_homogenize<<<bgrid(b.max_pin, 64, b.cap), 64, 0, s>>>(b);
+    kb_homogenize<<<bgrid(b.max_pin * b.max_g, 64, b.cap), 64, 0, s>>>(b);
 }
 
 __global__ void kb_set_pin_flux(BatchViews b)

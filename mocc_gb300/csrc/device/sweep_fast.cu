@@ -11,6 +11,7 @@
 // After the bundles, the unit's tally is added to the global FSR tally with
 // one atomic per touched FSR.
 #include <algorithm>
+#include <climits>
 
 #include "kernels.cuh"
 
@@ -28,13 +29,26 @@ __device__ __forceinline__ double att_fast(double tau, const double *tab)
     double d0 = __ldg(tab + i), d1 = __ldg(tab + i + 1);
     return 1.0 - (d0 + (d1 - d0) * v * rspace);
 }
-__device__ __forceinline__ float att_fast(float tau, const double *)
+// 1 - e^{-tau} in FP32 from the identity e^{-tau} = 2^{-tau log2 e}, with
+// the hardware base-2 exponential (ex2.approx, relative error about 2^-22).
+// The absolute error of the difference is about one ulp of 1.0 (6e-8) for
+// every tau, the size of the FP32 rounding of the angular-flux update it
+// feeds and below the interpolation error of MOCC's FP64 table (h^2/8 =
+// 1.25e-7). `ntau_l2` is -tau * log2(e).
+__device__ __forceinline__ float att_exp2(float ntau_l2)
 {
-    // 4-term Taylor series of 1 - e^{-tau} below 1/64, hardware exponential
-    // above; both are evaluated and selected so a warp never diverges here
-    const float poly = tau * (1.0f - tau * (0.5f - tau * (0.16666667f - tau * 0.041666668f)));
-    const float hw = 1.0f - __expf(-tau);
-    return tau < 0.015625f ? poly : hw;
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(ntau_l2));
+    return 1.0f - e;
+}
+
+// Attenuation 1 - e^{-tau0 / sin(theta)} of one polar angle; `rs` is the
+// per-polar factor prepared by polar_factor().
+__device__ __forceinline__ double atten(double tau0, double rs, const double *tab) { return att_fast(tau0 * rs, tab); }
+__device__ __forceinline__ float atten(float tau0, float rs, const double *) { return att_exp2(tau0 * rs); }
+template <typename Real> __device__ __forceinline__ Real polar_factor(double rsin)
+{
+    return sizeof(Real) == 4 ? (Real)(-rsin * 1.4426950408889634) : (Real)rsin; // FP32: -log2(e)/sin
 }
 
 template <typename Real> struct Pair;
@@ -45,7 +59,7 @@ template <> struct Pair<double> {
     using T = double2;
 };
 template <typename Real> struct Chunk {
-    static constexpr int rows = sizeof(Real) == 4 ? 32 : 16; // rows per streamed chunk
+    static constexpr int rows = 16; // rows per streamed chunk
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -60,6 +74,32 @@ template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile(
 template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
 {
     return 2 * (size_t)Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
+}
+
+// Adds each lane's contribution to the shared tally. Lanes of one bundle are
+// neighbouring parallel tracks, so consecutive lanes often cross the same FSR
+// in the same row; a float atomic on shared memory is a compare-and-swap
+// loop that serialises such collisions. Runs of consecutive lanes with the
+// same FSR are therefore summed first (a segmented shuffle reduction towards
+// the run's first lane) and each run issues one atomic. Padding lanes carry
+// a zero contribution and may join a run harmlessly. Warp-uniform control
+// flow: every lane of the warp must call this.
+template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int lane)
+{
+    const unsigned full = 0xffffffffu;
+    const int lprev = __shfl_up_sync(full, l, 1);
+    const bool head = (lane == 0) || (l != lprev);
+    const unsigned heads = __ballot_sync(full, head);
+    if (heads != full) {
+        const unsigned above = heads & ~((2u << lane) - 1u); // run heads after this lane
+        const int span = (above ? (__ffs(above) - 2) : 31) - lane; // lanes after this one in its run
+        const int max_span = __reduce_max_sync(full, span);
+        for (int o = 1; o <= max_span; o <<= 1) {
+            const Real other = __shfl_down_sync(full, acc, o);
+            if (o <= span) acc += other;
+        }
+    }
+    if (head && acc != (Real)0) atomicAdd(s_tal + l, acc);
 }
 
 template <typename Real, int NPOL, bool GS, bool CUR>
@@ -95,19 +135,19 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
 
     Real rsin[NPOL], wt[NPOL];
     int af[NPOL], ab[NPOL];
-    double cw[NPOL][2], fwt[NPOL][2];
+    Real cw[NPOL][2], fwt[NPOL][2]; // current / surface-flux weights (FP32 in the mixed path)
 #pragma unroll
     for (int p = 0; p < NPOL; p++) {
         const SetPolar sp = g.sp[u.set * NPOL + p];
-        rsin[p] = (Real)sp.rsin;
+        rsin[p] = polar_factor<Real>(sp.rsin);
         wt[p] = (Real)sp.wt;
         af[p] = sp.ang_fwd;
         ab[p] = sp.ang_bwd;
         if (CUR) {
-            cw[p][0] = sp.cw[0];
-            cw[p][1] = sp.cw[1];
-            fwt[p][0] = sp.fw[0];
-            fwt[p][1] = sp.fw[1];
+            cw[p][0] = (Real)sp.cw[0];
+            cw[p][1] = (Real)sp.cw[1];
+            fwt[p][0] = (Real)sp.fw[0];
+            fwt[p][1] = (Real)sp.fw[1];
         }
     }
     double *cur = st.cur + (size_t)group * g.n_surf;
@@ -136,21 +176,26 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             ev = fwd ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
             ev_end = fwd ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
         }
-        const double sign = fwd ? 1.0 : -1.0;
+        // row of the next crossing event, kept in a register so rows without
+        // an event cost one compare
+        int ev_next = (CUR && ev < ev_end) ? ev_pt[ev] : INT_MAX;
         auto events = [&](int k) {
-            while (ev < ev_end && ev_pt[ev] == k) {
+            while (ev_next == k) {
                 int c = ev_code[ev];
                 int surf = c >> 1;
                 bool ynorm = c & 1;
-                double jc = 0.0, fc = 0.0;
+                // partial current and surface flux of this crossing in the
+                // sweep precision, accumulated in FP64
+                Real jc = 0, fc = 0;
 #pragma unroll
                 for (int p = 0; p < NPOL; p++) {
-                    jc += (double)psi[p] * (ynorm ? cw[p][1] : cw[p][0]);
-                    fc += (double)psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
+                    jc += psi[p] * (ynorm ? cw[p][1] : cw[p][0]);
+                    fc += psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
                 }
-                atomicAdd(cur + surf, sign * jc);
-                atomicAdd(sfl + surf, fc);
+                atomicAdd(cur + surf, fwd ? (double)jc : -(double)jc);
+                atomicAdd(sfl + surf, (double)fc);
                 ev++;
+                ev_next = (ev < ev_end) ? ev_pt[ev] : INT_MAX;
             }
         };
         // chunk c of this direction covers rows [lo, hi)
@@ -214,7 +259,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                 for (int v = 0; v < U; v++) {
                     const Real tau0 = sq[v].x * L[v];
 #pragma unroll
-                    for (int p = 0; p < NPOL; p++) e[v][p] = att_fast(tau0 * rsin[p], g.exp_tab);
+                    for (int p = 0; p < NPOL; p++) e[v][p] = atten(tau0, rsin[p], g.exp_tab);
                 }
 #pragma unroll
                 for (int v = 0; v < U; v++) {
@@ -229,7 +274,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                         psi[p] -= d;
                         acc += d * wt[p];
                     }
-                    if (L[v] > (Real)0) atomicAdd(s_tal + l[v], acc);
+                    tally_add(s_tal, l[v], acc, lane);
                 }
             }
             for (; k < nr; k++) {
@@ -242,12 +287,12 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                 Real acc = 0;
 #pragma unroll
                 for (int p = 0; p < NPOL; p++) {
-                    Real e = att_fast(tau0 * rsin[p], g.exp_tab);
+                    Real e = atten(tau0, rsin[p], g.exp_tab);
                     Real d = (psi[p] - sq.y) * e;
                     psi[p] -= d;
                     acc += d * wt[p];
                 }
-                if (L > (Real)0) atomicAdd(s_tal + l, acc);
+                tally_add(s_tal, l, acc, lane);
             }
             __syncwarp();
         }
