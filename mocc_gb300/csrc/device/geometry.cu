@@ -206,6 +206,12 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         bundle_row_.upload(L.bundle_row);
         bundle_nrows_.upload(L.bundle_nrows);
         bundle_track_.upload(L.bundle_track);
+        {
+            std::vector<int2> bbc(L.bundle_track.size(), make_int2(0, 0));
+            for (size_t i = 0; i < L.bundle_track.size(); i++)
+                if (L.bundle_track[i] >= 0) bbc[i] = make_int2(f.trk_bc0[L.bundle_track[i]], f.trk_bc1[L.bundle_track[i]]);
+            bundle_bc_.upload(bbc);
+        }
         local_fsr_.upload(L.local_fsr);
         blfsr_.upload(L.lfsr);
         if (precision == 0) blen_d_.upload(L.len);
@@ -221,6 +227,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         fv.bundle_row = bundle_row_.p;
         fv.bundle_nrows = bundle_nrows_.p;
         fv.bundle_track = bundle_track_.p;
+        fv.bundle_bc = bundle_bc_.p;
         fv.len = precision == 0 ? (const void *)blen_d_.p : (const void *)blen_f_.p;
         fv.lfsr = blfsr_.p;
         fv.local_fsr = local_fsr_.p;
@@ -259,6 +266,13 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     ev_bw_begin_.upload(ebb);
     ev_bw_pt_.upload(ebp);
     ev_bw_code_.upload(ebc);
+    {
+        std::vector<int2> pf(efp.size()), pb(ebp.size());
+        for (size_t i = 0; i < efp.size(); i++) pf[i] = make_int2(efp[i], efc[i]);
+        for (size_t i = 0; i < ebp.size(); i++) pb[i] = make_int2(ebp[i], ebc[i]);
+        ev_fw_.upload(pf);
+        ev_bw_.upload(pb);
+    }
     std::vector<int> pfr(f.pin_first_reg.begin(), f.pin_first_reg.end());
     pin_first_reg_.upload(pfr);
     pin_cell_.upload(f.pin_cell);
@@ -303,6 +317,8 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     g.ev_bw_begin = ev_bw_begin_.p;
     g.ev_bw_pt = ev_bw_pt_.p;
     g.ev_bw_code = ev_bw_code_.p;
+    g.ev_fw = ev_fw_.p;
+    g.ev_bw = ev_bw_.p;
     g.exp_tab = exp_tab_.p;
     g.pin_first_reg = pin_first_reg_.p;
     g.pin_cell = pin_cell_.p;
@@ -312,6 +328,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     bytes_ = seg_begin_.bytes() + trk_bc0_.bytes() * 3 + seg_fsr_.bytes() + seg_len_d_.bytes() + seg_len_f_.bytes() +
              fsr_mat_.bytes() + fsr_vol_.bytes() * 2 + sp_.bytes() + bc_off_.bytes() + wt_tgt_.bytes() +
              ev_fw_pt_.bytes() * 2 + ev_bw_pt_.bytes() * 2 + ev_fw_begin_.bytes() * 2 + wu_.bytes() +
+             ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() +
              bundle_row_.bytes() + bundle_nrows_.bytes() + bundle_track_.bytes() + local_fsr_.bytes() +
              blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes();
     MOCGPU_CUDA(cudaDeviceSynchronize());

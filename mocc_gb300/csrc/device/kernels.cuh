@@ -43,6 +43,7 @@ struct GeomView {
     const int *wt_tgt; // [n_ang*2] reflect targets (-1 vacuum), [n_ang] x-face sizes, [n_ang*2] target bases
     const int *ev_fw_begin, *ev_fw_pt, *ev_fw_code; // forward crossing events
     const int *ev_bw_begin, *ev_bw_pt, *ev_bw_code; // backward crossing events
+    const int2 *ev_fw, *ev_bw;                      // the same events packed as (row, code)
     const double *exp_tab;                          // kExpN + 1 entries
     const int *pin_first_reg, *pin_cell;            // pins in FSR order
     const double *pin_area;
@@ -89,6 +90,7 @@ struct FastView {
     const WorkUnitDev *wu;
     const int64_t *bundle_row;
     const int *bundle_nrows, *bundle_track;
+    const int2 *bundle_bc; // [bundle][32]: both boundary indices of each lane's track (0 for padding lanes)
     const void *len; // Real [rows][32]
     const uint16_t *lfsr;
     const int *local_fsr;

@@ -59,7 +59,7 @@ template <> struct Pair<double> {
     using T = double2;
 };
 template <typename Real> struct Chunk {
-    static constexpr int rows = 16; // rows per streamed chunk
+    static constexpr int rows = 8; // rows per streamed chunk
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -76,30 +76,13 @@ template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
     return 2 * (size_t)Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
 }
 
-// Adds each lane's contribution to the shared tally. Lanes of one bundle are
-// neighbouring parallel tracks, so consecutive lanes often cross the same FSR
-// in the same row; a float atomic on shared memory is a compare-and-swap
-// loop that serialises such collisions. Runs of consecutive lanes with the
-// same FSR are therefore summed first (a segmented shuffle reduction towards
-// the run's first lane) and each run issues one atomic. Padding lanes carry
-// a zero contribution and may join a run harmlessly. Warp-uniform control
-// flow: every lane of the warp must call this.
-template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int lane)
+// Adds each lane's contribution to the shared tally (a float add on shared
+// memory is a compare-and-swap loop; merging lanes that hit the same FSR
+// first, with shuffles, measured slower than letting those few collide).
+// Padding lanes carry a zero contribution and skip the add.
+template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int)
 {
-    const unsigned full = 0xffffffffu;
-    const int lprev = __shfl_up_sync(full, l, 1);
-    const bool head = (lane == 0) || (l != lprev);
-    const unsigned heads = __ballot_sync(full, head);
-    if (heads != full) {
-        const unsigned above = heads & ~((2u << lane) - 1u); // run heads after this lane
-        const int span = (above ? (__ffs(above) - 2) : 31) - lane; // lanes after this one in its run
-        const int max_span = __reduce_max_sync(full, span);
-        for (int o = 1; o <= max_span; o <<= 1) {
-            const Real other = __shfl_down_sync(full, acc, o);
-            if (o <= span) acc += other;
-        }
-    }
-    if (head && acc != (Real)0) atomicAdd(s_tal + l, acc);
+    if (acc != (Real)0) atomicAdd(s_tal + l, acc);
 }
 
 template <typename Real, int NPOL, bool GS, bool CUR>
@@ -133,16 +116,28 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     Real *psi_out = (Real *)st.psi_out;
     const int ny_set = g.set_ny[u.set];
 
+    // per unit: boundary-flux offsets of every (direction, polar) angle and
+    // the reflected angles' incoming offsets for the Gauss-Seidel write-through
+    __shared__ int s_off[2][kMaxPolar], s_tgt[2][kMaxPolar][2];
+    if (threadIdx.x < 2 * NPOL) {
+        const int dir = threadIdx.x / NPOL, p = threadIdx.x % NPOL;
+        const SetPolar sp = g.sp[u.set * NPOL + p];
+        const int a = dir == 0 ? sp.ang_fwd : sp.ang_bwd;
+        s_off[dir][p] = g.bc_off[a];
+        if (GS) {
+            s_tgt[dir][p][0] = g.wt_tgt[a * 2];
+            s_tgt[dir][p][1] = g.wt_tgt[a * 2 + 1];
+        }
+    }
+    __syncthreads();
+
     Real rsin[NPOL], wt[NPOL];
-    int af[NPOL], ab[NPOL];
     Real cw[NPOL][2], fwt[NPOL][2]; // current / surface-flux weights (FP32 in the mixed path)
 #pragma unroll
     for (int p = 0; p < NPOL; p++) {
         const SetPolar sp = g.sp[u.set * NPOL + p];
         rsin[p] = polar_factor<Real>(sp.rsin);
         wt[p] = (Real)sp.wt;
-        af[p] = sp.ang_fwd;
-        ab[p] = sp.ang_bwd;
         if (CUR) {
             cw[p][0] = (Real)sp.cw[0];
             cw[p][1] = (Real)sp.cw[1];
@@ -157,31 +152,30 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         const int b = u.bundle_begin + (task >> 1);
         const bool fwd = (task & 1) == 0;
         const int t = fv.bundle_track[(size_t)b * 32 + lane];
+        const int2 bc = fv.bundle_bc[(size_t)b * 32 + lane];
         const int nrows = fv.bundle_nrows[b];
         const int64_t row0 = fv.bundle_row[b];
         const int nch = (nrows + CH - 1) / CH;
-        int bc_in = 0, bc_out = 0;
-        const int *angs = fwd ? af : ab;
-        if (t >= 0) {
-            bc_in = fwd ? g.trk_bc0[t] : g.trk_bc1[t];
-            bc_out = fwd ? g.trk_bc1[t] : g.trk_bc0[t];
-        }
+        const int dir = fwd ? 0 : 1;
+        const int bc_in = fwd ? bc.x : bc.y, bc_out = fwd ? bc.y : bc.x;
         Real psi[NPOL];
 #pragma unroll
-        for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? psi_in[g.bc_off[angs[p]] + bc_in] : (Real)0;
+        for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? psi_in[s_off[dir][p] + bc_in] : (Real)0;
         int ev = 0, ev_end = 0;
-        const int *ev_pt = fwd ? g.ev_fw_pt : g.ev_bw_pt;
-        const int *ev_code = fwd ? g.ev_fw_code : g.ev_bw_code;
+        const int2 *evp = fwd ? g.ev_fw : g.ev_bw;
         if (CUR && t >= 0) {
             ev = fwd ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
             ev_end = fwd ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
         }
-        // row of the next crossing event, kept in a register so rows without
-        // an event cost one compare
-        int ev_next = (CUR && ev < ev_end) ? ev_pt[ev] : INT_MAX;
+        // the next two crossing events (row, code) live in registers, so a row
+        // without an event costs one compare and the load of the event after
+        // next has rows of time to arrive
+        const int2 none = make_int2(INT_MAX, 0);
+        int2 ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
+        int2 ev1 = (CUR && ev + 1 < ev_end) ? evp[ev + 1] : none;
         auto events = [&](int k) {
-            while (ev_next == k) {
-                int c = ev_code[ev];
+            while (ev0.x == k) {
+                int c = ev0.y;
                 int surf = c >> 1;
                 bool ynorm = c & 1;
                 // partial current and surface flux of this crossing in the
@@ -195,7 +189,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                 atomicAdd(cur + surf, fwd ? (double)jc : -(double)jc);
                 atomicAdd(sfl + surf, (double)fc);
                 ev++;
-                ev_next = (ev < ev_end) ? ev_pt[ev] : INT_MAX;
+                ev0 = ev1;
+                ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
             }
         };
         // chunk c of this direction covers rows [lo, hi)
@@ -301,10 +296,10 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
 #pragma unroll
             for (int p = 0; p < NPOL; p++) {
                 if (GS) {
-                    int tgt = g.wt_tgt[angs[p] * 2 + (bc_out < ny_set ? 0 : 1)];
+                    int tgt = s_tgt[dir][p][bc_out < ny_set ? 0 : 1];
                     if (tgt >= 0) psi_in[tgt + bc_out] = psi[p];
                 } else {
-                    psi_out[g.bc_off[angs[p]] + bc_out] = psi[p];
+                    psi_out[s_off[dir][p] + bc_out] = psi[p];
                 }
             }
         }
