@@ -28,8 +28,9 @@ Printed JSON (one line, rank 0):
                  bandwidth
   cpu_baseline   the CPU oracle (FP64 OpenMP restatement of MOCC) solving one
                  case of each size with all host threads
-The segment streams of the 256 cases (about 0.4 GB) exceed the 129 MB L2,
-so no explicit L2 flush is needed between steps.
+L2 is flushed (256 MB write) before every timed step; within a step the four
+shared traced geometries (~35 MB of segment streams) stay in the 129 MB L2 by
+design, while the per-solve state (~0.2 GB for 256 solves) does not fit.
 
 --impl reference times the reference's CPU algorithm (the oracle port:
 MOCC itself cannot be built without Blitz++, Eigen, pugixml and HDF5) with
@@ -134,6 +135,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def profiled_traffic(name="kb_sweep_fast_dram_branch256.md"):
+    """DRAM bytes per sweep launch from the committed ncu summary (None if absent)."""
+    p = ROOT / "profiles" / name
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    return None
+
+
 def pcm(k, k_ref):
     return 1e5 * abs(k - k_ref) / k_ref
 
@@ -163,7 +174,7 @@ CONFIG = {"workload": "branch256: 256 eigenvalue solves, lattices uniform over 1
           "spacing_cm": 0.05, "perturbation": "moderator x U[0.9,1.1], fuel nu-Sigma_f x U[0.95,1.05]",
           "cmfd": "pin mesh, BiCGSTAB", "tolerances": "k 1e-6, psi 1e-5", "n_inner": 5,
           "precision": "FP32 sweep, FP64 k/fission source/CMFD",
-          "l2": "no flush: the 256 segment streams (~0.4 GB) exceed the 129 MB L2"}
+          "l2": "flushed (256 MB write) before each timed step; shared geometries (~35 MB) L2-resident within a step"}
 
 
 def oracle_sample(cases, per_size=1):
@@ -216,7 +227,7 @@ def run_branch(args, rank, world):
 
     import mocc_gb300 as m
     from mocc_gb300 import workloads as W
-    from mocc_gb300.serve import Request, poisson_arrivals, serve
+    from mocc_gb300.serve import Request, poisson_arrivals, run_batch, serve
     from mocc_gb300.tune import tune_bundles_per_unit
     m.load_library()
     dev = int(os.environ.get("LOCAL_RANK", 0))
@@ -229,48 +240,85 @@ def run_branch(args, rank, world):
     tune = tune_bundles_per_unit(lambda b: m.BatchEngine(precision=1, capacity=64, bundles_per_unit=b),
                                  reqs[:64])
     bpu = tune["best"]
-    E = m.BatchEngine(precision=1, capacity=n, bundles_per_unit=bpu)
 
-    def batch():
-        ids = [E.submit(P, x) for P, x in reqs]
-        E.run()
-        return [E.take(i, n_pin_max) for i in ids]
+    def make_lanes(n_lanes):
+        cap = (n + n_lanes - 1) // n_lanes
+        return {k: m.BatchEngine(precision=1, capacity=cap, bundles_per_unit=bpu) for k in range(n_lanes)}
 
+    def timed_batch(lanes):
+        """One batch of all cases over the lanes (round robin); device span of
+        the run from CUDA events on every lane's stream, and the results."""
+        streams = {k: torch.cuda.ExternalStream(e.stream()) for k, e in lanes.items()}
+        ev0 = {k: torch.cuda.Event(enable_timing=True) for k in lanes}
+        ev1 = {k: torch.cuda.Event(enable_timing=True) for k in lanes}
+        for k in lanes:
+            ev0[k].record(streams[k])
+        res = run_batch(lanes, [(P, x, i % len(lanes)) for i, (P, x) in enumerate(reqs)], n_pin_max)
+        for k in lanes:
+            ev1[k].record(streams[k])
+        torch.cuda.synchronize()
+        first = next(iter(lanes))
+        span = max(ev0[first].elapsed_time(ev1[k]) for k in lanes) - min(
+            ev0[first].elapsed_time(ev0[k]) for k in lanes)
+        return span, res
+
+    # lanes: one engine, or two engines on their own streams whose outer
+    # iterations overlap on the GPU (one lane's CMFD beside the other's sweeps)
+    lane_ms = {}
+    for nl in (1, 2):
+        L = make_lanes(nl)
+        timed_batch(L)
+        lane_ms[nl] = timed_batch(L)[0]
+        for e in L.values():
+            e.close()
+    n_lanes = min(lane_ms, key=lane_ms.get)
+    lanes = make_lanes(n_lanes)
     for _ in range(args.warmup):
-        batch()
-    E.set_timing(True)
-    batch()  # capture the timing graph outside the timed region
+        timed_batch(lanes)
+    for e in lanes.values():
+        e.set_timing(True)
+    timed_batch(lanes)  # capture the timing graphs outside the timed region
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     barrier(world)
     torch.cuda.synchronize()
     clocks = Clocks()
-    s0 = E.stats()
+    s0 = {k: e.stats() for k, e in lanes.items()}
     l0 = m.launch_count()
     h0, d0 = m.copy_bytes()
-    t0 = time.perf_counter()
+    wall, span_ms = 0.0, 0.0
     results = None
     for _ in range(args.steps):
-        results = batch()
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sp, results = timed_batch(lanes)
+        wall += time.perf_counter() - t0
+        span_ms += sp
     launches = m.launch_count() - l0
     h1, d1 = m.copy_bytes()
-    s1 = E.stats()
+    s1 = {k: e.stats() for k, e in lanes.items()}
     barrier(world)
     clk = clocks.stop()
-    replay_ms = max_over_ranks(s1["replay_ms"] - s0["replay_ms"], world)
+
+    def delta(key):
+        return sum(s1[k][key] - s0[k][key] for k in lanes)
+
+    span_ms = max_over_ranks(span_ms, world)
     wall = max_over_ranks(wall, world)
-    value = world * n * args.steps / (replay_ms / 1e3)
+    value = world * n * args.steps / (span_ms / 1e3)
     e2e = world * n * args.steps / wall
     assert all(r["error"] == 0 and r["converged"] == 1 for r in results), [r for r in results if r["error"]][:2]
-    sweep_ms = s1["sweep_ms"] - s0["sweep_ms"]
-    sweep_launches = s1["sweep_launches"] - s0["sweep_launches"]
-    sweep_bytes = s1["sweep_bytes"] - s0["sweep_bytes"]
-    sgu = s1["sweep_sgu"] - s0["sweep_sgu"]
+    replay_ms = delta("replay_ms")
+    sweep_ms = delta("sweep_ms")
+    sweep_launches = delta("sweep_launches")
+    sweep_bytes = delta("sweep_bytes")
+    sgu = delta("sweep_sgu")
     peak, peak_kind = measured_peaks()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
 
     # plain single-solve GPU path on the same cases (sequential, one handle each)
-    E.set_timing(False)
+    for e in lanes.values():
+        e.set_timing(False)
     plain_t, plain_k = [], []
     for P, x in reqs:
         S = m.MoCSweeper(P, 1, xsl=x)
@@ -285,42 +333,56 @@ def run_branch(args, rank, world):
     k_vs_plain = max(pcm(r["k"], k) for r, k in zip(results, plain_k))
 
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": replay_ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": span_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {**CONFIG, "cases": n, "bundles_per_unit": bpu, "replicas": world},
-            "sgu_per_s": sgu / (sweep_ms / 1e3), "sgu_per_s_whole_replay": world * sgu / (replay_ms / 1e3),
+            "config": {**CONFIG, "cases": n, "bundles_per_unit": bpu, "lanes": n_lanes, "replicas": world},
+            "lanes_ms_per_batch": lane_ms,
+            "sgu_per_s": sgu / (sweep_ms / 1e3), "sgu_per_s_whole_run": world * sgu / (span_ms / 1e3),
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int((h1 - h0) / args.steps),
                     "d2h_bytes_per_step": int((d1 - d0) / args.steps)},
             "plain": {"value": plain, "unit": "solves/s", "speedup": value / plain, "speedup_e2e": e2e / plain,
                       "k_max_diff_pcm_vs_batched": k_vs_plain,
                       "what": "sequential EigenSolver solves of the same cases, FP32 sweep, one handle each"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "kb_sweep_fast",
+                         "traffic": profiled_traffic(),
+                         "traffic_note": "DRAM bytes per launch from profiles/kb_sweep_fast_dram_branch256.md "
+                                         "(first 20 launches, all 256 solves active, algorithmic 2.95e8 B each): "
+                                         "the shared geometries stay in L2",
+                         "kernel": "kb_sweep_fast",
                          "bytes_per_launch": sweep_bytes / max(sweep_launches, 1),
                          "ms_per_launch": sweep_ms / max(sweep_launches, 1), "peak_source": peak_kind,
-                         "sweep_share_of_replay": sweep_ms / (s1["replay_ms"] - s0["replay_ms"])},
+                         "sweep_share_of_replay": sweep_ms / replay_ms},
             "tuning": tune, "clocks": clk, "gpu_launches": int(launches),
             "outer_iterations": int(sum(r["iterations"] for r in results))}
 
-    # served request stream
+    # served request stream: Poisson arrivals at several rates
     if not args.no_serve:
         scases = W.branch_cases(512, seed=11, weights=(0.4, 0.3, 0.2, 0.1), groups=(7, 23))
         sb = {}
         for size, ng, xml, xsl in scases:
             if (size, ng) not in sb:
                 sb[(size, ng)] = m.Problem(xml, xsl)
-        rate = 1000.0
-        arr = poisson_arrivals(len(scases), rate, seed=5)
-        rq = [Request(sb[(size, ng)], xsl, float(a)) for (size, ng, xml, xsl), a in zip(scases, arr)]
-        SE = m.BatchEngine(precision=1, capacity=256, bundles_per_unit=bpu)
-        serve(SE, rq[:64], n_pin_max)  # warm-up: captures
-        rep = serve(SE, rq, n_pin_max)
-        ok = all(r is not None and r["error"] == 0 for r in rep.results)
-        line["serving"] = {"rate_req_per_s": rate, "requests": len(rq), "solves_per_s": rep.solves_per_s,
-                           "p50_ms": rep.percentile_ms(50), "p99_ms": rep.percentile_ms(99), "all_ok": ok,
-                           "mix": "sizes 1/3/7/17 weighted 0.4/0.3/0.2/0.1, groups 7 or 23",
-                           "budget": "80% of free device memory"}
-        SE.close()
+        # one lane per group count: 7-group solves do not wait on 23-group replays
+        free_b = torch.cuda.mem_get_info()[0]
+        SE = {ng: m.BatchEngine(precision=1, capacity=256, mem_budget=0.4 * free_b, bundles_per_unit=bpu)
+              for ng in (7, 23)}
+        warm = [Request(sb[(size, ng)], xsl, 0.0, ng) for size, ng, xml, xsl in scases[:64]]
+        serve(SE, warm, n_pin_max)  # captures the graphs
+        runs = []
+        for rate, nreq in ((100.0, 200), (400.0, 512), (1600.0, 512)):
+            arr = poisson_arrivals(nreq, rate, seed=5)
+            rq = [Request(sb[(size, ng)], xsl, float(a), ng)
+                  for (size, ng, xml, xsl), a in zip(scases[:nreq], arr)]
+            rep = serve(SE, rq, n_pin_max)
+            runs.append({"rate_req_per_s": rate, "requests": nreq, "solves_per_s": rep.solves_per_s,
+                         "p50_ms": rep.percentile_ms(50), "p99_ms": rep.percentile_ms(99),
+                         "all_ok": all(r is not None and r["error"] == 0 for r in rep.results)})
+        line["serving"] = {"runs": runs, "mix": "sizes 1/3/7/17 weighted 0.4/0.3/0.2/0.1, groups 7 or 23",
+                           "budget": "80% of free device memory, split between the two lanes", "capacity": 256,
+                           "lanes": "one engine per group count, pipelined on two streams",
+                           "latency": "request arrival to result read on the host"}
+        for e in SE.values():
+            e.close()
 
     if rank == 0 and not args.no_cpu:
         import oracle

@@ -203,7 +203,9 @@ int mocgpu_launch_count(int64_t *n);
  * sources and convergence test (k_tol, psi_tol, min_iter, max_iter of its
  * problem). Converged solves retire between iterations and queued ones take
  * their slots (continuous batching); admission waits until the device bytes
- * of the solve's geometry and state fit the memory budget. All solves of one
+ * of the solve's geometry and state fit the memory budget. Retired handles
+ * are kept and re-used by later solves of the same geometry, so steady-state
+ * admission allocates no device memory. All solves of one
  * engine must share polar angles per track set, inner iterations and the
  * CMFD switch; the Gauss-Seidel boundary update is the only one batched.
  * The engine keeps what it needs of a submitted problem, so the problem
@@ -248,6 +250,12 @@ int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xs
 /* Admits what fits, runs one outer iteration of every active solve, retires
  * finished ones; *n_active = solves still active. */
 int mocgpu_batch_step(mocgpu_batch *b, int *n_active);
+/* mocgpu_batch_step in two halves, so that several engines (each on its own
+ * stream) can have outer iterations on the GPU at the same time: launch
+ * admits and enqueues one replay and returns at once; finish waits for it
+ * and retires finished solves. A launch must be followed by a finish. */
+int mocgpu_batch_launch(mocgpu_batch *b, int *n_active);
+int mocgpu_batch_finish(mocgpu_batch *b, int *n_active);
 /* Steps until nothing is queued or active. */
 int mocgpu_batch_run(mocgpu_batch *b);
 /* *ready = 1 and the result (removed from the engine) once solve id is done;

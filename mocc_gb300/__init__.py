@@ -130,6 +130,8 @@ def load_library(build: bool = True):
         "mocgpu_batch_submit": (I, [P, P, CP, I64P]),
         "mocgpu_batch_step": (I, [P, IP]),
         "mocgpu_batch_run": (I, [P]),
+        "mocgpu_batch_launch": (I, [P, IP]),
+        "mocgpu_batch_finish": (I, [P, IP]),
         "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
         "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
         "mocgpu_batch_stream": (I, [P, C.POINTER(C.c_void_p)]),
@@ -451,6 +453,18 @@ class BatchEngine:
 
     def run(self):
         _check(self._lib.mocgpu_batch_run(self._h))
+
+    def launch(self) -> int:
+        """Enqueues one outer iteration of every active solve; returns at once."""
+        n = C.c_int()
+        _check(self._lib.mocgpu_batch_launch(self._h, C.byref(n)))
+        return n.value
+
+    def finish(self) -> int:
+        """Waits for the launched iteration and retires finished solves."""
+        n = C.c_int()
+        _check(self._lib.mocgpu_batch_finish(self._h, C.byref(n)))
+        return n.value
 
     def take(self, solve_id: int, n_pin_max: int = 1 << 16):
         """Result dict of a finished solve (None while it runs)."""

@@ -629,6 +629,22 @@ int mocgpu_batch_step(mocgpu_batch *b, int *n_active)
     });
 }
 
+int mocgpu_batch_launch(mocgpu_batch *b, int *n_active)
+{
+    return guarded([&] {
+        int n = eng(b).launch();
+        if (n_active) *n_active = n;
+    });
+}
+
+int mocgpu_batch_finish(mocgpu_batch *b, int *n_active)
+{
+    return guarded([&] {
+        int n = eng(b).finish();
+        if (n_active) *n_active = n;
+    });
+}
+
 int mocgpu_batch_run(mocgpu_batch *b)
 {
     return guarded([&] { eng(b).run(); });

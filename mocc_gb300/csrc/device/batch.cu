@@ -142,10 +142,25 @@ bool BatchEngine::try_admit(Pending &p)
         }
     }
     size_t need_state = Sweeper::state_bytes_for(f, precision_, (int)bcpg);
+    auto pit = pool_.find(p.P.get());
+    const bool reuse = pit != pool_.end() && !pit->second.empty();
+    if (reuse) need_state = 0;
     if (in_use_ + need_geo + need_state > budget_) {
-        // release resident geometries that no solve uses
+        // release pooled handles of other geometries, then resident
+        // geometries that no solve uses
+        for (auto it = pool_.begin(); it != pool_.end() && in_use_ + need_geo + need_state > budget_; ++it) {
+            if (it->first == p.P.get()) continue;
+            while (!it->second.empty() && in_use_ + need_geo + need_state > budget_) {
+                const size_t b = it->second.back()->state_bytes();
+                it->second.pop_back();
+                in_use_ -= b;
+                pooled_bytes_ -= b;
+            }
+        }
         for (auto it = geos_.begin(); it != geos_.end() && in_use_ + need_geo + need_state > budget_;) {
-            if (it->second.users == 0 && it->first != p.P.get()) {
+            auto pl = pool_.find(it->first);
+            const bool pooled = pl != pool_.end() && !pl->second.empty();
+            if (it->second.users == 0 && !pooled && it->first != p.P.get()) {
                 in_use_ -= it->second.geo->bytes();
                 it = geos_.erase(it);
             } else {
@@ -166,7 +181,15 @@ bool BatchEngine::try_admit(Pending &p)
     ge.users++;
 
     Slot &S = slots_[slot];
-    S.sw = std::make_unique<Sweeper>(*p.P, precision_, stream_, geo, p.xs.get());
+    if (reuse) {
+        S.sw = std::move(pit->second.back());
+        pit->second.pop_back();
+        S.sw->rebind(*p.P, p.xs.get());
+        pooled_bytes_ -= S.sw->state_bytes();
+    } else {
+        S.sw = std::make_unique<Sweeper>(*p.P, precision_, stream_, geo, p.xs.get());
+        in_use_ += S.sw->state_bytes();
+    }
     S.geo = geo;
     S.key = p.P.get();
     S.id = p.id;
@@ -178,7 +201,6 @@ bool BatchEngine::try_admit(Pending &p)
     S.t_submit = p.t_submit;
     S.t_admit = now();
     S.bytes = S.sw->state_bytes();
-    in_use_ += S.bytes;
 
     // EigenSolver::solve start (eigen_solver.cpp:131-160): flat flux, k = 1,
     // fission source at k = 1.
@@ -227,10 +249,12 @@ void BatchEngine::retire(int slot, int error, const std::string &msg, bool conve
     }
     r.t_done = now();
     done_[r.id] = std::move(r);
-    in_use_ -= S.bytes;
+    // the handle (and its device memory) waits in the pool for the next solve
+    // of the same geometry: admission then allocates nothing
+    pool_[S.key].push_back(std::move(S.sw));
+    pooled_bytes_ += S.bytes;
     auto it = geos_.find(S.key);
     if (it != geos_.end()) it->second.users--;
-    S.sw.reset();
     S.geo.reset();
     S.key = nullptr;
     S.id = -1;
@@ -402,8 +426,9 @@ void BatchEngine::capture()
     st_.captures++;
 }
 
-int BatchEngine::step()
+int BatchEngine::launch()
 {
+    if (in_flight_) MOCGPU_THROW(1, "the previous outer iteration has not been finished");
     // continuous batching: fill free slots from the queue, in order
     while (!queue_.empty()) {
         if (try_admit(queue_.front())) {
@@ -434,7 +459,19 @@ int BatchEngine::step()
     MOCGPU_CUDA(cudaEventRecord(rep1_, stream_));
     note_launches(graph_nodes_);
     MOCGPU_CUDA(copy_async(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
+    in_flight_ = true;
+    return (int)act_.size();
+}
+
+int BatchEngine::finish()
+{
+    if (!in_flight_) {
+        int n = 0;
+        for (const Slot &S : slots_) n += S.id >= 0;
+        return n;
+    }
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    in_flight_ = false;
     st_.graph_replays++;
     st_.outer_iterations += (int64_t)act_.size();
     {
@@ -477,6 +514,12 @@ int BatchEngine::step()
     int n = 0;
     for (const Slot &S : slots_) n += S.id >= 0;
     return n;
+}
+
+int BatchEngine::step()
+{
+    launch();
+    return finish();
 }
 
 void BatchEngine::run()

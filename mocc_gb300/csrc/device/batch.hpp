@@ -63,6 +63,13 @@ class BatchEngine {
     // Admits queued solves that fit, runs one outer iteration of every active
     // solve and retires the finished ones. Returns the number still active.
     int step();
+    // step() in two halves, so that several engines on their own streams can
+    // have their outer iterations on the GPU at the same time: launch()
+    // admits, (re)captures and enqueues one replay and returns at once;
+    // finish() waits for it and retires the finished solves. Both return the
+    // number of active solves.
+    int launch();
+    int finish();
     // Steps until nothing is queued or active.
     void run();
     // Finished result of solve `id` (removed from the engine); false if the
@@ -118,6 +125,10 @@ class BatchEngine {
         int users = 0;
     };
     std::map<const Problem *, GeoEntry> geos_;
+    // retired solve handles kept for reuse, by geometry
+    std::map<const Problem *, std::vector<std::unique_ptr<Sweeper>>> pool_;
+    size_t pooled_bytes_ = 0;
+    bool in_flight_ = false;
     BatchStats st_{};
 
     // batch configuration fixed by the first solve

@@ -120,18 +120,22 @@ __device__ double thickness(const CmfdView &c, int cell, int nrm)
 }
 __device__ __forceinline__ double cell_vol(const CmfdView &c, int i) { return c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz; }
 
+// Row i of the 5-point operator applied to x.
+__device__ __forceinline__ double spmv_row(const double *__restrict__ m, const double *x, int i, int n, int nx)
+{
+    double v = m[i] * x[i];
+    int ix = i % nx;
+    if (ix > 0) v += m[n + i] * x[i - 1];
+    if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
+    if (i >= nx) v += m[3 * n + i] * x[i - nx];
+    if (i + nx < n) v += m[4 * n + i] * x[i + nx];
+    return v;
+}
+
 __device__ void spmv(const CmfdView &c, const double *__restrict__ m, const double *x, double *y)
 {
     const int n = c.n_cell, nx = c.nx;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double v = m[i] * x[i];
-        int ix = i % nx;
-        if (ix > 0) v += m[n + i] * x[i - 1];
-        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
-        if (i >= nx) v += m[3 * n + i] * x[i - nx];
-        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
-        y[i] = v;
-    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = spmv_row(m, x, i, n, nx);
 }
 
 // b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
@@ -203,9 +207,12 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
             y[i] = pi * m[5 * n + i];
         }
         B.sync();
-        spmv(c, m, y, v);
         double r0v = 0.0, dummy = 0.0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) r0v += r0[i] * v[i];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double vi = spmv_row(m, y, i, n, c.nx);
+            v[i] = vi;
+            r0v += r0[i] * vi;
+        }
         B.sum2(r0v, dummy);
         alpha = rho / r0v;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -214,11 +221,12 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
             z[i] = si * m[5 * n + i];
         }
         B.sync();
-        spmv(c, m, z, t);
         double tt = 0.0, ts = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            tt += t[i] * t[i];
-            ts += t[i] * s[i];
+            const double ti = spmv_row(m, z, i, n, c.nx);
+            t[i] = ti;
+            tt += ti * ti;
+            ts += ti * s[i];
         }
         B.sum2(tt, ts);
         om = (tt > 0.0) ? ts / tt : 0.0;
@@ -287,6 +295,8 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     const int n = c.n_cell, G = c.G, ns = c.n_surf;
     // work vectors: b, x (group flux copy), 8 BiCGSTAB vectors
     double *vec = vec_in_smem ? sm + 128 : c.vec;
+    // mode 2: the current group's operator is also staged in shared memory
+    double *ms = (vec_in_smem == 2) ? sm + 128 + 10 * n : nullptr;
     double *b = vec, *x = vec + n, *w = vec + 2 * n;
     double k = *c.k;
     if (c.fixup)
@@ -379,6 +389,10 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             const double *m = c.mat + (size_t)g * 6 * n;
             double *fg = c.flux + (size_t)g * n;
             B.sync();
+            if (ms) {
+                for (int i = threadIdx.x; i < 6 * n; i += blockDim.x) ms[i] = m[i];
+                m = ms;
+            }
             build_source(c, g, b);
             for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = fg[i];
             B.sync();
@@ -424,8 +438,7 @@ __global__ void kb_cmfd_solve(BatchViews b, int vec_in_smem)
     const int slot = b.act[blockIdx.x];
     CmfdView c = b.cv[slot];
     c.has_radial = (c.red[RED_HAS_RADIAL] != 0.0) ? 1 : 0;
-    if (!vec_in_smem || 10 * c.n_cell + 128 > 10 * b.max_cell + 128) vec_in_smem = 0;
-    cmfd_body(c, vec_in_smem);
+    cmfd_body(c, vec_in_smem); // the CTA's shared memory is sized for the largest mesh of the batch
     if (threadIdx.x == 0) c.red[RED_CMFD_ITS] += c.stats[0];
 }
 
@@ -442,13 +455,23 @@ static int cmfd_warps(int n_cell)
     return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
 
+// Shared-memory mode of a CMFD CTA: 2 = work vectors and the current group's
+// operator, 1 = work vectors only, 0 = nothing (vectors in global memory).
+static int cmfd_smem_mode(int n_cell, size_t *bytes)
+{
+    const size_t base = 128 * sizeof(double), lim = 200 * 1024;
+    const size_t vec = (size_t)10 * n_cell * sizeof(double), op = (size_t)6 * n_cell * sizeof(double);
+    int mode = (base + vec + op <= lim) ? 2 : (base + vec <= lim) ? 1 : 0;
+    *bytes = base + (mode >= 1 ? vec : 0) + (mode == 2 ? op : 0);
+    return mode;
+}
+
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
 {
     const int max_cell = b.max_cell;
     const int nw = cmfd_warps(max_cell);
-    size_t vec_bytes = (size_t)10 * max_cell * sizeof(double);
-    int in_smem = (vec_bytes + 128 * sizeof(double)) <= 200 * 1024 ? 1 : 0;
-    size_t smem = 128 * sizeof(double) + (in_smem ? vec_bytes : 0);
+    size_t smem = 0;
+    const int in_smem = cmfd_smem_mode(max_cell, &smem);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         MOCGPU_CUDA(cudaFuncSetAttribute(kb_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -461,9 +484,8 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
 void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
 {
     const int nw = cmfd_warps(c.n_cell);
-    size_t vec_bytes = (size_t)10 * c.n_cell * sizeof(double);
-    int in_smem = (vec_bytes + 128 * sizeof(double)) <= 200 * 1024 ? 1 : 0;
-    size_t smem = 128 * sizeof(double) + (in_smem ? vec_bytes : 0);
+    size_t smem = 0;
+    const int in_smem = cmfd_smem_mode(c.n_cell, &smem);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         MOCGPU_CUDA(cudaFuncSetAttribute(k_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -63,6 +63,18 @@ template <typename T> struct DevBuf {
         }
     }
     template <typename V> void upload(const V &v) { upload(v.data(), v.size()); }
+    // Copies into the existing allocation when the size matches (no allocation).
+    template <typename V> void assign(const V &v)
+    {
+        if (v.size() != n) {
+            upload(v);
+            return;
+        }
+        if (n) {
+            note_copy_bytes(cudaMemcpyHostToDevice, n * sizeof(T));
+            MOCGPU_CUDA(cudaMemcpy(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+        }
+    }
     void zero(cudaStream_t s = 0)
     {
         if (n) MOCGPU_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));

@@ -132,6 +132,12 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         if (nrm == 2) MOCGPU_THROW(6, "track crosses a z-normal surface");
         return surf * 2 + nrm;
     };
+    // A track that leaves the core exactly through a pin-cell corner on the
+    // core boundary has its second corner surface recorded after the walk
+    // has stepped out of the core (the extra record of ray.cpp:147-166).
+    // MOCC then indexes a surface from the out-of-core cell, which is
+    // undefined; that second crossing lies outside the core, so it is
+    // dropped here.
     std::vector<int> efb{0}, efp, efc, ebb{0}, ebp, ebc;
     for (int t = 0; t < f.n_tracks; t++) {
         int n = (int)(f.trk_seg_begin[t + 1] - f.trk_seg_begin[t]);
@@ -142,12 +148,15 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         for (int c = c0; c < c1; c++) {
             int s = f.cm_fw[c];
             if (s != INVALID) {
-                if (cell < 0) MOCGPU_THROW(6, "coarse walk left the core (forward)");
                 k += f.cm_nseg_fw[c];
-                efp.push_back(k);
-                efc.push_back(coarse_surf(cell, s) * 2 + (s == NORTH || s == SOUTH ? 1 : 0));
+                if (cell >= 0) {
+                    efp.push_back(k);
+                    efc.push_back(coarse_surf(cell, s) * 2 + (s == NORTH || s == SOUTH ? 1 : 0));
+                } else if (f.cm_nseg_fw[c] != 0) {
+                    MOCGPU_THROW(6, "coarse walk left the core before the track ends (forward)");
+                }
             }
-            cell = (cell >= 0) ? neighbor(cell, s) : cell;
+            if (cell >= 0) cell = neighbor(cell, s);
         }
         if (k != n) MOCGPU_THROW(6, "coarse forward walk does not end at the last segment");
         efb.push_back((int)efp.size());
@@ -158,12 +167,15 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         for (int c = c0; c < c1; c++) {
             int s = f.cm_bw[c];
             if (s != INVALID) {
-                if (cell < 0) MOCGPU_THROW(6, "coarse walk left the core (backward)");
                 k -= f.cm_nseg_bw[c];
-                ebp.push_back(k);
-                ebc.push_back(coarse_surf(cell, s) * 2 + (s == NORTH || s == SOUTH ? 1 : 0));
+                if (cell >= 0) {
+                    ebp.push_back(k);
+                    ebc.push_back(coarse_surf(cell, s) * 2 + (s == NORTH || s == SOUTH ? 1 : 0));
+                } else if (f.cm_nseg_bw[c] != 0) {
+                    MOCGPU_THROW(6, "coarse walk left the core before the track ends (backward)");
+                }
             }
-            cell = (cell >= 0) ? neighbor(cell, s) : cell;
+            if (cell >= 0) cell = neighbor(cell, s);
         }
         if (k != 0) MOCGPU_THROW(6, "coarse backward walk does not end at the first segment");
         ebb.push_back((int)ebp.size());

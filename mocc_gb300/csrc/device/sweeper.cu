@@ -162,6 +162,52 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
 
 Sweeper::~Sweeper() = default;
 
+void Sweeper::rebind(const Problem &P, const CrossSections *xs)
+{
+    const FlatProblem &pf = P.flat;
+    if (pf.n_fsr != f_.n_fsr || pf.ng != f_.ng || pf.n_mat != f_.n_mat || pf.n_pin != f_.n_pin ||
+        pf.n_tracks != f_.n_tracks || pf.n_seg != f_.n_seg)
+        MOCGPU_THROW(1, "rebind needs a problem with the same traced geometry and materials");
+    FlatProblem f = flat_without_tracks(pf);
+    if (xs) {
+        if (xs->ng != f.ng || xs->xstr.size() != f.xstr.size() || xs->scat.size() != f.scat.size())
+            MOCGPU_THROW(4, "cross sections do not match the problem's materials and groups");
+        f.xstr = xs->xstr;
+        f.xsnf = xs->xsnf;
+        f.xsf = xs->xsf;
+        f.xsch = xs->xsch;
+        f.scat = xs->scat;
+    }
+    f_ = std::move(f);
+    opts_ = P.opts;
+    xstr_.assign(f_.xstr);
+    xsnf_.assign(f_.xsnf);
+    xsf_.assign(f_.xsf);
+    xsch_.assign(f_.xsch);
+    scat_.assign(f_.scat);
+    gv_.xstr = xstr_.p;
+    gv_.xsnf = xsnf_.p;
+    gv_.xsf = xsf_.p;
+    gv_.xsch = xsch_.p;
+    gv_.scat = scat_.p;
+    n_fissile_ = 0;
+    const int G = f_.ng;
+    for (int r = 0; r < f_.n_fsr; r++) {
+        bool fis = false;
+        for (int g = 0; g < G; g++)
+            if (f_.xsnf[(size_t)f_.fsr_mat[r] * G + g] > 0.0) fis = true;
+        if (fis) n_fissile_++;
+    }
+    cv_.k_tol = opts_.cmfd_k_tol;
+    cv_.psi_tol = opts_.cmfd_psi_tol;
+    cv_.resid_reduction = opts_.cmfd_resid_reduction;
+    cv_.max_iter = opts_.cmfd_max_iter;
+    cv_.fixup = opts_.cmfd_negative_fixup ? 1 : 0;
+    double nfis = n_fissile_;
+    MOCGPU_CUDA(copy_async(red_.p + RED_N_FISSILE, &nfis, sizeof(double), cudaMemcpyHostToDevice, stream_));
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void Sweeper::check_status()
 {
     unsigned st = 0;

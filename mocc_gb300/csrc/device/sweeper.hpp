@@ -40,6 +40,10 @@ class Sweeper {
     Sweeper(const Sweeper &) = delete;
     Sweeper &operator=(const Sweeper &) = delete;
 
+    // Re-targets this handle (same traced geometry, same materials) at
+    // another solve: new options and cross sections, no device allocation.
+    void rebind(const Problem &P, const CrossSections *xs = nullptr);
+
     int precision() const { return precision_; }
     const FlatProblem &flat() const { return f_; }
     const SolverOptions &options() const { return opts_; }

@@ -433,6 +433,15 @@ const PinMesh *CoreMesh::get_pinmesh(Point2 &p, int &first_reg) const
     return pm;
 }
 
+int CoreMesh::point_cell(Point2 p) const
+{
+    long ix = std::upper_bound(x_vec.begin(), x_vec.end(), p.x) - x_vec.begin() - 1;
+    long iy = std::upper_bound(y_vec.begin(), y_vec.end(), p.y) - y_vec.begin() - 1;
+    ix = std::min<long>(nx - 1, std::max<long>(0, ix));
+    iy = std::min<long>(ny - 1, std::max<long>(0, iy));
+    return coarse_cell((int)ix, (int)iy);
+}
+
 void CoreMesh::trace(std::vector<Point2> &ps) const
 {
     Line l(ps[0], ps[1]);
@@ -442,6 +451,22 @@ void CoreMesh::trace(std::vector<Point2> &ps) const
     }
     std::sort(ps.begin(), ps.end());
     ps.erase(std::unique(ps.begin(), ps.end()), ps.end());
+    // A ray that starts or ends (to within rounding) on a pin-cell corner
+    // picks up a pin-line crossing a few 1e-13 cm from its end point that the
+    // fuzzy comparison does not merge. MOCC keeps that sliver as a pin
+    // crossing of its own, which adds a spurious coarse-surface crossing and
+    // shifts the coarse-current walk of the whole ray by one cell (breaking
+    // the CMFD balance on cores with vacuum faces). Crossings closer than
+    // kSliver to either end point are dropped here; the end point's cell is
+    // already chosen by the corner convention of coarse_boundary_cell().
+    constexpr double kSliver = 1e-10;
+    if (ps.size() > 2) {
+        const Point2 a = ps.front(), b = ps.back();
+        auto near_end = [&](const Point2 &p) {
+            return std::hypot(p.x - a.x, p.y - a.y) < kSliver || std::hypot(p.x - b.x, p.y - b.y) < kSliver;
+        };
+        ps.erase(std::remove_if(ps.begin() + 1, ps.end() - 1, near_end), ps.end() - 1);
+    }
 }
 
 std::vector<double> CoreMesh::areas() const

@@ -119,6 +119,8 @@ struct CoreMesh {
     int n_surf_plane() const { return (nx + 1) * ny + (ny + 1) * nx + nx * ny; }
     int n_surf() const { return (nx + 1) * ny + (ny + 1) * nx + 2 * nx * ny; }
     int coarse_cell(int ix, int iy) const { return iy * nx + ix; }
+    // Coarse cell containing an interior point (no boundary disambiguation).
+    int point_cell(Point2 p) const;
     int coarse_surf(int cell, Surface s) const { return coarse_surf_[cell * 6 + (int)s]; }
     int coarse_neighbor(int cell, Surface s) const;
     Normal surface_normal(int surf) const;

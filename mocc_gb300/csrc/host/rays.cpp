@@ -33,56 +33,110 @@ std::pair<int, int> rational_approximation(double target, double tol, int max_d)
     return {a, b};
 }
 
+namespace {
+
+// One pin crossing of the fine trace: its coarse cell, segment count and
+// chord length.
+struct PinCrossing {
+    int cell, nseg;
+    double len;
+};
+
+// Crossings shorter than this (a ray grazing a pin-cell corner) are slivers:
+// the fuzzy point comparisons of the trace can leave them as pin crossings of
+// their own, sometimes assigned to a pin off the ray's path.
+constexpr double kSliver = 1e-9;
+
+int cell_x(const CoreMesh &m, int c) { return c % m.nx; }
+int cell_y(const CoreMesh &m, int c) { return c / m.nx; }
+
+// Coarse crossings of one direction of a ray (moc::Current's walk data,
+// ray.cpp:52-166): the entry cell and surface, then for every crossing the
+// surface and the number of segments before it. The surfaces between two
+// pins follow the cells of the traced segments (adjacent cells: one face;
+// diagonal cells: the corner pair in MOCC's order for the octant, the second
+// after zero segments), so the walk always visits the cells the segments lie
+// in. Slivers are folded into the neighbouring crossing in traversal order.
+void coarse_walk(const CoreMesh &m, const std::vector<PinCrossing> &px, int octant, Point2 start, Point2 end,
+                 int &cell0, int &surf0, std::vector<Surface> &surfs, std::vector<int> &nsegs)
+{
+    std::vector<int> cells, counts;
+    int pending = 0;
+    for (const PinCrossing &c : px) {
+        const bool sliver = c.len < kSliver && px.size() > 1;
+        if (sliver) {
+            if (counts.empty()) pending += c.nseg;
+            else counts.back() += c.nseg;
+            continue;
+        }
+        if (!cells.empty() && cells.back() == c.cell) {
+            counts.back() += c.nseg + pending; // a split of one pin crossing
+        } else {
+            cells.push_back(c.cell);
+            counts.push_back(c.nseg + pending);
+        }
+        pending = 0;
+    }
+    if (cells.empty()) MOCGPU_THROW(6, "ray crosses no pin");
+    if (pending) counts.back() += pending;
+
+    Surface s[2];
+    cell0 = cells.front();
+    if (m.coarse_norm_point(start, octant, s) != 1) MOCGPU_THROW(6, "ray starts on more than one coarse surface");
+    surf0 = m.coarse_surf(cell0, s[0]);
+    for (size_t k = 0; k + 1 < cells.size(); k++) {
+        const int dx = cell_x(m, cells[k + 1]) - cell_x(m, cells[k]);
+        const int dy = cell_y(m, cells[k + 1]) - cell_y(m, cells[k]);
+        Surface fx = dx > 0 ? EAST : WEST, fy = dy > 0 ? NORTH : SOUTH;
+        if (std::abs(dx) + std::abs(dy) == 1) {
+            surfs.push_back(dx != 0 ? fx : fy);
+            nsegs.push_back(counts[k]);
+        } else if (std::abs(dx) == 1 && std::abs(dy) == 1) {
+            // corner: x face first, then y face (mesh.cpp:471-493)
+            surfs.push_back(fx);
+            surfs.push_back(fy);
+            nsegs.push_back(counts[k]);
+            nsegs.push_back(0);
+        } else {
+            MOCGPU_THROW(6, "consecutive pin crossings of a ray are not neighbouring cells");
+        }
+    }
+    const int ns = m.coarse_norm_point(end, octant, s);
+    if (ns < 1) MOCGPU_THROW(6, "ray does not end on a coarse surface");
+    for (int j = 0; j < ns; j++) surfs.push_back(s[j]);
+    nsegs.push_back(counts.back());
+    if (ns > 1) nsegs.push_back(0);
+}
+
+} // namespace
+
 Ray::Ray(Point2 a, Point2 b, std::array<int, 2> bc_, const CoreMesh &mesh) : bc(bc_), p1(a), p2(b)
 {
     std::vector<Point2> ps{a, b};
     mesh.trace(ps);
     const std::vector<Point2> &cps = ps;
 
-    // Fine trace, pin crossing by pin crossing.
-    std::vector<int> cm_nseg;
+    // Fine trace, pin crossing by pin crossing (ray.cpp:62-83).
+    std::vector<PinCrossing> px;
     Point2 prev = cps.front();
     for (size_t i = 1; i < ps.size(); i++) {
         Point2 pin_p = midpoint(ps[i], prev);
+        const Point2 mid = pin_p;
         int first_reg = 0;
         const PinMesh *pm = mesh.get_pinmesh(pin_p, first_reg);
         int n = pm->trace(prev - pin_p, ps[i] - pin_p, first_reg, seg_len, seg_fsr);
-        cm_nseg.push_back(n);
+        px.push_back(PinCrossing{mesh.point_cell(mid), n, std::hypot(ps[i].x - prev.x, ps[i].y - prev.y)});
         prev = ps[i];
     }
 
     // Coarse crossings, forward then backward.
-    Surface s[2];
-    int octant = (b.x > a.x) ? 1 : 2;
+    const int octant = (b.x > a.x) ? 1 : 2;
     std::vector<Surface> surfs_fw, surfs_bw;
     std::vector<int> nsegs_fw, nsegs_bw;
-    {
-        cm_cell_fw = mesh.coarse_boundary_cell(cps.front(), octant);
-        int ns = mesh.coarse_norm_point(cps.front(), octant, s);
-        if (ns != 1) MOCGPU_THROW(6, "ray starts on more than one coarse surface");
-        cm_surf_fw = mesh.coarse_surf(cm_cell_fw, s[0]);
-        for (size_t k = 0; k < cm_nseg.size(); k++) {
-            ns = mesh.coarse_norm_point(cps[k + 1], octant, s);
-            for (int j = 0; j < ns; j++) surfs_fw.push_back(s[j]);
-            nsegs_fw.push_back(cm_nseg[k]);
-            if (ns > 1) nsegs_fw.push_back(0);
-        }
-    }
-    std::reverse(cm_nseg.begin(), cm_nseg.end());
-    octant = (octant == 1) ? 3 : 4;
-    {
-        size_t np = cps.size();
-        cm_cell_bw = mesh.coarse_boundary_cell(cps[np - 1], octant);
-        int ns = mesh.coarse_norm_point(cps[np - 1], octant, s);
-        if (ns != 1) MOCGPU_THROW(6, "ray ends on more than one coarse surface");
-        cm_surf_bw = mesh.coarse_surf(cm_cell_bw, s[0]);
-        for (size_t k = 0; k < cm_nseg.size(); k++) {
-            ns = mesh.coarse_norm_point(cps[np - 2 - k], octant, s);
-            for (int j = 0; j < ns; j++) surfs_bw.push_back(s[j]);
-            nsegs_bw.push_back(cm_nseg[k]);
-            if (ns > 1) nsegs_bw.push_back(0);
-        }
-    }
+    coarse_walk(mesh, px, octant, cps.front(), cps.back(), cm_cell_fw, cm_surf_fw, surfs_fw, nsegs_fw);
+    std::reverse(px.begin(), px.end());
+    coarse_walk(mesh, px, octant == 1 ? 3 : 4, cps.back(), cps.front(), cm_cell_bw, cm_surf_bw, surfs_bw, nsegs_bw);
+
     size_t stp = std::min(nsegs_fw.size(), nsegs_bw.size());
     for (size_t i = 0; i < stp; i++) {
         CoarseCrossing c;
@@ -93,7 +147,7 @@ Ray::Ray(Point2 a, Point2 b, std::array<int, 2> bc_, const CoreMesh &mesh) : bc(
         cm_data.push_back(c);
     }
     // A corner double-crossing at one end only: extra record, no-op on the
-    // other direction.
+    // other direction (ray.cpp:147-166).
     if (nsegs_fw.size() > nsegs_bw.size()) {
         CoarseCrossing c;
         c.fw = surfs_fw.back();

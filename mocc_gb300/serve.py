@@ -1,12 +1,17 @@
-"""Request loop over the batch engine: continuous batching of arriving solves.
+"""Request loop over batch engines: continuous batching of arriving solves.
 
 Requests arrive on a schedule (a seeded Poisson process for the benchmark);
-each is submitted to the :class:`~mocc_gb300.BatchEngine` as soon as its
-arrival time has passed, the engine admits it into a free slot once its
-geometry and state fit the device-memory budget, every active solve advances
-one power iteration per graph replay, and results are collected as solves
-retire. Latency is measured from a request's arrival time to the moment its
-result is read on the host, so queueing is included.
+each is submitted as soon as its arrival time has passed to the engine
+(lane) its key selects, the engine admits it into a free slot once its
+geometry and state fit the device-memory budget, every active solve of a
+lane advances one power iteration per graph replay, and results are
+collected as solves retire. Lanes run on their own CUDA streams and are
+stepped in a pipeline (finish one lane's iteration, launch its next, move
+on), so their iterations overlap on the GPU: solves with few energy groups
+need not wait for the replays of 23-group solves, and one lane's
+latency-bound CMFD phase runs beside another lane's sweeps. Latency is
+measured from a request's arrival time to the moment its result is read on
+the host, so queueing is included.
 """
 from __future__ import annotations
 
@@ -21,6 +26,7 @@ class Request:
     problem: object          # mocc_gb300.Problem whose traced geometry is used
     xsl: str | None = None   # cross sections for its materials (None: its own)
     arrival: float = 0.0     # seconds after the start of the run
+    lane: object = 0         # key of the engine that runs it
 
 
 @dataclass
@@ -44,35 +50,64 @@ def poisson_arrivals(n: int, rate: float, seed: int) -> np.ndarray:
     return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
-def serve(engine, requests: list[Request], max_pins: int = 1 << 12) -> ServeReport:
-    """Runs the request stream to completion; returns latencies and results
-    in request order."""
+def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeReport:
+    """Runs the request stream to completion on `engines` (one BatchEngine, or
+    a dict lane key -> BatchEngine); returns latencies and results in request
+    order."""
+    if not isinstance(engines, dict):
+        engines = {0: engines}
+        requests = [Request(r.problem, r.xsl, r.arrival, 0) for r in requests]
     order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
     t0 = time.perf_counter()
     nxt = 0
-    outstanding: dict[int, int] = {}  # solve id -> request index
+    outstanding = {k: {} for k in engines}  # lane -> {solve id: request index}
+    in_flight = {k: False for k in engines}
     lat = [0.0] * len(requests)
     res = [None] * len(requests)
     done = 0
-    while done < len(requests):
+
+    def admit_arrivals():
+        nonlocal nxt
         now = time.perf_counter() - t0
         while nxt < len(order) and requests[order[nxt]].arrival <= now:
             i = order[nxt]
-            outstanding[engine.submit(requests[i].problem, requests[i].xsl)] = i
+            r = requests[i]
+            outstanding[r.lane][engines[r.lane].submit(r.problem, r.xsl)] = i
             nxt += 1
-        if outstanding:
-            engine.step()
-            for sid in list(outstanding):
-                r = engine.take(sid, max_pins)
-                if r is None:
-                    continue
-                i = outstanding.pop(sid)
-                lat[i] = time.perf_counter() - t0 - requests[i].arrival
-                res[i] = r
-                done += 1
-        elif nxt < len(order):
+
+    while done < len(requests):
+        admit_arrivals()
+        busy = False
+        for k, eng in engines.items():
+            if in_flight[k]:
+                eng.finish()
+                in_flight[k] = False
+                for sid in list(outstanding[k]):
+                    r = eng.take(sid, max_pins)
+                    if r is None:
+                        continue
+                    i = outstanding[k].pop(sid)
+                    lat[i] = time.perf_counter() - t0 - requests[i].arrival
+                    res[i] = r
+                    done += 1
+                admit_arrivals()
+            if outstanding[k]:
+                eng.launch()
+                in_flight[k] = True
+                busy = True
+        if not busy and nxt < len(order):
             wait = requests[order[nxt]].arrival - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(min(wait, 1e-3))
     wall = time.perf_counter() - t0
     return ServeReport(n=len(requests), wall_s=wall, latencies_s=lat, results=res)
+
+
+def run_batch(engines, jobs, max_pins: int = 1 << 12) -> list:
+    """Submits every (problem, xsl, lane) job at once and runs the lanes in a
+    pipeline until all finish; returns the results in job order."""
+    reqs = [Request(p, x, 0.0, lane) for p, x, lane in jobs]
+    if not isinstance(engines, dict):
+        engines = {0: engines}
+        reqs = [Request(r.problem, r.xsl, 0.0, 0) for r in reqs]
+    return serve(engines, reqs, max_pins).results

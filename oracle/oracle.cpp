@@ -386,24 +386,28 @@ struct orc_solver {
         current[(size_t)surf_bw * G + group] -= psi2[iseg_bw] * cw[norm_bw];
         surface_flux[(size_t)surf_fw * G + group] += psi1[iseg_fw] * fw[norm_fw];
         surface_flux[(size_t)surf_bw * G + group] += psi2[iseg_bw] * fw[norm_bw];
+        // A crossing recorded after the walk stepped out of the core (a track
+        // leaving through a pin-cell corner on the core boundary,
+        // ray.cpp:147-166) lies outside the core and is dropped; MOCC indexes
+        // a surface from the out-of-core cell there, which is undefined.
         for (int c = p.trk_cm_begin[t]; c < p.trk_cm_begin[t + 1]; c++) {
             int fws = p.cm_fw[c], bws = p.cm_bw[c];
-            if (fws != INVALID) {
-                iseg_fw += p.cm_nseg_fw[c];
+            if (fws != INVALID) iseg_fw += p.cm_nseg_fw[c];
+            if (fws != INVALID && cell_fw >= 0) {
                 norm_fw = surface_to_normal(fws);
                 surf_fw = coarse_surf(cell_fw, fws);
                 current[(size_t)surf_fw * G + group] += psi1[iseg_fw] * cw[norm_fw];
                 surface_flux[(size_t)surf_fw * G + group] += psi1[iseg_fw] * fw[norm_fw];
             }
-            if (bws != INVALID) {
-                iseg_bw -= p.cm_nseg_bw[c];
+            if (bws != INVALID) iseg_bw -= p.cm_nseg_bw[c];
+            if (bws != INVALID && cell_bw >= 0) {
                 norm_bw = surface_to_normal(bws);
                 surf_bw = coarse_surf(cell_bw, bws);
                 current[(size_t)surf_bw * G + group] -= psi2[iseg_bw] * cw[norm_bw];
                 surface_flux[(size_t)surf_bw * G + group] += psi2[iseg_bw] * fw[norm_bw];
             }
-            cell_fw = (cell_fw >= 0) ? coarse_neighbor(cell_fw, fws) : cell_fw;
-            cell_bw = (cell_bw >= 0) ? coarse_neighbor(cell_bw, bws) : cell_bw;
+            if (cell_fw >= 0) cell_fw = coarse_neighbor(cell_fw, fws);
+            if (cell_bw >= 0) cell_bw = coarse_neighbor(cell_bw, bws);
         }
     }
 

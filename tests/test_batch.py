@@ -157,3 +157,27 @@ def test_batch_rejects_mismatched_configuration():
     with pytest.raises(m.MocgpuError) as e:
         E.submit(b)
     assert e.value.code == 1
+
+
+def test_pipelined_lanes_give_the_same_results():
+    from mocc_gb300.serve import run_batch
+    cases = _cases(8, seed=21, sizes=(1, 3, 7))
+    probs = [m.Problem(x, s) for x, s in cases]
+    one = _run(m.BatchEngine(precision=0, capacity=8), probs)
+    lanes = {0: m.BatchEngine(precision=0, capacity=3), 1: m.BatchEngine(precision=0, capacity=3)}
+    two = run_batch(lanes, [(P, None, i % 2) for i, P in enumerate(probs)])
+    for a, b in zip(one, two):
+        assert a["error"] == b["error"] == 0
+        assert a["iterations"] == b["iterations"]
+        assert abs(a["k"] - b["k"]) < 1e-11
+        assert max_pin_err(b["pin_powers"], a["pin_powers"]) < 1e-10
+
+
+def test_retired_handles_are_reused_without_allocation():
+    P = m.Problem(*W.lattice_case(3, 8, 0.05, "double", seed=8))
+    E = m.BatchEngine(precision=0, capacity=2)
+    first = _run(E, [P, P])
+    used = E.stats()["bytes_in_use"]
+    again = _run(E, [P, P, P, P])
+    assert E.stats()["bytes_in_use"] == used  # the two pooled handles served all four solves
+    assert all(abs(r["k"] - first[0]["k"]) < 1e-11 for r in again)

@@ -159,6 +159,19 @@ def test_vacuum_boundaries_small_core(precision):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
+def test_corner_exits_small_core(precision):
+    # 8 azimuths per octant on a core with vacuum faces: many tracks pass
+    # through, start or end on pin-cell corners
+    xml, xsl = W.minicore(n_lat=3, n_azi=8, spacing=0.05, precision="double")
+    P, S, O = _pair(xml, xsl, precision)
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"] and rb["converged"]
+    assert pcm(ra["k"], rb["k"]) < (1e-4 if precision == 0 else PCM_TOL)
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < (1e-8 if precision == 0 else PIN_TOL)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
 def test_ihm_on_gpu(ref_xsl, precision):
     from test_oracle_known_answers import analytic_spectrum, ihm_problem
     P = ihm_problem(ref_xsl, n_inner=200)
