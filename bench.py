@@ -362,24 +362,31 @@ def run_branch(args, rank, world):
         for size, ng, xml, xsl in scases:
             if (size, ng) not in sb:
                 sb[(size, ng)] = m.Problem(xml, xsl)
-        # one lane per group count: 7-group solves do not wait on 23-group replays
+        # one lane per (group count, lattice class): small solves (1x1, 3x3)
+        # do not wait on the replays of large ones, 7-group solves not on
+        # 23-group ones; the lanes' iterations overlap on the GPU
+        def lane_of(size, ng):
+            return (ng, "small" if size <= 3 else "large")
+
+        keys = [(ng, c) for ng in (7, 23) for c in ("small", "large")]
         free_b = torch.cuda.mem_get_info()[0]
-        SE = {ng: m.BatchEngine(precision=1, capacity=256, mem_budget=0.4 * free_b, bundles_per_unit=bpu)
-              for ng in (7, 23)}
-        warm = [Request(sb[(size, ng)], xsl, 0.0, ng) for size, ng, xml, xsl in scases[:64]]
+        SE = {k: m.BatchEngine(precision=1, capacity=256, mem_budget=0.8 * free_b / len(keys), bundles_per_unit=bpu)
+              for k in keys}
+        warm = [Request(sb[(size, ng)], xsl, 0.0, lane_of(size, ng)) for size, ng, xml, xsl in scases[:96]]
         serve(SE, warm, n_pin_max)  # captures the graphs
         runs = []
         for rate, nreq in ((100.0, 200), (400.0, 512), (1600.0, 512)):
             arr = poisson_arrivals(nreq, rate, seed=5)
-            rq = [Request(sb[(size, ng)], xsl, float(a), ng)
+            rq = [Request(sb[(size, ng)], xsl, float(a), lane_of(size, ng))
                   for (size, ng, xml, xsl), a in zip(scases[:nreq], arr)]
             rep = serve(SE, rq, n_pin_max)
             runs.append({"rate_req_per_s": rate, "requests": nreq, "solves_per_s": rep.solves_per_s,
                          "p50_ms": rep.percentile_ms(50), "p99_ms": rep.percentile_ms(99),
                          "all_ok": all(r is not None and r["error"] == 0 for r in rep.results)})
         line["serving"] = {"runs": runs, "mix": "sizes 1/3/7/17 weighted 0.4/0.3/0.2/0.1, groups 7 or 23",
-                           "budget": "80% of free device memory, split between the two lanes", "capacity": 256,
-                           "lanes": "one engine per group count, pipelined on two streams",
+                           "budget": "80% of free device memory, split between the lanes", "capacity": 256,
+                           "lanes": "one engine per (group count, lattice class 1-3 / 7-17 pins), pipelined on "
+                                    "four streams",
                            "latency": "request arrival to result read on the host"}
         for e in SE.values():
             e.close()

@@ -256,12 +256,18 @@ int mocgpu_batch_step(mocgpu_batch *b, int *n_active);
  * and retires finished solves. A launch must be followed by a finish. */
 int mocgpu_batch_launch(mocgpu_batch *b, int *n_active);
 int mocgpu_batch_finish(mocgpu_batch *b, int *n_active);
+/* *done = 1 when nothing is in flight or the launched iteration has
+ * completed, so that mocgpu_batch_finish would not block. */
+int mocgpu_batch_poll(mocgpu_batch *b, int *done);
 /* Steps until nothing is queued or active. */
 int mocgpu_batch_run(mocgpu_batch *b);
 /* *ready = 1 and the result (removed from the engine) once solve id is done;
  * pin_powers (may be NULL) receives res->n_pin values. */
 int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_result *res, double *pin_powers,
                         int n_pin_capacity);
+/* Ids of finished solves not taken yet: up to `capacity` into ids, the
+ * total in *n. */
+int mocgpu_batch_ready(mocgpu_batch *b, int64_t *ids, int capacity, int *n);
 int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out);
 /* The CUDA stream (cudaStream_t) of the engine's launches. */
 int mocgpu_batch_stream(mocgpu_batch *b, void **stream);

@@ -132,8 +132,10 @@ def load_library(build: bool = True):
         "mocgpu_batch_run": (I, [P]),
         "mocgpu_batch_launch": (I, [P, IP]),
         "mocgpu_batch_finish": (I, [P, IP]),
+        "mocgpu_batch_poll": (I, [P, IP]),
         "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
         "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
+        "mocgpu_batch_ready": (I, [P, I64P, I, IP]),
         "mocgpu_batch_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "mocgpu_batch_set_timing": (I, [P, I]),
         "mocgpu_copy_bytes": (I, [I64P, I64P]),
@@ -460,6 +462,12 @@ class BatchEngine:
         _check(self._lib.mocgpu_batch_launch(self._h, C.byref(n)))
         return n.value
 
+    def poll(self) -> bool:
+        """True when finish() would not block."""
+        d = C.c_int()
+        _check(self._lib.mocgpu_batch_poll(self._h, C.byref(d)))
+        return bool(d.value)
+
     def finish(self) -> int:
         """Waits for the launched iteration and retires finished solves."""
         n = C.c_int()
@@ -478,6 +486,17 @@ class BatchEngine:
         out["message"] = r.message.decode()
         out["pin_powers"] = pins[:r.n_pin].copy()
         return out
+
+    def ready(self) -> list[int]:
+        """Ids of finished solves whose results have not been taken."""
+        n = C.c_int()
+        _check(self._lib.mocgpu_batch_ready(self._h, None, 0, C.byref(n)))
+        if n.value == 0:
+            return []
+        ids = np.zeros(n.value, dtype=np.int64)
+        _check(self._lib.mocgpu_batch_ready(self._h, ids.ctypes.data_as(C.POINTER(C.c_int64)), n.value,
+                                            C.byref(n)))
+        return [int(i) for i in ids[:n.value]]
 
     def stats(self) -> dict:
         st = _BatchStats()

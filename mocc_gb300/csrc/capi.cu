@@ -645,6 +645,14 @@ int mocgpu_batch_finish(mocgpu_batch *b, int *n_active)
     });
 }
 
+int mocgpu_batch_poll(mocgpu_batch *b, int *done)
+{
+    return guarded([&] {
+        REQUIRE(done, "null argument");
+        *done = eng(b).poll() ? 1 : 0;
+    });
+}
+
 int mocgpu_batch_run(mocgpu_batch *b)
 {
     return guarded([&] { eng(b).run(); });
@@ -677,6 +685,16 @@ int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_resu
             REQUIRE(n_pin_capacity >= res->n_pin, "pin_powers buffer too small");
             std::memcpy(pin_powers, r.pin_powers.data(), sizeof(double) * r.pin_powers.size());
         }
+    });
+}
+
+int mocgpu_batch_ready(mocgpu_batch *b, int64_t *ids, int capacity, int *n)
+{
+    return guarded([&] {
+        REQUIRE(n && (ids || capacity == 0), "null argument");
+        std::vector<int64_t> v = eng(b).ready_ids();
+        *n = (int)v.size();
+        for (int i = 0; i < (int)v.size() && i < capacity; i++) ids[i] = v[i];
     });
 }
 

@@ -57,6 +57,7 @@ BatchEngine::~BatchEngine()
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (h_sum_) cudaFreeHost(h_sum_);
+    if (h_pins_) cudaFreeHost(h_pins_);
     for (cudaEvent_t e : tev_) cudaEventDestroy(e);
     if (rep0_) cudaEventDestroy(rep0_);
     if (rep1_) cudaEventDestroy(rep1_);
@@ -244,8 +245,13 @@ void BatchEngine::retire(int slot, int error, const std::string &msg, bool conve
     r.t_submit = S.t_submit;
     r.t_admit = S.t_admit;
     if (!error) {
-        r.pin_powers.resize(S.sw->flat().n_pin);
-        S.sw->pin_powers(r.pin_powers.data());
+        // fission-rate pin powers normalised to the fuel pin count, from the
+        // last replay's read-back (transport_sweeper.cpp:140-193)
+        const FlatProblem &f = S.sw->flat();
+        const double *row = h_pins_ + (size_t)slot * pins_stride_;
+        const double scale = f.n_fuel_2d / row[f.n_pin];
+        r.pin_powers.resize(f.n_pin);
+        for (int i = 0; i < f.n_pin; i++) r.pin_powers[i] = row[i] * scale;
     }
     r.t_done = now();
     done_[r.id] = std::move(r);
@@ -327,8 +333,7 @@ void BatchEngine::rebuild_lists()
                                         sizeof(int2) * items[ph].size(), cudaMemcpyHostToDevice, stream_));
     MOCGPU_CUDA(copy_async(d_nitems_.p, nitems.data(), sizeof(int) * nitems.size(), cudaMemcpyHostToDevice,
                                 stream_));
-    // pageable sources: wait for the copies before the host vectors go away
-    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    // (pageable sources are staged before each call returns: no wait needed)
     lists_dirty_ = false;
 }
 
@@ -360,6 +365,14 @@ void BatchEngine::capture()
     b.max_g = shape_.max_g;
     if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local);
     else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local);
+    // pin powers of every active solve, read back with the summary
+    pins_stride_ = shape_.max_pin + 1;
+    if ((size_t)cap_ * pins_stride_ > d_pins_.n) {
+        d_pins_.alloc((size_t)cap_ * pins_stride_);
+        if (h_pins_) cudaFreeHost(h_pins_);
+        h_pins_ = nullptr;
+        MOCGPU_CUDA(cudaMallocHost((void **)&h_pins_, sizeof(double) * (size_t)cap_ * pins_stride_));
+    }
 
     const int n_sweeps = shape_.max_g * n_inner_ * 2;
     if (timing_)
@@ -412,6 +425,7 @@ void BatchEngine::capture()
         launch_b_k_update(b, stream_);
         launch_b_errors(b, stream_);
         launch_b_summary(b, d_sum_.p, stream_);
+        launch_b_pin_powers(b, d_pins_.p, pins_stride_, stream_);
     } catch (...) {
         cudaGraph_t g = nullptr;
         cudaStreamEndCapture(stream_, &g);
@@ -459,6 +473,8 @@ int BatchEngine::launch()
     MOCGPU_CUDA(cudaEventRecord(rep1_, stream_));
     note_launches(graph_nodes_);
     MOCGPU_CUDA(copy_async(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(copy_async(h_pins_, d_pins_.p, sizeof(double) * (size_t)cap_ * pins_stride_, cudaMemcpyDeviceToHost,
+                           stream_));
     in_flight_ = true;
     return (int)act_.size();
 }
@@ -516,6 +532,16 @@ int BatchEngine::finish()
     return n;
 }
 
+bool BatchEngine::poll() const
+{
+    if (!in_flight_) return true;
+    cudaError_t e = cudaStreamQuery(stream_);
+    if (e == cudaSuccess) return true;
+    if (e == cudaErrorNotReady) return false;
+    MOCGPU_CUDA(e);
+    return false;
+}
+
 int BatchEngine::step()
 {
     launch();
@@ -537,6 +563,14 @@ bool BatchEngine::take_result(int64_t id, BatchResult &out)
     out = std::move(it->second);
     done_.erase(it);
     return true;
+}
+
+std::vector<int64_t> BatchEngine::ready_ids() const
+{
+    std::vector<int64_t> v;
+    v.reserve(done_.size());
+    for (const auto &kv : done_) v.push_back(kv.first);
+    return v;
 }
 
 BatchStats BatchEngine::stats() const

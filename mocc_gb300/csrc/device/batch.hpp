@@ -70,11 +70,16 @@ class BatchEngine {
     // number of active solves.
     int launch();
     int finish();
+    // true when no iteration is in flight or the launched one has completed
+    // (finish() would not block)
+    bool poll() const;
     // Steps until nothing is queued or active.
     void run();
     // Finished result of solve `id` (removed from the engine); false if the
     // solve has not finished.
     bool take_result(int64_t id, BatchResult &out);
+    // ids of the finished solves whose results have not been taken yet
+    std::vector<int64_t> ready_ids() const;
     BatchStats stats() const;
     double now() const; // engine clock (s)
     // Records CUDA events around every sweep launch of the captured graph so
@@ -147,6 +152,9 @@ class BatchEngine {
     DevBuf<int> d_nitems_;
     DevBuf<double> d_sum_;
     double *h_sum_ = nullptr; // pinned summary
+    DevBuf<double> d_pins_;    // [cap][pins_stride_] pin powers of the last replay
+    double *h_pins_ = nullptr; // pinned copy
+    int pins_stride_ = 0;
     std::vector<int> act_;
     bool lists_dirty_ = true;
 

@@ -278,6 +278,12 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     ev_bw_begin_.upload(ebb);
     ev_bw_pt_.upload(ebp);
     ev_bw_code_.upload(ebc);
+    if (precision == 0) {
+        psi_init_dev_.upload(reinterpret_cast<const unsigned char *>(psi_init.data()), psi_init.size() * 8);
+    } else {
+        std::vector<float> pf(psi_init.begin(), psi_init.end());
+        psi_init_dev_.upload(reinterpret_cast<const unsigned char *>(pf.data()), pf.size() * 4);
+    }
     {
         std::vector<int2> pf(efp.size()), pb(ebp.size());
         for (size_t i = 0; i < efp.size(); i++) pf[i] = make_int2(efp[i], efc[i]);
@@ -340,7 +346,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     bytes_ = seg_begin_.bytes() + trk_bc0_.bytes() * 3 + seg_fsr_.bytes() + seg_len_d_.bytes() + seg_len_f_.bytes() +
              fsr_mat_.bytes() + fsr_vol_.bytes() * 2 + sp_.bytes() + bc_off_.bytes() + wt_tgt_.bytes() +
              ev_fw_pt_.bytes() * 2 + ev_bw_pt_.bytes() * 2 + ev_fw_begin_.bytes() * 2 + wu_.bytes() +
-             ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() +
+             ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() + psi_init_dev_.bytes() +
              bundle_row_.bytes() + bundle_nrows_.bytes() + bundle_track_.bytes() + local_fsr_.bytes() +
              blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes();
     MOCGPU_CUDA(cudaDeviceSynchronize());

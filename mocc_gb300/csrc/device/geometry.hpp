@@ -39,6 +39,8 @@ class DeviceGeometry {
     // view with geometry pointers filled and cross-section pointers null
     GeomView view() const { return gv_; }
     const double *surf_area() const { return surf_area_.p; }
+    // initial incoming boundary flux of one group, in the sweep precision
+    const void *psi_init_device() const { return psi_init_dev_.p; }
     const double *dx() const { return dx_.p; }
     const double *dy() const { return dy_.p; }
     size_t bytes() const { return bytes_; }
@@ -56,6 +58,7 @@ class DeviceGeometry {
     DevBuf<SetPolar> sp_;
     DevBuf<int> ev_fw_begin_, ev_fw_pt_, ev_fw_code_, ev_bw_begin_, ev_bw_pt_, ev_bw_code_;
     DevBuf<int2> ev_fw_, ev_bw_, bundle_bc_;
+    DevBuf<unsigned char> psi_init_dev_;
     DevBuf<int> pin_first_reg_, pin_cell_, pin_fuel_;
     DevBuf<double> pin_area_, surf_area_, dx_, dy_;
     DevBuf<WorkUnitDev> wu_;

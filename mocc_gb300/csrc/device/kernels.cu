@@ -876,4 +876,36 @@ void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s)
     kb_summary<<<(b.cap + 127) / 128, 128, 0, s>>>(b, out);
 }
 
+// Fission-rate pin powers of every active solve (transport_sweeper.cpp:140-193):
+// row `slot` of out gets sum phi Sigma_f V per coarse cell and, in entry
+// n_pin, their total. One CTA per solve.
+__global__ void kb_pin_powers(BatchViews b, double *out, int stride)
+{
+    __shared__ double scratch[32];
+    if ((int)blockIdx.x >= *b.n_act) return;
+    const int slot = b.act[blockIdx.x];
+    const GeomView &g = b.gv[slot];
+    const StateView &st = b.sv[slot];
+    double *row = out + (size_t)slot * stride;
+    double tot = 0.0;
+    for (int ip = threadIdx.x; ip < g.n_pin; ip += blockDim.x) {
+        double p = 0.0;
+        for (int r = g.pin_first_reg[ip]; r < g.pin_first_reg[ip + 1]; r++) {
+            const double *xf = g.xsf + (size_t)g.fsr_mat[r] * g.G;
+            double fp = 0.0;
+            for (int ig = 0; ig < g.G; ig++) fp += st.phi[(size_t)ig * g.n_fsr + r] * xf[ig] * g.fsr_vol[r];
+            p += fp;
+        }
+        row[g.pin_cell[ip]] = p;
+        tot += p;
+    }
+    tot = block_sum(tot, scratch);
+    if (threadIdx.x == 0) row[g.n_pin] = tot;
+}
+void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s)
+{
+    note_launch();
+    kb_pin_powers<<<b.cap, 128, 0, s>>>(b, out, stride);
+}
+
 } // namespace mocgpu

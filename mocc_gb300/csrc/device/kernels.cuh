@@ -148,6 +148,8 @@ void launch_b_errors(const BatchViews &b, cudaStream_t s);   // error_k, error_p
 // out[slot * 6 + {0..5}] = k, error_k, error_psi, status, CMFD iterations, has_radial
 void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s);
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
+// pin powers of every active solve: out[slot * stride + cell], total at n_pin
+void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
 template <typename Real>
 void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
                     bool cur, int pol, int bundles_per_unit, int max_local, cudaStream_t s);

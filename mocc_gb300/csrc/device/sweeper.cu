@@ -157,7 +157,6 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     dev_bytes_ = state_bytes_for(f, precision_, bcpg);
     double nfis = n_fissile_;
     MOCGPU_CUDA(copy_async(red_.p + RED_N_FISSILE, &nfis, sizeof(double), cudaMemcpyHostToDevice, stream_));
-    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
 Sweeper::~Sweeper() = default;
@@ -180,11 +179,17 @@ void Sweeper::rebind(const Problem &P, const CrossSections *xs)
     }
     f_ = std::move(f);
     opts_ = P.opts;
-    xstr_.assign(f_.xstr);
-    xsnf_.assign(f_.xsnf);
-    xsf_.assign(f_.xsf);
-    xsch_.assign(f_.xsch);
-    scat_.assign(f_.scat);
+    // stream-ordered uploads into the existing buffers (the sizes match: same
+    // materials and groups); f_ keeps the host arrays alive
+    auto put = [&](DevBuf<double> &d, const std::vector<double> &h) {
+        if (h.size() != d.n) MOCGPU_THROW(1, "rebind: cross-section array size changed");
+        MOCGPU_CUDA(copy_async(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    };
+    put(xstr_, f_.xstr);
+    put(xsnf_, f_.xsnf);
+    put(xsf_, f_.xsf);
+    put(xsch_, f_.xsch);
+    put(scat_, f_.scat);
     gv_.xstr = xstr_.p;
     gv_.xsnf = xsnf_.p;
     gv_.xsf = xsf_.p;
@@ -231,18 +236,13 @@ void Sweeper::initialize()
     launch_fill(phi_.p, 1.0, (int64_t)G * f_.n_fsr, stream_);
     launch_fill(phi_old_.p, 1.0, (int64_t)G * f_.n_fsr, stream_);
     launch_fill(cflux_.p, 1.0, (int64_t)G * f_.n_pin, stream_);
-    const std::vector<double> &pi = geo_->psi_init;
-    const int bcpg = geo_->bc_per_group;
-    std::vector<double> init((size_t)G * bcpg);
-    for (int g = 0; g < G; g++) std::copy(pi.begin(), pi.end(), init.begin() + (size_t)g * bcpg);
-    if (precision_ == 0) {
-        MOCGPU_CUDA(copy_async(psi_in_.p, init.data(), init.size() * 8, cudaMemcpyHostToDevice, stream_));
-        MOCGPU_CUDA(cudaStreamSynchronize(stream_));
-    } else {
-        std::vector<float> fi(init.begin(), init.end());
-        MOCGPU_CUDA(copy_async(psi_in_.p, fi.data(), fi.size() * 4, cudaMemcpyHostToDevice, stream_));
-        MOCGPU_CUDA(cudaStreamSynchronize(stream_));
-    }
+    // incoming boundary flux of every group from the geometry's device copy
+    // (stream-ordered, no host round trip)
+    const size_t rb = precision_ == 0 ? sizeof(double) : sizeof(float);
+    const size_t gbytes = rb * (size_t)geo_->bc_per_group;
+    for (int g = 0; g < G; g++)
+        MOCGPU_CUDA(cudaMemcpyAsync(psi_in_.p + g * gbytes, geo_->psi_init_device(), gbytes, cudaMemcpyDeviceToDevice,
+                                    stream_));
     tally_.zero(stream_);
     cur_.zero(stream_);
     sflux_.zero(stream_);

@@ -78,23 +78,31 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
     while done < len(requests):
         admit_arrivals()
         busy = False
+        progressed = False
         for k, eng in engines.items():
             if in_flight[k]:
+                busy = True
+                if len(engines) > 1 and not eng.poll():
+                    continue  # another lane may be ready: do not block on this one
+                progressed = True
                 eng.finish()
                 in_flight[k] = False
-                for sid in list(outstanding[k]):
-                    r = eng.take(sid, max_pins)
-                    if r is None:
+                for sid in eng.ready():
+                    if sid not in outstanding[k]:
                         continue
+                    r = eng.take(sid, max_pins)
                     i = outstanding[k].pop(sid)
                     lat[i] = time.perf_counter() - t0 - requests[i].arrival
                     res[i] = r
                     done += 1
                 admit_arrivals()
-            if outstanding[k]:
+            if outstanding[k] and not in_flight[k]:
                 eng.launch()
                 in_flight[k] = True
                 busy = True
+                progressed = True
+        if busy and not progressed:
+            time.sleep(5e-5)  # every lane is on the GPU
         if not busy and nxt < len(order):
             wait = requests[order[nxt]].arrival - (time.perf_counter() - t0)
             if wait > 0:
