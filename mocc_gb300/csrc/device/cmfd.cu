@@ -15,6 +15,23 @@ namespace mocgpu {
 
 namespace {
 
+// Warp sum of two doubles with five FP64 adds per lane instead of ten: after
+// one exchange the even lanes carry a and the odd lanes b, then a butterfly
+// over the remaining bits sums each; every lane ends with both totals.
+__device__ __forceinline__ void warp_sum2(double &a, double &b)
+{
+    const unsigned full = 0xffffffffu;
+    const bool odd = threadIdx.x & 1;
+    double keep = odd ? b : a;
+    const double send = odd ? a : b;
+    keep += __shfl_xor_sync(full, send, 1);
+#pragma unroll
+    for (int o = 2; o < 32; o <<= 1) keep += __shfl_xor_sync(full, keep, o);
+    const double other = __shfl_xor_sync(full, keep, 1);
+    a = odd ? other : keep;
+    b = odd ? keep : other;
+}
+
 struct Blk {
     int nw; // warps in the CTA
     double *scratch;
@@ -24,11 +41,11 @@ struct Blk {
         if (nw == 1) __syncwarp();
         else __syncthreads();
     }
-    // Two block sums with a single barrier (double-buffered scratch).
+    // Two block sums with a single barrier (double-buffered scratch); the
+    // per-warp partials are combined pairwise so the adds form a tree.
     __device__ void sum2(double &a, double &b)
     {
-        a = warp_sum(a);
-        b = warp_sum(b);
+        warp_sum2(a, b);
         if (nw == 1) return;
         int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
         double *s = scratch + buf * 64;
@@ -37,20 +54,30 @@ struct Blk {
             s[32 + wid] = b;
         }
         __syncthreads();
-        double ta = 0.0, tb = 0.0;
-        for (int w = 0; w < nw; w++) {
-            ta += s[w];
-            tb += s[32 + w];
-        }
-        a = ta;
-        b = tb;
+        a = tree(s, nw);
+        b = tree(s + 32, nw);
         buf ^= 1;
     }
+    // One block sum (five FP64 adds per lane in the warp stage).
     __device__ double sum(double a)
     {
-        double b = 0.0;
-        sum2(a, b);
+        a = warp_sum(a);
+        if (nw == 1) return a;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        double *s = scratch + buf * 64;
+        if (lane == 0) s[wid] = a;
+        __syncthreads();
+        a = tree(s, nw);
+        buf ^= 1;
         return a;
+    }
+    // sum of v[0..n) as a pairwise tree (same order in every thread)
+    __device__ static double tree(const double *v, int n)
+    {
+        if (n == 4) return (v[0] + v[1]) + (v[2] + v[3]);
+        double t = 0.0;
+        for (int w = 0; w < n; w++) t += v[w];
+        return t;
     }
 };
 
@@ -207,13 +234,13 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
             y[i] = pi * m[5 * n + i];
         }
         B.sync();
-        double r0v = 0.0, dummy = 0.0;
+        double r0v = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const double vi = spmv_row(m, y, i, n, c.nx);
             v[i] = vi;
             r0v += r0[i] * vi;
         }
-        B.sum2(r0v, dummy);
+        r0v = B.sum(r0v);
         alpha = rho / r0v;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             double si = r[i] - alpha * v[i];
