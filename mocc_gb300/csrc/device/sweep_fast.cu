@@ -42,6 +42,23 @@ __device__ __forceinline__ float att_exp2(float ntau_l2)
     return 1.0f - e;
 }
 
+// FP32 -> FP64 by re-packing the IEEE-754 fields with integer operations
+// (sign, exponent rebiased from 127 to 1023, mantissa shifted by 29 bits), so
+// the crossing-current tally of the mixed path issues no FP64 instruction.
+// Zeros and subnormals become signed zero; infinities and NaNs keep their
+// class.
+__device__ __forceinline__ double widen(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned e = (u >> 23) & 0xFFu;
+    const unsigned long long man = (unsigned long long)(u & 0x7FFFFFu) << 29;
+    const unsigned long long ex = (e == 0u) ? 0ull : (e == 0xFFu) ? 0x7FFull : (unsigned long long)(e + 896u);
+    const unsigned long long bits = sign | (ex << 52) | (e == 0u ? 0ull : man);
+    return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
 // Attenuation 1 - e^{-tau0 / sin(theta)} of one polar angle; `rs` is the
 // per-polar factor prepared by polar_factor().
 __device__ __forceinline__ double atten(double tau0, double rs, const double *tab) { return att_fast(tau0 * rs, tab); }
@@ -186,8 +203,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                     jc += psi[p] * (ynorm ? cw[p][1] : cw[p][0]);
                     fc += psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
                 }
-                atomicAdd(cur + surf, fwd ? (double)jc : -(double)jc);
-                atomicAdd(sfl + surf, (double)fc);
+                atomicAdd(cur + surf, widen(fwd ? jc : -jc));
+                atomicAdd(sfl + surf, widen(fc));
                 ev++;
                 ev0 = ev1;
                 ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
