@@ -455,11 +455,11 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     }
 }
 
-__global__ void k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
+__global__ void __launch_bounds__(512) k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
 
 // One CTA per active solve of a batch; the coarse-current flag and the CMFD
 // iteration count live in each solve's scalar block.
-__global__ void kb_cmfd_solve(BatchViews b, int vec_in_smem)
+__global__ void __launch_bounds__(512) kb_cmfd_solve(BatchViews b, int vec_in_smem)
 {
     if ((int)blockIdx.x >= *b.n_act) return;
     const int slot = b.act[blockIdx.x];
@@ -537,7 +537,7 @@ namespace mocgpu {
 constexpr int kStaticCmfdMaxCells = 8192;
 static __device__ __align__(256) double g_cmfd_static_scratch[10 * kStaticCmfdMaxCells];
 
-__global__ void k_cmfd_solve_static(CmfdView c) { cmfd_body(c, 0); }
+__global__ void __launch_bounds__(512) k_cmfd_solve_static(CmfdView c) { cmfd_body(c, 0); }
 
 // Device address of the array, looked up once per device (with that device
 // current) on the first call that runs there.

@@ -76,7 +76,9 @@ template <> struct Pair<double> {
     using T = double2;
 };
 template <typename Real> struct Chunk {
-    static constexpr int rows = 8; // rows per streamed chunk
+    static constexpr int rows = 8;   // rows per streamed chunk
+    static constexpr int stages = 2; // chunks in flight per warp ring
+    static constexpr int tally_copies = 2; // shared tallies, lane l adds into copy l % tally_copies
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -90,19 +92,27 @@ template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile(
 // Bytes of one warp's ring buffer (two chunks of lengths and local FSR ids).
 template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
 {
-    return 2 * (size_t)Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
+    return (size_t)Chunk<Real>::stages * Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
 }
 
-// Adds each lane's contribution to the shared tally (a float add on shared
-// memory is a compare-and-swap loop; merging lanes that hit the same FSR
-// first, with shuffles, measured slower than letting those few collide).
-// Padding lanes carry a zero contribution and skip the add.
+// Adds each lane's contribution to the shared tally. A float add on shared
+// memory is a compare-and-swap loop, and neighbouring lanes of a bundle often
+// cross the same FSR in the same row; even and odd lanes therefore add into
+// two copies of the tally (summed when the unit ends), which halves those
+// collisions. Measured slower: merging colliding lanes with shuffles first,
+// match-any de-duplication, four or more copies (shared memory), per-warp
+// copies, global-memory float reductions. Padding lanes carry a zero
+// contribution and skip the add.
 template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int)
 {
     if (acc != (Real)0) atomicAdd(s_tal + l, acc);
 }
 
-template <typename Real, int NPOL, bool GS, bool CUR>
+// CUR: 0 no coarse tallies; 1 currents and surface fluxes; 2 currents only
+// (the batched eigen path: MOCC's surface fluxes only feed the partial-current
+// store of CMFD::store_currents, cmfd.cpp:555-666, whose consumer
+// update_incoming_flux is disabled at eigen_solver.cpp:289).
+template <typename Real, int NPOL, bool GS, int CUR>
 __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv, const StateView &st, int group,
                                            int wu, unsigned char *smem_raw)
 {
@@ -113,17 +123,21 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     const int nwarps = blockDim.x >> 5;
     // [warp rings][(sigma_t, qbar) pairs][tally]
     unsigned char *ring = smem_raw + (size_t)warp * ring_bytes<Real>();
-    Real *ring_len = reinterpret_cast<Real *>(ring);                                   // [2][CH][32]
-    uint16_t *ring_fsr = reinterpret_cast<uint16_t *>(ring + 2 * CH * 32 * sizeof(Real)); // [2][CH][32]
+    constexpr int ST = Chunk<Real>::stages;
+    Real *ring_len = reinterpret_cast<Real *>(ring);                                    // [ST][CH][32]
+    uint16_t *ring_fsr = reinterpret_cast<uint16_t *>(ring + ST * CH * 32 * sizeof(Real)); // [ST][CH][32]
     R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real>());
-    Real *s_tal = reinterpret_cast<Real *>(s_sq + fv.max_local);
+    constexpr int TC = Chunk<Real>::tally_copies;
+    Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // [TC][max_local]
+    Real *s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
 
     const Real *sigt = (const Real *)st.sigt;
     const Real *qbar = (const Real *)st.qbar;
     for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
         int gl = fv.local_fsr[u.fsr_begin + i];
         s_sq[i] = R2{sigt[gl], qbar[gl]};
-        s_tal[i] = (Real)0;
+#pragma unroll
+        for (int c = 0; c < TC; c++) s_tal0[(size_t)c * fv.max_local + i] = (Real)0;
     }
     __syncthreads();
 
@@ -201,10 +215,10 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
 #pragma unroll
                 for (int p = 0; p < NPOL; p++) {
                     jc += psi[p] * (ynorm ? cw[p][1] : cw[p][0]);
-                    fc += psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
+                    if (CUR == 1) fc += psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
                 }
                 atomicAdd(cur + surf, widen(fwd ? jc : -jc));
-                atomicAdd(sfl + surf, widen(fc));
+                if (CUR == 1) atomicAdd(sfl + surf, widen(fc));
                 ev++;
                 ev0 = ev1;
                 ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
@@ -224,7 +238,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             int lo, hi;
             chunk_rows(c, lo, hi);
             const int nr = hi - lo;
-            const int buf = c & 1;
+            const int buf = c % ST;
             const char *gl = (const char *)(lenp + (row0 + lo) * 32);
             char *sl = (char *)(ring_len + (size_t)buf * CH * 32);
             const int nl = nr * 32 * (int)sizeof(Real) / 16;
@@ -236,19 +250,22 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             cp_async_commit();
         };
 
-        if (nch > 0) issue(0);
+        // ST-1 chunks ahead: one commit group per chunk (empty groups past
+        // the end keep the count uniform), so waiting until at most ST-1
+        // groups are pending means chunk c has landed
+        for (int c = 0; c < ST - 1; c++) {
+            if (c < nch) issue(c);
+            else cp_async_commit();
+        }
         for (int c = 0; c < nch; c++) {
-            if (c + 1 < nch) {
-                issue(c + 1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
+            if (c + ST - 1 < nch) issue(c + ST - 1);
+            else cp_async_commit();
+            cp_async_wait<ST - 1>();
             __syncwarp();
             int lo, hi;
             chunk_rows(c, lo, hi);
-            const Real *cl = ring_len + (size_t)(c & 1) * CH * 32;
-            const uint16_t *cf = ring_fsr + (size_t)(c & 1) * CH * 32;
+            const Real *cl = ring_len + (size_t)(c % ST) * CH * 32;
+            const uint16_t *cf = ring_fsr + (size_t)(c % ST) * CH * 32;
             const int nr = hi - lo;
             // Four rows per step: the loads, gathers and attenuations of the
             // four rows are independent and issue back to back; only the psi
@@ -324,14 +341,16 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     __syncthreads();
     Real *tally = (Real *)st.tally;
     for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
-        Real v = s_tal[i];
+        Real v = s_tal0[i];
+#pragma unroll
+        for (int c = 1; c < TC; c++) v += s_tal0[(size_t)c * fv.max_local + i];
         if (v != (Real)0) atomicAdd(tally + fv.local_fsr[u.fsr_begin + i], v);
     }
 }
 
 void note_launch_external();
 
-template <typename Real, int NPOL, bool GS, bool CUR>
+template <typename Real, int NPOL, bool GS, int CUR>
 __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, int wu0)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -340,7 +359,7 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
 
 // Persistent batched sweep: a fixed grid walks the (solve slot, work unit)
 // list of every active solve, largest units first.
-template <typename Real, int NPOL, bool GS, bool CUR>
+template <typename Real, int NPOL, bool GS, int CUR>
 __global__ void kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -354,10 +373,11 @@ __global__ void kb_sweep_fast(BatchViews b, const int2 *items, const int *n_item
 
 template <typename Real> static size_t batched_smem(int bundles_per_unit, int max_local)
 {
-    return (size_t)(2 * bundles_per_unit) * ring_bytes<Real>() + (size_t)max_local * (3 * sizeof(Real));
+    return (size_t)(2 * bundles_per_unit) * ring_bytes<Real>() +
+           (size_t)max_local * ((2 + Chunk<Real>::tally_copies) * sizeof(Real));
 }
 
-template <typename Real, int NPOL, bool GS, bool CUR> static void prepare_batched(size_t smem)
+template <typename Real, int NPOL, bool GS, int CUR> static void prepare_batched(size_t smem)
 {
     auto k = kb_sweep_fast<Real, NPOL, GS, CUR>;
     static size_t configured = 0;
@@ -367,7 +387,7 @@ template <typename Real, int NPOL, bool GS, bool CUR> static void prepare_batche
     }
 }
 
-template <typename Real, int NPOL, bool GS, bool CUR>
+template <typename Real, int NPOL, bool GS, int CUR>
 static void launch_batched(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group,
                            int bundles_per_unit, int max_local, cudaStream_t s)
 {
@@ -387,7 +407,7 @@ static void launch_batched(const BatchViews &b, const int2 *items, const int *n_
 template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local)
 {
     const size_t smem = batched_smem<Real>(bundles_per_unit, max_local);
-#define MOCGPU_P(NP)                                                                                                     if (pol == NP) {                                                                                                         prepare_batched<Real, NP, true, false>(smem);                                                                        prepare_batched<Real, NP, true, true>(smem);                                                                         prepare_batched<Real, NP, false, false>(smem);                                                                       prepare_batched<Real, NP, false, true>(smem);                                                                        return;                                                                                                          }
+#define MOCGPU_P(NP)                                                                                                     if (pol == NP) {                                                                                                         prepare_batched<Real, NP, true, 0>(smem);                                                                        prepare_batched<Real, NP, true, 2>(smem);                                                                         prepare_batched<Real, NP, false, 0>(smem);                                                                       prepare_batched<Real, NP, false, 2>(smem);                                                                        return;                                                                                                          }
     MOCGPU_P(1)
     MOCGPU_P(2)
     MOCGPU_P(3)
@@ -406,13 +426,13 @@ void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, 
     note_launch_external();
 #define MOCGPU_B(NP)                                                                                                 \
     if (pol == NP) {                                                                                                 \
-        if (gs && !cur) launch_batched<Real, NP, true, false>(b, items, n_items, max_items, group, bundles_per_unit,  \
+        if (gs && !cur) launch_batched<Real, NP, true, 0>(b, items, n_items, max_items, group, bundles_per_unit,  \
                                                               max_local, s);                                         \
-        else if (gs && cur) launch_batched<Real, NP, true, true>(b, items, n_items, max_items, group,               \
+        else if (gs && cur) launch_batched<Real, NP, true, 2>(b, items, n_items, max_items, group,               \
                                                                  bundles_per_unit, max_local, s);                     \
-        else if (!gs && !cur) launch_batched<Real, NP, false, false>(b, items, n_items, max_items, group,           \
+        else if (!gs && !cur) launch_batched<Real, NP, false, 0>(b, items, n_items, max_items, group,           \
                                                                      bundles_per_unit, max_local, s);                 \
-        else launch_batched<Real, NP, false, true>(b, items, n_items, max_items, group, bundles_per_unit, max_local,  \
+        else launch_batched<Real, NP, false, 2>(b, items, n_items, max_items, group, bundles_per_unit, max_local,  \
                                                    s);                                                               \
         return;                                                                                                      \
     }
@@ -431,12 +451,12 @@ template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int
 template <typename Real> size_t fast_sweep_smem(const FastView &fv)
 {
     int nwarps = 2 * fv.bundles_per_unit;
-    return (size_t)nwarps * ring_bytes<Real>() + (size_t)fv.max_local * (3 * sizeof(Real));
+    return (size_t)nwarps * ring_bytes<Real>() + (size_t)fv.max_local * ((2 + Chunk<Real>::tally_copies) * sizeof(Real));
 }
 template size_t fast_sweep_smem<float>(const FastView &);
 template size_t fast_sweep_smem<double>(const FastView &);
 
-template <typename Real, int NPOL, bool GS, bool CUR>
+template <typename Real, int NPOL, bool GS, int CUR>
 static void launch_one(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,
                        cudaStream_t s)
 {
@@ -455,10 +475,10 @@ template <typename Real, int NPOL>
 static void launch_np(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1, bool gs,
                       bool cur, cudaStream_t s)
 {
-    if (gs && !cur) launch_one<Real, NPOL, true, false>(g, fv, st, group, wu0, wu1, s);
-    else if (gs && cur) launch_one<Real, NPOL, true, true>(g, fv, st, group, wu0, wu1, s);
-    else if (!gs && !cur) launch_one<Real, NPOL, false, false>(g, fv, st, group, wu0, wu1, s);
-    else launch_one<Real, NPOL, false, true>(g, fv, st, group, wu0, wu1, s);
+    if (gs && !cur) launch_one<Real, NPOL, true, 0>(g, fv, st, group, wu0, wu1, s);
+    else if (gs && cur) launch_one<Real, NPOL, true, 1>(g, fv, st, group, wu0, wu1, s);
+    else if (!gs && !cur) launch_one<Real, NPOL, false, 0>(g, fv, st, group, wu0, wu1, s);
+    else launch_one<Real, NPOL, false, 1>(g, fv, st, group, wu0, wu1, s);
 }
 
 template <typename Real>
