@@ -204,12 +204,15 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     // --- bundled work-unit layout (two Gauss-Seidel phases) -----------------
     {
         int tracks_phase = f.set_first_track[sets_oct];
-        // up to 4 bundles (8 warps) per unit; unit FSR sets sized so the
-        // staged pairs, the tally and the warps' segment rings fit in 227 KB
-        int tpu = 32 * std::max(1, std::min(4, tracks_phase / (2 * 152 * 32)));
+        // 1-2 bundles per unit when chosen automatically (measured best on
+        // the 68x68 mini-core; the batch engine passes its own); unit FSR
+        // sets sized so the staged pairs, the tallies and the warps' segment
+        // rings fit in 227 KB; bundles dealt round-robin from the
+        // length-sorted tracks
+        int tpu = 32 * std::max(1, std::min(2, tracks_phase / (2 * 152 * 32)));
         if (bundles_per_unit > 0) tpu = 32 * std::min(bundles_per_unit, 4);
         int max_local = (precision == 0) ? 4096 : 8192;
-        SweepLayout L = build_sweep_layout(f, true, tpu, max_local);
+        SweepLayout L = build_sweep_layout(f, true, tpu, max_local, true);
         std::vector<WorkUnitDev> wud(L.wu.size());
         for (size_t i = 0; i < L.wu.size(); i++)
             wud[i] = WorkUnitDev{L.wu[i].set, L.wu[i].bundle_begin, L.wu[i].n_bundles, L.wu[i].fsr_begin,

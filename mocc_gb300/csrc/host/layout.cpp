@@ -6,7 +6,7 @@
 
 namespace mocgpu {
 
-SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local)
+SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local, bool interleave)
 {
     SweepLayout L;
     const int W = SweepLayout::kLanes;
@@ -65,22 +65,28 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                 std::stable_sort(tracks.begin(), tracks.end(), [&](int a, int b) {
                     return (f.trk_seg_begin[a + 1] - f.trk_seg_begin[a]) > (f.trk_seg_begin[b + 1] - f.trk_seg_begin[b]);
                 });
-                for (size_t b0 = 0; b0 < tracks.size(); b0 += W) {
+                // bundles: the length-sorted tracks dealt round-robin, so the
+                // lanes of a bundle have similar lengths (little padding) but
+                // are not spatial neighbours, which cross the same FSR in the
+                // same row and contend for its tally
+                const size_t nb = (tracks.size() + W - 1) / W;
+                std::vector<std::vector<int>> groups(nb);
+                for (size_t j = 0; j < tracks.size(); j++)
+                    groups[interleave ? j % nb : j / W].push_back(tracks[j]);
+                for (const std::vector<int> &grp : groups) {
                     int nrows = 0;
-                    for (size_t j = b0; j < std::min(tracks.size(), b0 + W); j++)
-                        nrows = std::max<int>(nrows, (int)(f.trk_seg_begin[tracks[j] + 1] - f.trk_seg_begin[tracks[j]]));
+                    for (int tr : grp) nrows = std::max<int>(nrows, (int)(f.trk_seg_begin[tr + 1] - f.trk_seg_begin[tr]));
                     L.bundle_row.push_back(L.n_rows);
                     L.bundle_nrows.push_back(nrows);
                     size_t base = L.len.size();
                     L.len.resize(base + (size_t)nrows * W, 0.0);
                     L.lfsr.resize(base + (size_t)nrows * W, 0);
                     for (int lane = 0; lane < W; lane++) {
-                        size_t j = b0 + lane;
-                        if (j >= tracks.size()) {
+                        if (lane >= (int)grp.size()) {
                             L.bundle_track.push_back(-1);
                             continue;
                         }
-                        int tr = tracks[j];
+                        int tr = grp[lane];
                         L.bundle_track.push_back(tr);
                         int64_t a = f.trk_seg_begin[tr];
                         int n = (int)(f.trk_seg_begin[tr + 1] - a);

@@ -45,6 +45,7 @@ struct SweepLayout {
 // gs: two phases (octant-1 sets, then octant-2 sets); otherwise one phase.
 // tracks_per_unit: target tracks per unit (a multiple of 32); max_local: cap
 // on FSRs per unit.
-SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local);
+SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local,
+                               bool interleave = false);
 
 } // namespace mocgpu
