@@ -249,6 +249,9 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         fv.bundles_per_unit = tpu / 32;
         fv.split = 1;
         fv.max_local = L.max_local;
+        fv.max_hits = L.max_hits;
+        if (precision != 0 && L.max_hits > kMaxTallyHits)
+            MOCGPU_THROW(6, "a work unit adds more often to one FSR tally than the fixed-point tally allows");
         layout_padding = L.padding;
         layout_units = (int)L.wu.size();
         layout_max_local = L.max_local;

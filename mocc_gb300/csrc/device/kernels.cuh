@@ -18,6 +18,10 @@ namespace mocgpu {
 
 constexpr int kExpN = 10000;       // table intervals on [-10, 0]
 constexpr int kMaxPolar = 4;
+// Cap on the adds one FSR tally of a work unit takes in a group sweep: the
+// low words of the FP32 path's fixed-point tally take up to 2^20 per add and
+// must not wrap (2048 * 2^20 = 2^31).
+constexpr int kMaxTallyHits = 2048;
 
 struct SetPolar {
     int ang_fwd, ang_bwd; // angle indices (octants 1-4) swept forward/backward
@@ -97,6 +101,7 @@ struct FastView {
     int bundles_per_unit; // warps per CTA = bundles_per_unit * (split ? 2 : 1)
     int split;            // forward and backward on separate warps
     int max_local;
+    int max_hits; // most tally adds on one unit FSR in one group sweep (bounds the fixed-point tally)
 };
 
 // Per-solve scalars kept in device memory (StateView::red) so that batched

@@ -3,7 +3,8 @@
 //
 // One CTA per work unit. The unit's FSR cross sections and sources are staged
 // into shared memory as (Sigma_t, qbar) pairs and the unit's FSR tally lives
-// in shared memory; one warp sweeps one bundle of 32 tracks in one direction,
+// in shared memory (fixed point in the FP32 path, see tally_fixed); one warp
+// sweeps one bundle of 32 tracks in one direction,
 // one track per lane, all polar angles of the azimuth in registers (the
 // forward and the backward pass of a bundle run on two warps). Each warp
 // streams its bundle's segment rows through a double-buffered shared-memory
@@ -78,7 +79,8 @@ template <> struct Pair<double> {
 template <typename Real> struct Chunk {
     static constexpr int rows = 8;   // rows per streamed chunk
     static constexpr int stages = 2; // chunks in flight per warp ring
-    static constexpr int tally_copies = 2; // shared tallies, lane l adds into copy l % tally_copies
+    static constexpr int tally_copies = 2; // FP64 shared tallies, lane l adds into copy l % tally_copies
+    static constexpr bool fixed = sizeof(Real) == 4; // FP32: two-word fixed-point tally (same bytes)
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
@@ -95,17 +97,53 @@ template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
     return (size_t)Chunk<Real>::stages * Chunk<Real>::rows * (32 * sizeof(Real) + 32 * sizeof(uint16_t));
 }
 
-// Adds each lane's contribution to the shared tally. A float add on shared
-// memory is a compare-and-swap loop, and neighbouring lanes of a bundle often
-// cross the same FSR in the same row; even and odd lanes therefore add into
-// two copies of the tally (summed when the unit ends), which halves those
-// collisions. Measured slower: merging colliding lanes with shuffles first,
-// match-any de-duplication, four or more copies (shared memory), per-warp
-// copies, global-memory float reductions. Padding lanes carry a zero
+// FP64 path: adds each lane's contribution to the shared tally. A float add
+// on shared memory is a compare-and-swap loop, and lanes of a bundle may cross
+// the same FSR in the same row; even and odd lanes therefore add into two
+// copies of the tally (summed when the unit ends). Padding lanes carry a zero
 // contribution and skip the add.
 template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int)
 {
     if (acc != (Real)0) atomicAdd(s_tal + l, acc);
+}
+
+// FP32 path: the unit's tally is fixed point, two 32-bit words per FSR (a
+// signed high word counting 2^20 and an unsigned low word), added with
+// shared-memory integer atomics. Those are single native operations (a float
+// add on shared memory is a compare-and-swap loop that retries and serialises
+// the lanes of a warp crossing the same FSR in the same row), they commute,
+// and nothing waits on them. A contribution x, multiplied by the unit's
+// power-of-two scale, is split exactly as x = hi * 2^20 + lo with
+// hi = floor(x / 2^20) and 0 <= lo <= 2^20 (lo rounded to an integer; its
+// error is half a unit, 2^-51 of the unit's bound below). The scale makes
+// |x| < 2^50 / max_hits, so at most max_hits adds keep the high word within
+// 2^30 + max_hits and the low word within max_hits * 2^20 <= 2^31.
+// Measured slower than the compare-and-swap tally: merging colliding lanes
+// with shuffles first, match-any de-duplication, per-warp copies, global
+// float reductions.
+__device__ __forceinline__ void tally_fixed(int2 *s_fix, int l, float acc, float scale)
+{
+    if (acc != 0.f) {
+        const float xs = acc * scale;
+        const float hf = floorf(xs * 0x1p-20f);
+        atomicAdd(&s_fix[l].x, (int)hf);
+        atomicAdd(reinterpret_cast<unsigned *>(&s_fix[l].y), (unsigned)__float2int_rn(fmaf(hf, -0x1p20f, xs)));
+    }
+}
+
+// Power-of-two scale of the fixed-point tally of a unit, and its inverse:
+// 2^(50 - E) with bound < 2^E, bound = hits * 2 * m * sum_p |w_p| and m the
+// largest |qbar| or incoming |psi| of the unit. psi stays between its
+// incoming value and the qbar of the FSRs it crosses (each segment moves it
+// toward qbar by the fraction 1 - e^-tau), so every contribution
+// sum_p (psi_p - qbar) (1 - e^-tau_p) w_p is at most 2 m sum_p |w_p|.
+__device__ __forceinline__ void fixed_scale(float m, float sum_w, int hits, float &scale, float &inv)
+{
+    const float bound = 2.f * m * sum_w * (float)hits;
+    const int E = (int)((__float_as_uint(bound) >> 23) & 0xFFu) - 126; // bound < 2^E (normal bound)
+    const int se = max(-126, min(127, 50 - E));
+    scale = __uint_as_float((unsigned)(se + 127) << 23);
+    inv = __uint_as_float((unsigned)(127 - se) << 23);
 }
 
 // CUR: 0 no coarse tallies; 1 currents and surface fluxes; 2 currents only
@@ -128,18 +166,10 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     uint16_t *ring_fsr = reinterpret_cast<uint16_t *>(ring + ST * CH * 32 * sizeof(Real)); // [ST][CH][32]
     R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real>());
     constexpr int TC = Chunk<Real>::tally_copies;
-    Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // [TC][max_local]
+    constexpr bool FIXED = Chunk<Real>::fixed;
+    Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // FP64: [TC][max_local]
     Real *s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
-
-    const Real *sigt = (const Real *)st.sigt;
-    const Real *qbar = (const Real *)st.qbar;
-    for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
-        int gl = fv.local_fsr[u.fsr_begin + i];
-        s_sq[i] = R2{sigt[gl], qbar[gl]};
-#pragma unroll
-        for (int c = 0; c < TC; c++) s_tal0[(size_t)c * fv.max_local + i] = (Real)0;
-    }
-    __syncthreads();
+    int2 *s_fix = reinterpret_cast<int2 *>(s_sq + fv.max_local);  // FP32: [max_local] (hi, lo)
 
     const int ntasks = 2 * u.n_bundles;
     const Real *lenp = (const Real *)fv.len;
@@ -150,6 +180,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     // per unit: boundary-flux offsets of every (direction, polar) angle and
     // the reflected angles' incoming offsets for the Gauss-Seidel write-through
     __shared__ int s_off[2][kMaxPolar], s_tgt[2][kMaxPolar][2];
+    __shared__ unsigned s_mbits; // largest |qbar| or incoming |psi| of the unit (float bits)
     if (threadIdx.x < 2 * NPOL) {
         const int dir = threadIdx.x / NPOL, p = threadIdx.x % NPOL;
         const SetPolar sp = g.sp[u.set * NPOL + p];
@@ -159,6 +190,39 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             s_tgt[dir][p][0] = g.wt_tgt[a * 2];
             s_tgt[dir][p][1] = g.wt_tgt[a * 2 + 1];
         }
+    }
+    if (FIXED && threadIdx.x == 0) s_mbits = 0u;
+    __syncthreads();
+
+    const Real *sigt = (const Real *)st.sigt;
+    const Real *qbar = (const Real *)st.qbar;
+    unsigned mbits = 0u; // float bits of a non-negative value order like the integers
+    for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
+        int gl = fv.local_fsr[u.fsr_begin + i];
+        const Real q = qbar[gl];
+        s_sq[i] = R2{sigt[gl], q};
+        if constexpr (FIXED) {
+            mbits = max(mbits, __float_as_uint(fabsf((float)q)));
+            s_fix[i] = make_int2(0, 0);
+        } else {
+#pragma unroll
+            for (int c = 0; c < TC; c++) s_tal0[(size_t)c * fv.max_local + i] = (Real)0;
+        }
+    }
+    if constexpr (FIXED) {
+        // incoming angular fluxes of every lane, direction and polar angle
+        for (int i = threadIdx.x; i < u.n_bundles * 64; i += blockDim.x) {
+            const size_t bl = (size_t)(u.bundle_begin + (i >> 6)) * 32 + (i & 31);
+            const int dir = (i >> 5) & 1;
+            if (fv.bundle_track[bl] < 0) continue;
+            const int2 bc = fv.bundle_bc[bl];
+            const int bc_in = dir == 0 ? bc.x : bc.y;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++)
+                mbits = max(mbits, __float_as_uint(fabsf((float)psi_in[s_off[dir][p] + bc_in])));
+        }
+        mbits = __reduce_max_sync(0xffffffffu, mbits);
+        if (lane == 0 && mbits) atomicMax(&s_mbits, mbits);
     }
     __syncthreads();
 
@@ -178,6 +242,15 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     }
     double *cur = st.cur + (size_t)group * g.n_surf;
     double *sfl = st.sflux + (size_t)group * g.n_surf;
+    float scale = 1.f, inv_scale = 1.f;
+    if constexpr (FIXED) {
+        float sum_w = 0.f;
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) sum_w += fabsf((float)wt[p]);
+        const unsigned mb = s_mbits;
+        if (mb >= 0x7F800000u && threadIdx.x == 0) atomicOr(st.status, (unsigned)DEV_NAN); // inf or NaN
+        fixed_scale(__uint_as_float(mb), sum_w, fv.max_hits, scale, inv_scale);
+    }
 
     for (int task = warp; task < ntasks; task += nwarps) {
         const int b = u.bundle_begin + (task >> 1);
@@ -303,7 +376,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                         psi[p] -= d;
                         acc += d * wt[p];
                     }
-                    tally_add(s_tal, l[v], acc, lane);
+                    if constexpr (FIXED) tally_fixed(s_fix, l[v], (float)acc, scale);
+                    else tally_add(s_tal, l[v], acc, lane);
                 }
             }
             for (; k < nr; k++) {
@@ -321,7 +395,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
                     psi[p] -= d;
                     acc += d * wt[p];
                 }
-                tally_add(s_tal, l, acc, lane);
+                if constexpr (FIXED) tally_fixed(s_fix, l, (float)acc, scale);
+                else tally_add(s_tal, l, acc, lane);
             }
             __syncwarp();
         }
@@ -341,9 +416,16 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     __syncthreads();
     Real *tally = (Real *)st.tally;
     for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
-        Real v = s_tal0[i];
+        Real v;
+        if constexpr (FIXED) {
+            const int2 w = s_fix[i];
+            const long long x = (long long)w.x * (1ll << 20) + (long long)(unsigned)w.y;
+            v = (Real)(__ll2float_rn(x) * inv_scale);
+        } else {
+            v = s_tal0[i];
 #pragma unroll
-        for (int c = 1; c < TC; c++) v += s_tal0[(size_t)c * fv.max_local + i];
+            for (int c = 1; c < TC; c++) v += s_tal0[(size_t)c * fv.max_local + i];
+        }
         if (v != (Real)0) atomicAdd(tally + fv.local_fsr[u.fsr_begin + i], v);
     }
 }

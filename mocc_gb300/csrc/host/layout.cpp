@@ -69,6 +69,13 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                 // lanes of a bundle have similar lengths (little padding) but
                 // are not spatial neighbours, which cross the same FSR in the
                 // same row and contend for its tally
+                {
+                    std::vector<int> hits(fsrs.size(), 0);
+                    for (int tr : tracks)
+                        for (int64_t k = f.trk_seg_begin[tr]; k < f.trk_seg_begin[tr + 1]; k++)
+                            hits[loc[f.seg_fsr[k]]] += 2; // swept forward and backward
+                    for (int h : hits) L.max_hits = std::max(L.max_hits, h);
+                }
                 const size_t nb = (tracks.size() + W - 1) / W;
                 std::vector<std::vector<int>> groups(nb);
                 for (size_t j = 0; j < tracks.size(); j++)
