@@ -180,8 +180,9 @@ int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep
 /* ---- layout inspection (no MOCC counterpart) ---------------------------
  * Builds the bundled work-unit layout of the GPU sweep on the host and
  * reports: [0] units, [1] bundles, [2] rows, [3] real segment entries,
- * [4] largest unit FSR set, [5] phases; stats_d: [0] sum of real segment
- * lengths, [1] padding fraction. */
+ * [4] FSR slots of the largest unit (its FSRs + 1 padding slot),
+ * [5] phases; stats_d: [0] sum of real segment lengths, [1] padding
+ * fraction. */
 int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int64_t *stats,
                         double *stats_d);
 

@@ -506,32 +506,32 @@ int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, in
         mocgpu::SweepLayout L = mocgpu::build_sweep_layout(p->P->flat, gs != 0, tracks_per_unit, max_local);
         int64_t real = 0;
         double sum = 0.0;
-        for (size_t b = 0; b < L.bundle_row.size(); b++)
+        std::vector<int> unit_of(L.bundle_row.size(), -1);
+        for (size_t u = 0; u < L.wu.size(); u++)
+            for (int b = L.wu[u].bundle_begin; b < L.wu[u].bundle_begin + L.wu[u].n_bundles; b++) unit_of[b] = (int)u;
+        const auto &f = p->P->flat;
+        for (size_t b = 0; b < L.bundle_row.size(); b++) {
+            const int wu = unit_of[b];
+            if (wu < 0) throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "bundle outside every work unit");
             for (int lane = 0; lane < 32; lane++) {
                 int t = L.bundle_track[b * 32 + lane];
-                if (t < 0) continue;
-                const auto &f = p->P->flat;
-                int n = (int)(f.trk_seg_begin[t + 1] - f.trk_seg_begin[t]);
+                int n = t < 0 ? 0 : (int)(f.trk_seg_begin[t + 1] - f.trk_seg_begin[t]);
                 for (int r = 0; r < L.bundle_nrows[b]; r++) {
                     size_t i = (size_t)(L.bundle_row[b] + r) * 32 + lane;
                     if (r < n) {
                         real++;
                         sum += L.len[i];
                         // the unit-local index must map back to the segment's FSR
-                        int wu = -1;
-                        for (size_t u = 0; u < L.wu.size(); u++)
-                            if ((int)b >= L.wu[u].bundle_begin && (int)b < L.wu[u].bundle_begin + L.wu[u].n_bundles) {
-                                wu = (int)u;
-                                break;
-                            }
-                        if (wu < 0 || L.local_fsr[L.wu[wu].fsr_begin + L.lfsr[i]] != f.seg_fsr[f.trk_seg_begin[t] + r] ||
+                        if (L.lfsr[i] >= L.wu[wu].n_local ||
+                            L.local_fsr[L.wu[wu].fsr_begin + L.lfsr[i]] != f.seg_fsr[f.trk_seg_begin[t] + r] ||
                             L.len[i] != f.seg_len[f.trk_seg_begin[t] + r])
                             throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "layout maps a segment to the wrong FSR or length");
-                    } else if (L.len[i] != 0.0) {
-                        throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "non-zero padding segment");
+                    } else if (L.len[i] != 0.0 || L.lfsr[i] != L.wu[wu].n_local) {
+                        throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "padding entry not zero-length or not on the padding slot");
                     }
                 }
             }
+        }
         stats[0] = (int64_t)L.wu.size();
         stats[1] = (int64_t)L.bundle_row.size();
         stats[2] = L.n_rows;

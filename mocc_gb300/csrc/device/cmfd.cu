@@ -147,22 +147,23 @@ __device__ double thickness(const CmfdView &c, int cell, int nrm)
 }
 __device__ __forceinline__ double cell_vol(const CmfdView &c, int i) { return c.dx[i % c.nx] * c.dy[i / c.nx] * c.hz; }
 
-// Row i of the 5-point operator applied to x.
+// The operator of each group is kept column-scaled by the Jacobi
+// preconditioner: m[0..n) holds the diagonal d (1 where it vanishes), m[5n..6n)
+// its inverse, and m[n..5n) the off-diagonal entries A_ij / d_j of the west,
+// east, south and north neighbours. Right-preconditioned BiCGSTAB applies
+// A D^-1 to its search vectors, which is this operator with a unit diagonal:
+// four FP64 multiply-adds per row and no separate preconditioner product.
+
+// Row i of A D^-1 applied to x (unit diagonal).
 __device__ __forceinline__ double spmv_row(const double *__restrict__ m, const double *x, int i, int n, int nx)
 {
-    double v = m[i] * x[i];
+    double v = x[i];
     int ix = i % nx;
     if (ix > 0) v += m[n + i] * x[i - 1];
     if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
     if (i >= nx) v += m[3 * n + i] * x[i - nx];
     if (i + nx < n) v += m[4 * n + i] * x[i + nx];
     return v;
-}
-
-__device__ void spmv(const CmfdView &c, const double *__restrict__ m, const double *x, double *y)
-{
-    const int n = c.n_cell, nx = c.nx;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) y[i] = spmv_row(m, x, i, n, nx);
 }
 
 // b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
@@ -179,20 +180,25 @@ __device__ void build_source(const CmfdView &c, int g, double *b)
 }
 
 // Preconditioned BiCGSTAB (van der Vorst 1992) with a diagonal (Jacobi)
-// preconditioner, stopping on ||r||^2 <= tol^2 ||b||^2 or max_it
-// iterations, restarting the shadow residual when it becomes orthogonal.
-// x is in/out; w holds 8 work vectors.
+// preconditioner applied from the right, as Eigen's BiCGSTAB with its
+// DiagonalPreconditioner (the solver of cmfd.cpp), stopping on the true
+// residual, ||r||^2 <= tol^2 ||b||^2, or after max_it iterations, and
+// restarting the shadow residual when it becomes orthogonal. The iteration
+// runs on xh = D x with the column-scaled operator (xh += alpha p + omega s
+// is x += alpha D^-1 p + omega D^-1 s), which gives the same iterates as
+// applying D^-1 to p and s. x is in/out; w holds 8 work vectors; rr0 returns
+// ||b - A x||^2 of the incoming x.
 __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double *b, double *x, double tol, int max_it,
-                        double *w)
+                        double *w, double &rr0)
 {
-    const int n = c.n_cell;
-    double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *y = w + 4 * n, *z = w + 5 * n, *s = w + 6 * n,
-           *t = w + 7 * n;
+    const int n = c.n_cell, nx = c.nx;
+    double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *s = w + 6 * n, *t = w + 7 * n;
     const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
-    spmv(c, m, x, r);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= m[i];
+    B.sync();
     double rr = 0.0, bb = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double ri = b[i] - r[i];
+        double ri = b[i] - spmv_row(m, x, i, n, nx);
         r[i] = ri;
         r0[i] = ri;
         p[i] = 0.0;
@@ -201,6 +207,7 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         bb += b[i] * b[i];
     }
     B.sum2(rr, bb);
+    rr0 = rr;
     if (bb == 0.0) {
         for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = 0.0;
         B.sync();
@@ -215,10 +222,9 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         rho = rho_new;
         if (fabs(rho) < eps2 * r0_sq) {
             B.sync();
-            spmv(c, m, x, r);
             double acc = 0.0;
             for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double ri = b[i] - r[i];
+                double ri = b[i] - spmv_row(m, x, i, n, nx);
                 r[i] = ri;
                 r0[i] = ri;
                 acc += ri * ri;
@@ -228,29 +234,21 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
             if (restarts++ == 0) it = 0;
         }
         const double beta = (rho / rho_old) * (alpha / om);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double pi = r[i] + beta * (p[i] - om * v[i]);
-            p[i] = pi;
-            y[i] = pi * m[5 * n + i];
-        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = r[i] + beta * (p[i] - om * v[i]);
         B.sync();
         double r0v = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double vi = spmv_row(m, y, i, n, c.nx);
+            const double vi = spmv_row(m, p, i, n, nx);
             v[i] = vi;
             r0v += r0[i] * vi;
         }
         r0v = B.sum(r0v);
         alpha = rho / r0v;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            double si = r[i] - alpha * v[i];
-            s[i] = si;
-            z[i] = si * m[5 * n + i];
-        }
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = r[i] - alpha * v[i];
         B.sync();
         double tt = 0.0, ts = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double ti = spmv_row(m, z, i, n, c.nx);
+            const double ti = spmv_row(m, s, i, n, nx);
             t[i] = ti;
             tt += ti * ti;
             ts += ti * s[i];
@@ -259,7 +257,7 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         om = (tt > 0.0) ? ts / tt : 0.0;
         double nrr = 0.0, nrho = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            x[i] += alpha * y[i] + om * z[i];
+            x[i] += alpha * p[i] + om * s[i];
             double ri = s[i] - om * t[i];
             r[i] = ri;
             nrr += ri * ri;
@@ -270,6 +268,8 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
         rho_new = nrho;
         it++;
     }
+    B.sync();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= m[5 * n + i];
     B.sync();
     return it;
 }
@@ -293,7 +293,7 @@ __device__ double total_fission(const CmfdView &c, Blk &B)
     return B.sum(f);
 }
 
-// ||M_g x - b_g||^2 with x the group flux
+// ||M_g x - b_g||^2 with x the group flux (A_ij = m_ij d_j off the diagonal)
 __device__ double residual_g(const CmfdView &c, Blk &B, const double *m, const double *x, const double *b)
 {
     const int n = c.n_cell, nx = c.nx;
@@ -301,10 +301,10 @@ __device__ double residual_g(const CmfdView &c, Blk &B, const double *m, const d
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double v = m[i] * x[i];
         int ix = i % nx;
-        if (ix > 0) v += m[n + i] * x[i - 1];
-        if (ix < nx - 1) v += m[2 * n + i] * x[i + 1];
-        if (i >= nx) v += m[3 * n + i] * x[i - nx];
-        if (i + nx < n) v += m[4 * n + i] * x[i + nx];
+        if (ix > 0) v += m[n + i] * (m[i - 1] * x[i - 1]);
+        if (ix < nx - 1) v += m[2 * n + i] * (m[i + 1] * x[i + 1]);
+        if (i >= nx) v += m[3 * n + i] * (m[i - nx] * x[i - nx]);
+        if (i + nx < n) v += m[4 * n + i] * (m[i + nx] * x[i + nx]);
         double d = v - b[i];
         acc += d * d;
     }
@@ -374,7 +374,7 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             diag += area(c, i, s) * (dt[sf] + h);
         }
         double *m = c.mat + (size_t)g * 6 * n;
-        m[i] = diag;
+        m[i] = (diag != 0.0) ? diag : 1.0;
         m[(size_t)5 * n + i] = (diag != 0.0) ? 1.0 / diag : 1.0; // Jacobi preconditioner
         const int offs[4] = {WEST, EAST, SOUTH, NORTH};
         for (int q = 0; q < 4; q++) {
@@ -388,6 +388,17 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             }
             m[(size_t)(q + 1) * n + i] = v;
         }
+    }
+    B.sync();
+    // column scaling by the neighbour's inverse diagonal
+    for (int idx = threadIdx.x; idx < G * n; idx += blockDim.x) {
+        const int g = idx / n, i = idx % n, ix = i % c.nx;
+        double *m = c.mat + (size_t)g * 6 * n;
+        const double *dinv = m + (size_t)5 * n;
+        if (ix > 0) m[(size_t)n + i] *= dinv[i - 1];
+        if (ix < c.nx - 1) m[(size_t)2 * n + i] *= dinv[i + 1];
+        if (i >= c.nx) m[(size_t)3 * n + i] *= dinv[i - c.nx];
+        if (i + c.nx < n) m[(size_t)4 * n + i] *= dinv[i + c.nx];
     }
     B.sync();
 
@@ -423,8 +434,9 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             build_source(c, g, b);
             for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = fg[i];
             B.sync();
-            ri += residual_g(c, B, m, x, b);
-            bic_its += bicgstab(c, B, m, b, x, tol, 150, w);
+            double rr0 = 0.0;
+            bic_its += bicgstab(c, B, m, b, x, tol, 150, w, rr0);
+            ri += rr0;
             for (int i = threadIdx.x; i < n; i += blockDim.x) fg[i] = x[i];
         }
         B.sync();

@@ -112,19 +112,19 @@ template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, 
 // shared-memory integer atomics. Those are single native operations (a float
 // add on shared memory is a compare-and-swap loop that retries and serialises
 // the lanes of a warp crossing the same FSR in the same row), they commute,
-// and nothing waits on them. A contribution x, multiplied by the unit's
-// power-of-two scale, is split exactly as x = hi * 2^20 + lo with
-// hi = floor(x / 2^20) and 0 <= lo <= 2^20 (lo rounded to an integer; its
+// and nothing waits on them. A contribution x, already multiplied by the
+// unit's power-of-two scale (folded into the polar weights), is split
+// exactly as x = hi * 2^20 + lo with hi = floor(x / 2^20) and
+// 0 <= lo <= 2^20 (lo rounded to an integer; its
 // error is half a unit, 2^-51 of the unit's bound below). The scale makes
 // |x| < 2^50 / max_hits, so at most max_hits adds keep the high word within
 // 2^30 + max_hits and the low word within max_hits * 2^20 <= 2^31.
 // Measured slower than the compare-and-swap tally: merging colliding lanes
 // with shuffles first, match-any de-duplication, per-warp copies, global
 // float reductions.
-__device__ __forceinline__ void tally_fixed(int2 *s_fix, int l, float acc, float scale)
+__device__ __forceinline__ void tally_fixed(int2 *s_fix, int l, float xs)
 {
-    if (acc != 0.f) {
-        const float xs = acc * scale;
+    if (xs != 0.f) {
         const float hf = floorf(xs * 0x1p-20f);
         atomicAdd(&s_fix[l].x, (int)hf);
         atomicAdd(reinterpret_cast<unsigned *>(&s_fix[l].y), (unsigned)__float2int_rn(fmaf(hf, -0x1p20f, xs)));
@@ -141,46 +141,266 @@ __device__ __forceinline__ void fixed_scale(float m, float sum_w, int hits, floa
 {
     const float bound = 2.f * m * sum_w * (float)hits;
     const int E = (int)((__float_as_uint(bound) >> 23) & 0xFFu) - 126; // bound < 2^E (normal bound)
-    const int se = max(-126, min(127, 50 - E));
+    const int se = max(-126, min(100, 50 - E)); // capped so that weight * scale stays finite
     scale = __uint_as_float((unsigned)(se + 127) << 23);
     inv = __uint_as_float((unsigned)(127 - se) << 23);
 }
+
+// Per-unit values a warp needs to sweep one bundle in one direction.
+template <typename Real, int NPOL> struct UnitCtx {
+    using R2 = typename Pair<Real>::T;
+    const Real *ring_len;     // this warp's ring: [ST][CH][32] lengths
+    const uint16_t *ring_fsr; // [ST][CH][32] unit-local FSR ids
+    const R2 *s_sq;           // (Sigma_t, qbar) per unit FSR
+    Real *s_tal;              // FP64 tally copy of this lane
+    int2 *s_fix;              // FP32 fixed-point tally
+    Real *psi_in, *psi_out;
+    double *cur, *sfl;
+    const int (*s_off)[kMaxPolar];
+    const int (*s_tgt)[kMaxPolar][2];
+    int ny_set;
+    Real rsin[NPOL], wt[NPOL];    // wt: polar weights (FP32: times the fixed-point scale)
+    Real cw[NPOL][2], fwt[NPOL][2]; // current / surface-flux weights
+};
 
 // CUR: 0 no coarse tallies; 1 currents and surface fluxes; 2 currents only
 // (the batched eigen path: MOCC's surface fluxes only feed the partial-current
 // store of CMFD::store_currents, cmfd.cpp:555-666, whose consumer
 // update_incoming_flux is disabled at eigen_solver.cpp:289).
+//
+// One warp sweeps bundle b in one direction (FWD: rows ascending). Per
+// segment and polar angle the FP32 path computes psi' = qbar + (psi - qbar)
+// E with E = 2^(-tau log2(e) / sin(theta)), and the tally contribution of
+// the row as the drop of sum_p w_p psi_p across the segment; that is
+// MOCC's psi -= (psi - qbar)(1 - E) and tally += w (psi - qbar)(1 - E)
+// (moc_sweeper_kernel.inc.hpp:100-140) summed over the polar angles. The
+// FP64 path follows MOCC's form with its table exponential.
+template <typename Real, int NPOL, bool GS, int CUR, bool FWD>
+__device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv, const UnitCtx<Real, NPOL> &U,
+                                           int b, int lane)
+{
+    using R2 = typename Pair<Real>::T;
+    constexpr int CH = Chunk<Real>::rows;
+    constexpr int ST = Chunk<Real>::stages;
+    constexpr bool FIXED = Chunk<Real>::fixed;
+    const int t = fv.bundle_track[(size_t)b * 32 + lane];
+    const int2 bc = fv.bundle_bc[(size_t)b * 32 + lane];
+    const int nrows = fv.bundle_nrows[b];
+    const int64_t row0 = fv.bundle_row[b];
+    const int nch = (nrows + CH - 1) / CH;
+    constexpr int dir = FWD ? 0 : 1;
+    const int bc_in = FWD ? bc.x : bc.y, bc_out = FWD ? bc.y : bc.x;
+    const Real *lenp = (const Real *)fv.len;
+
+    // chunk c of this direction covers rows [lo, hi)
+    auto chunk_rows = [&](int c, int &lo, int &hi) {
+        if (FWD) {
+            lo = c * CH;
+            hi = min(nrows, lo + CH);
+        } else {
+            hi = nrows - c * CH;
+            lo = max(0, hi - CH);
+        }
+    };
+    auto issue = [&](int c) {
+        int lo, hi;
+        chunk_rows(c, lo, hi);
+        const int nr = hi - lo;
+        const int buf = c % ST;
+        const char *gl = (const char *)(lenp + (row0 + lo) * 32);
+        char *sl = (char *)(U.ring_len + (size_t)buf * CH * 32);
+        const int nl = nr * 32 * (int)sizeof(Real) / 16;
+        for (int i = lane; i < nl; i += 32) cp_async16(sl + 16 * i, gl + 16 * i);
+        const char *gf = (const char *)(fv.lfsr + (row0 + lo) * 32);
+        char *sf = (char *)(U.ring_fsr + (size_t)buf * CH * 32);
+        const int nf = nr * 32 * (int)sizeof(uint16_t) / 16;
+        for (int i = lane; i < nf; i += 32) cp_async16(sf + 16 * i, gf + 16 * i);
+        cp_async_commit();
+    };
+    // ST-1 chunks ahead: one commit group per chunk (empty groups past the
+    // end keep the count uniform), so waiting until at most ST-1 groups are
+    // pending means chunk c has landed
+    for (int c = 0; c < ST - 1; c++) {
+        if (c < nch) issue(c);
+        else cp_async_commit();
+    }
+
+    Real psi[NPOL];
+#pragma unroll
+    for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? U.psi_in[U.s_off[dir][p] + bc_in] : (Real)0;
+    Real S = 0; // FP32: sum_p w_p psi_p
+    if constexpr (FIXED) {
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) S = fmaf(U.wt[p], psi[p], S); // the same chain as in row()
+    }
+    int ev = 0, ev_end = 0;
+    const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
+    if (CUR && t >= 0) {
+        ev = FWD ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
+        ev_end = FWD ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
+    }
+    // the next two crossing events (row, code) live in registers, so a row
+    // without an event costs one compare and the load of the event after
+    // next has rows of time to arrive
+    const int2 none = make_int2(INT_MAX, 0);
+    int2 ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
+    int2 ev1 = (CUR && ev + 1 < ev_end) ? evp[ev + 1] : none;
+    auto events = [&](int k) {
+        while (ev0.x == k) {
+            int c = ev0.y;
+            int surf = c >> 1;
+            bool ynorm = c & 1;
+            // partial current and surface flux of this crossing in the
+            // sweep precision, accumulated in FP64
+            Real jc = 0, fc = 0;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                jc += psi[p] * (ynorm ? U.cw[p][1] : U.cw[p][0]);
+                if (CUR == 1) fc += psi[p] * (ynorm ? U.fwt[p][1] : U.fwt[p][0]);
+            }
+            atomicAdd(U.cur + surf, widen(FWD ? jc : -jc));
+            if (CUR == 1) atomicAdd(U.sfl + surf, widen(fc));
+            ev++;
+            ev0 = ev1;
+            ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
+        }
+    };
+    // Per row: the factors E (FP32: E = 2^(-tau log2(e) / sin), the
+    // transmitted fraction; FP64: 1 - e^-tau from MOCC's table) of a segment
+    // in unit FSR l with Sigma_t sq.x and length L. They do not depend on psi,
+    // so a group of rows computes them all before the serial psi updates and
+    // tally adds (shared-memory atomics, which later loads cannot pass).
+    auto factors = [&](Real L, const R2 &sq, Real (&E)[NPOL]) {
+        const Real tau0 = sq.x * L;
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) {
+            if constexpr (FIXED) {
+                float e;
+                asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"((float)(tau0 * U.rsin[p])));
+                E[p] = e;
+            } else {
+                E[p] = atten(tau0, U.rsin[p], g.exp_tab);
+            }
+        }
+    };
+    auto update = [&](const R2 &sq, const Real (&E)[NPOL], int l) {
+        if constexpr (FIXED) {
+            Real S1 = 0;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
+                S1 = fmaf(U.wt[p], psi[p], S1);
+            }
+            tally_fixed(U.s_fix, l, S - S1);
+            S = S1;
+        } else {
+            Real acc = 0;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                Real d = (psi[p] - sq.y) * E[p];
+                psi[p] -= d;
+                acc += d * U.wt[p];
+            }
+            tally_add(U.s_tal, l, acc, lane);
+        }
+    };
+
+    for (int c = 0; c < nch; c++) {
+        if (c + ST - 1 < nch) issue(c + ST - 1);
+        else cp_async_commit();
+        cp_async_wait<ST - 1>();
+        __syncwarp();
+        int lo, hi;
+        chunk_rows(c, lo, hi);
+        const int nr = hi - lo;
+        // rows of this chunk in sweep order: FWD from the first, else from the last
+        const Real *cl = U.ring_len + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
+        const uint16_t *cf = U.ring_fsr + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
+        constexpr int step = FWD ? 32 : -32;
+        // Four rows per step: the loads and gathers of the four rows issue
+        // back to back; only the psi recurrence that follows is serial.
+        constexpr int UR = 4;
+        int k = 0;
+        for (; k + UR <= nr; k += UR) {
+            Real L[UR];
+            int l[UR];
+            R2 sq[UR];
+            Real E[UR][NPOL];
+#pragma unroll
+            for (int v = 0; v < UR; v++) {
+                L[v] = cl[(k + v) * step];
+                l[v] = cf[(k + v) * step];
+            }
+#pragma unroll
+            for (int v = 0; v < UR; v++) sq[v] = U.s_sq[l[v]];
+#pragma unroll
+            for (int v = 0; v < UR; v++) factors(L[v], sq[v], E[v]);
+#pragma unroll
+            for (int v = 0; v < UR; v++) {
+                if (CUR && t >= 0) events(FWD ? lo + k + v : hi - (k + v));
+                update(sq[v], E[v], l[v]);
+            }
+        }
+        for (; k < nr; k++) {
+            if (CUR && t >= 0) events(FWD ? lo + k : hi - k);
+            const int l = cf[k * step];
+            const R2 sq = U.s_sq[l];
+            Real E[NPOL];
+            factors(cl[k * step], sq, E);
+            update(sq, E, l);
+        }
+        __syncwarp();
+    }
+    if (t >= 0) {
+        if (CUR) events(FWD ? nrows : 0);
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) {
+            if (GS) {
+                int tgt = U.s_tgt[dir][p][bc_out < U.ny_set ? 0 : 1];
+                if (tgt >= 0) U.psi_in[tgt + bc_out] = psi[p];
+            } else {
+                U.psi_out[U.s_off[dir][p] + bc_out] = psi[p];
+            }
+        }
+    }
+}
+
 template <typename Real, int NPOL, bool GS, int CUR>
 __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv, const StateView &st, int group,
                                            int wu, unsigned char *smem_raw)
 {
     using R2 = typename Pair<Real>::T;
     constexpr int CH = Chunk<Real>::rows;
+    constexpr int ST = Chunk<Real>::stages;
+    constexpr int TC = Chunk<Real>::tally_copies;
+    constexpr bool FIXED = Chunk<Real>::fixed;
     const WorkUnitDev u = fv.wu[wu];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     // [warp rings][(sigma_t, qbar) pairs][tally]
     unsigned char *ring = smem_raw + (size_t)warp * ring_bytes<Real>();
-    constexpr int ST = Chunk<Real>::stages;
-    Real *ring_len = reinterpret_cast<Real *>(ring);                                    // [ST][CH][32]
-    uint16_t *ring_fsr = reinterpret_cast<uint16_t *>(ring + ST * CH * 32 * sizeof(Real)); // [ST][CH][32]
     R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real>());
-    constexpr int TC = Chunk<Real>::tally_copies;
-    constexpr bool FIXED = Chunk<Real>::fixed;
     Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // FP64: [TC][max_local]
-    Real *s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
     int2 *s_fix = reinterpret_cast<int2 *>(s_sq + fv.max_local);  // FP32: [max_local] (hi, lo)
 
-    const int ntasks = 2 * u.n_bundles;
-    const Real *lenp = (const Real *)fv.len;
-    Real *psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
-    Real *psi_out = (Real *)st.psi_out;
-    const int ny_set = g.set_ny[u.set];
+    UnitCtx<Real, NPOL> U;
+    U.ring_len = reinterpret_cast<const Real *>(ring);
+    U.ring_fsr = reinterpret_cast<const uint16_t *>(ring + ST * CH * 32 * sizeof(Real));
+    U.s_sq = s_sq;
+    U.s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
+    U.s_fix = s_fix;
+    U.psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
+    U.psi_out = (Real *)st.psi_out;
+    U.cur = st.cur + (size_t)group * g.n_surf;
+    U.sfl = st.sflux + (size_t)group * g.n_surf;
+    U.ny_set = g.set_ny[u.set];
 
     // per unit: boundary-flux offsets of every (direction, polar) angle and
     // the reflected angles' incoming offsets for the Gauss-Seidel write-through
     __shared__ int s_off[2][kMaxPolar], s_tgt[2][kMaxPolar][2];
     __shared__ unsigned s_mbits; // largest |qbar| or incoming |psi| of the unit (float bits)
+    U.s_off = s_off;
+    U.s_tgt = s_tgt;
     if (threadIdx.x < 2 * NPOL) {
         const int dir = threadIdx.x / NPOL, p = threadIdx.x % NPOL;
         const SetPolar sp = g.sp[u.set * NPOL + p];
@@ -196,19 +416,41 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
 
     const Real *sigt = (const Real *)st.sigt;
     const Real *qbar = (const Real *)st.qbar;
+    const int *lf = fv.local_fsr + u.fsr_begin;
     unsigned mbits = 0u; // float bits of a non-negative value order like the integers
-    for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
-        int gl = fv.local_fsr[u.fsr_begin + i];
-        const Real q = qbar[gl];
-        s_sq[i] = R2{sigt[gl], q};
-        if constexpr (FIXED) {
-            mbits = max(mbits, __float_as_uint(fabsf((float)q)));
-            s_fix[i] = make_int2(0, 0);
-        } else {
+    // staging: four FSRs per thread in flight, so the dependent loads
+    // (local id, then Sigma_t and qbar) overlap
+    for (int i0 = threadIdx.x; i0 < u.n_local; i0 += 4 * blockDim.x) {
+        int gl[4];
 #pragma unroll
-            for (int c = 0; c < TC; c++) s_tal0[(size_t)c * fv.max_local + i] = (Real)0;
+        for (int j = 0; j < 4; j++) {
+            const int i = i0 + j * blockDim.x;
+            gl[j] = (i < u.n_local) ? lf[i] : -1;
+        }
+        Real sg[4], qq[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            sg[j] = gl[j] >= 0 ? sigt[gl[j]] : (Real)0;
+            qq[j] = gl[j] >= 0 ? qbar[gl[j]] : (Real)0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int i = i0 + j * blockDim.x;
+            if (i >= u.n_local) break;
+            s_sq[i] = R2{sg[j], qq[j]};
+            if constexpr (FIXED) {
+                mbits = max(mbits, __float_as_uint(fabsf((float)qq[j])));
+                s_fix[i] = make_int2(0, 0);
+            } else {
+#pragma unroll
+                for (int cc = 0; cc < TC; cc++) s_tal0[(size_t)cc * fv.max_local + i] = (Real)0;
+            }
         }
     }
+    // padding entries of the unit's rows point at the slot after its FSRs,
+    // which holds Sigma_t = qbar = 0: a padding row leaves psi unchanged
+    // bit for bit and adds nothing
+    if (threadIdx.x == 0) s_sq[u.n_local] = R2{(Real)0, (Real)0};
     if constexpr (FIXED) {
         // incoming angular fluxes of every lane, direction and polar angle
         for (int i = threadIdx.x; i < u.n_bundles * 64; i += blockDim.x) {
@@ -219,199 +461,43 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             const int bc_in = dir == 0 ? bc.x : bc.y;
 #pragma unroll
             for (int p = 0; p < NPOL; p++)
-                mbits = max(mbits, __float_as_uint(fabsf((float)psi_in[s_off[dir][p] + bc_in])));
+                mbits = max(mbits, __float_as_uint(fabsf((float)U.psi_in[s_off[dir][p] + bc_in])));
         }
         mbits = __reduce_max_sync(0xffffffffu, mbits);
         if (lane == 0 && mbits) atomicMax(&s_mbits, mbits);
     }
     __syncthreads();
 
-    Real rsin[NPOL], wt[NPOL];
-    Real cw[NPOL][2], fwt[NPOL][2]; // current / surface-flux weights (FP32 in the mixed path)
 #pragma unroll
     for (int p = 0; p < NPOL; p++) {
         const SetPolar sp = g.sp[u.set * NPOL + p];
-        rsin[p] = polar_factor<Real>(sp.rsin);
-        wt[p] = (Real)sp.wt;
+        U.rsin[p] = polar_factor<Real>(sp.rsin);
+        U.wt[p] = (Real)sp.wt;
         if (CUR) {
-            cw[p][0] = (Real)sp.cw[0];
-            cw[p][1] = (Real)sp.cw[1];
-            fwt[p][0] = (Real)sp.fw[0];
-            fwt[p][1] = (Real)sp.fw[1];
+            U.cw[p][0] = (Real)sp.cw[0];
+            U.cw[p][1] = (Real)sp.cw[1];
+            U.fwt[p][0] = (Real)sp.fw[0];
+            U.fwt[p][1] = (Real)sp.fw[1];
         }
     }
-    double *cur = st.cur + (size_t)group * g.n_surf;
-    double *sfl = st.sflux + (size_t)group * g.n_surf;
-    float scale = 1.f, inv_scale = 1.f;
+    float inv_scale = 1.f;
     if constexpr (FIXED) {
         float sum_w = 0.f;
 #pragma unroll
-        for (int p = 0; p < NPOL; p++) sum_w += fabsf((float)wt[p]);
+        for (int p = 0; p < NPOL; p++) sum_w += fabsf((float)U.wt[p]);
         const unsigned mb = s_mbits;
         if (mb >= 0x7F800000u && threadIdx.x == 0) atomicOr(st.status, (unsigned)DEV_NAN); // inf or NaN
+        float scale;
         fixed_scale(__uint_as_float(mb), sum_w, fv.max_hits, scale, inv_scale);
+#pragma unroll
+        for (int p = 0; p < NPOL; p++) U.wt[p] *= scale;
     }
 
+    const int ntasks = 2 * u.n_bundles;
     for (int task = warp; task < ntasks; task += nwarps) {
         const int b = u.bundle_begin + (task >> 1);
-        const bool fwd = (task & 1) == 0;
-        const int t = fv.bundle_track[(size_t)b * 32 + lane];
-        const int2 bc = fv.bundle_bc[(size_t)b * 32 + lane];
-        const int nrows = fv.bundle_nrows[b];
-        const int64_t row0 = fv.bundle_row[b];
-        const int nch = (nrows + CH - 1) / CH;
-        const int dir = fwd ? 0 : 1;
-        const int bc_in = fwd ? bc.x : bc.y, bc_out = fwd ? bc.y : bc.x;
-        Real psi[NPOL];
-#pragma unroll
-        for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? psi_in[s_off[dir][p] + bc_in] : (Real)0;
-        int ev = 0, ev_end = 0;
-        const int2 *evp = fwd ? g.ev_fw : g.ev_bw;
-        if (CUR && t >= 0) {
-            ev = fwd ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
-            ev_end = fwd ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
-        }
-        // the next two crossing events (row, code) live in registers, so a row
-        // without an event costs one compare and the load of the event after
-        // next has rows of time to arrive
-        const int2 none = make_int2(INT_MAX, 0);
-        int2 ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
-        int2 ev1 = (CUR && ev + 1 < ev_end) ? evp[ev + 1] : none;
-        auto events = [&](int k) {
-            while (ev0.x == k) {
-                int c = ev0.y;
-                int surf = c >> 1;
-                bool ynorm = c & 1;
-                // partial current and surface flux of this crossing in the
-                // sweep precision, accumulated in FP64
-                Real jc = 0, fc = 0;
-#pragma unroll
-                for (int p = 0; p < NPOL; p++) {
-                    jc += psi[p] * (ynorm ? cw[p][1] : cw[p][0]);
-                    if (CUR == 1) fc += psi[p] * (ynorm ? fwt[p][1] : fwt[p][0]);
-                }
-                atomicAdd(cur + surf, widen(fwd ? jc : -jc));
-                if (CUR == 1) atomicAdd(sfl + surf, widen(fc));
-                ev++;
-                ev0 = ev1;
-                ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
-            }
-        };
-        // chunk c of this direction covers rows [lo, hi)
-        auto chunk_rows = [&](int c, int &lo, int &hi) {
-            if (fwd) {
-                lo = c * CH;
-                hi = min(nrows, lo + CH);
-            } else {
-                hi = nrows - c * CH;
-                lo = max(0, hi - CH);
-            }
-        };
-        auto issue = [&](int c) {
-            int lo, hi;
-            chunk_rows(c, lo, hi);
-            const int nr = hi - lo;
-            const int buf = c % ST;
-            const char *gl = (const char *)(lenp + (row0 + lo) * 32);
-            char *sl = (char *)(ring_len + (size_t)buf * CH * 32);
-            const int nl = nr * 32 * (int)sizeof(Real) / 16;
-            for (int i = lane; i < nl; i += 32) cp_async16(sl + 16 * i, gl + 16 * i);
-            const char *gf = (const char *)(fv.lfsr + (row0 + lo) * 32);
-            char *sf = (char *)(ring_fsr + (size_t)buf * CH * 32);
-            const int nf = nr * 32 * (int)sizeof(uint16_t) / 16;
-            for (int i = lane; i < nf; i += 32) cp_async16(sf + 16 * i, gf + 16 * i);
-            cp_async_commit();
-        };
-
-        // ST-1 chunks ahead: one commit group per chunk (empty groups past
-        // the end keep the count uniform), so waiting until at most ST-1
-        // groups are pending means chunk c has landed
-        for (int c = 0; c < ST - 1; c++) {
-            if (c < nch) issue(c);
-            else cp_async_commit();
-        }
-        for (int c = 0; c < nch; c++) {
-            if (c + ST - 1 < nch) issue(c + ST - 1);
-            else cp_async_commit();
-            cp_async_wait<ST - 1>();
-            __syncwarp();
-            int lo, hi;
-            chunk_rows(c, lo, hi);
-            const Real *cl = ring_len + (size_t)(c % ST) * CH * 32;
-            const uint16_t *cf = ring_fsr + (size_t)(c % ST) * CH * 32;
-            const int nr = hi - lo;
-            // Four rows per step: the loads, gathers and attenuations of the
-            // four rows are independent and issue back to back; only the psi
-            // recurrence that follows is serial.
-            constexpr int U = 4;
-            int k = 0;
-            for (; k + U <= nr; k += U) {
-                Real L[U], e[U][NPOL];
-                int l[U];
-                R2 sq[U];
-#pragma unroll
-                for (int v = 0; v < U; v++) {
-                    const int j = fwd ? k + v : nr - 1 - (k + v);
-                    L[v] = cl[j * 32 + lane];
-                    l[v] = cf[j * 32 + lane];
-                }
-#pragma unroll
-                for (int v = 0; v < U; v++) sq[v] = s_sq[l[v]];
-#pragma unroll
-                for (int v = 0; v < U; v++) {
-                    const Real tau0 = sq[v].x * L[v];
-#pragma unroll
-                    for (int p = 0; p < NPOL; p++) e[v][p] = atten(tau0, rsin[p], g.exp_tab);
-                }
-#pragma unroll
-                for (int v = 0; v < U; v++) {
-                    if (CUR && t >= 0) {
-                        const int j = fwd ? k + v : nr - 1 - (k + v);
-                        events(fwd ? lo + j : lo + j + 1);
-                    }
-                    Real acc = 0;
-#pragma unroll
-                    for (int p = 0; p < NPOL; p++) {
-                        Real d = (psi[p] - sq[v].y) * e[v][p];
-                        psi[p] -= d;
-                        acc += d * wt[p];
-                    }
-                    if constexpr (FIXED) tally_fixed(s_fix, l[v], (float)acc, scale);
-                    else tally_add(s_tal, l[v], acc, lane);
-                }
-            }
-            for (; k < nr; k++) {
-                const int j = fwd ? k : nr - 1 - k; // row within the chunk
-                if (CUR && t >= 0) events(fwd ? lo + j : lo + j + 1);
-                const Real L = cl[j * 32 + lane];
-                const int l = cf[j * 32 + lane];
-                const R2 sq = s_sq[l];
-                const Real tau0 = sq.x * L;
-                Real acc = 0;
-#pragma unroll
-                for (int p = 0; p < NPOL; p++) {
-                    Real e = atten(tau0, rsin[p], g.exp_tab);
-                    Real d = (psi[p] - sq.y) * e;
-                    psi[p] -= d;
-                    acc += d * wt[p];
-                }
-                if constexpr (FIXED) tally_fixed(s_fix, l, (float)acc, scale);
-                else tally_add(s_tal, l, acc, lane);
-            }
-            __syncwarp();
-        }
-        if (t >= 0) {
-            if (CUR) events(fwd ? nrows : 0);
-#pragma unroll
-            for (int p = 0; p < NPOL; p++) {
-                if (GS) {
-                    int tgt = s_tgt[dir][p][bc_out < ny_set ? 0 : 1];
-                    if (tgt >= 0) psi_in[tgt + bc_out] = psi[p];
-                } else {
-                    psi_out[s_off[dir][p] + bc_out] = psi[p];
-                }
-            }
-        }
+        if ((task & 1) == 0) sweep_task<Real, NPOL, GS, CUR, true>(g, fv, U, b, lane);
+        else sweep_task<Real, NPOL, GS, CUR, false>(g, fv, U, b, lane);
     }
     __syncthreads();
     Real *tally = (Real *)st.tally;
@@ -424,9 +510,9 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         } else {
             v = s_tal0[i];
 #pragma unroll
-            for (int c = 1; c < TC; c++) v += s_tal0[(size_t)c * fv.max_local + i];
+            for (int cc = 1; cc < TC; cc++) v += s_tal0[(size_t)cc * fv.max_local + i];
         }
-        if (v != (Real)0) atomicAdd(tally + fv.local_fsr[u.fsr_begin + i], v);
+        if (v != (Real)0) atomicAdd(tally + lf[i], v);
     }
 }
 

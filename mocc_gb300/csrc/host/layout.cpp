@@ -60,7 +60,7 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                 u.fsr_begin = (int)L.local_fsr.size();
                 u.n_local = (int)fsrs.size();
                 L.local_fsr.insert(L.local_fsr.end(), fsrs.begin(), fsrs.end());
-                L.max_local = std::max(L.max_local, u.n_local);
+                L.max_local = std::max(L.max_local, u.n_local + 1); // + the padding slot
                 // longest first, bundles of W
                 std::stable_sort(tracks.begin(), tracks.end(), [&](int a, int b) {
                     return (f.trk_seg_begin[a + 1] - f.trk_seg_begin[a]) > (f.trk_seg_begin[b + 1] - f.trk_seg_begin[b]);
@@ -87,7 +87,7 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                     L.bundle_nrows.push_back(nrows);
                     size_t base = L.len.size();
                     L.len.resize(base + (size_t)nrows * W, 0.0);
-                    L.lfsr.resize(base + (size_t)nrows * W, 0);
+                    L.lfsr.resize(base + (size_t)nrows * W, (uint16_t)fsrs.size());
                     for (int lane = 0; lane < W; lane++) {
                         if (lane >= (int)grp.size()) {
                             L.bundle_track.push_back(-1);
@@ -101,7 +101,8 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                             L.len[base + (size_t)r * W + lane] = f.seg_len[a + r];
                             L.lfsr[base + (size_t)r * W + lane] = (uint16_t)loc[f.seg_fsr[a + r]];
                         }
-                        // padding rows keep length 0 and point at the unit's first FSR
+                        // padding rows keep length 0 and point at the padding slot
+                        // (local id n_local, after the unit's FSRs)
                         real += n;
                     }
                     padded += (int64_t)nrows * W;

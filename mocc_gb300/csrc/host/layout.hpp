@@ -38,7 +38,7 @@ struct SweepLayout {
     std::vector<uint16_t> lfsr;        // [rows * kLanes]
     std::vector<int> local_fsr;        // concatenated unit maps
     int64_t n_rows = 0;
-    int max_local = 0;
+    int max_local = 0;                 // FSR slots of the largest unit (its FSRs + the padding slot)
     int max_hits = 0;                  // most tally adds (segment entries x 2 directions) on one unit FSR
     double padding = 0.0;              // padded / real segments - 1
 };

@@ -1,11 +1,13 @@
-"""One batched branch-case run for profilers.
+"""One batched branch-case run (or one single solve) for profilers.
 
     python -m mocc_gb300.profile_batch [--cases 256] [--bundles-per-unit 1]
+    python -m mocc_gb300.profile_batch --single assembly17 [--precision 1]
 
 Runs the seeded branch-case batch (lattices uniform over 1x1/3x3/7x7/17x17
 pins, perturbed cross sections) once to capture the graph, then once more
 inside an NVTX range named ``mocgpu_timed`` so that a profiler can restrict
-itself to the second run, e.g.
+itself to the second run (with --single: one solve of that workload through
+MoCSweeper + EigenSolver, warmed up by a first solve), e.g.
 
     ncu --nvtx --nvtx-include "mocgpu_timed/" --metrics gpu__time_duration.sum \\
         --clock-control none --csv --log-file launches.csv \\
@@ -23,12 +25,32 @@ def main(argv=None):
     ap.add_argument("--cases", type=int, default=256)
     ap.add_argument("--bundles-per-unit", type=int, default=1)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--single", choices=["assembly17", "minicore"], default=None)
+    ap.add_argument("--precision", type=int, default=1)
     a = ap.parse_args(argv)
 
     import torch
 
     import mocc_gb300 as m
     from mocc_gb300 import workloads as W
+
+    if a.single:
+        prec = "mixed" if a.precision else "fp64"
+        xml, xsl = getattr(W, a.single)(precision=prec)
+        P = m.Problem(xml, xsl)
+        S = m.MoCSweeper(P, a.precision)
+        E = m.EigenSolver(P, sweeper=S)
+        E.solve()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("mocgpu_timed")
+        t = time.perf_counter()
+        r = E.solve()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"single": a.single, "precision": a.precision, "wall_s": wall, "k": r["k"],
+                          "iterations": r["iterations"], "converged": r["converged"]}))
+        return 0 if r["converged"] else 1
 
     cases = W.branch_cases(a.cases, seed=a.seed)
     bases = {}

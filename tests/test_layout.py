@@ -1,6 +1,6 @@
 """Host-side checks of the bundled sweep layout (every real segment appears
 exactly once, in its own track's lane, with its FSR and length; padding is
-zero-length; units respect the FSR cap)."""
+zero-length on the unit's padding slot; units respect the FSR cap)."""
 import numpy as np
 import pytest
 
@@ -15,7 +15,7 @@ def test_layout_covers_every_segment(gs, tpu, cap):
     st = P.layout_stats(gs=gs, tracks_per_unit=tpu, max_local=cap)
     assert st["real_segments"] == P.sizes["nseg"]
     assert st["len_sum"] == pytest.approx(P.export("seg_len").sum(), rel=1e-12)
-    assert st["max_local"] <= cap
+    assert st["max_local"] <= cap + 1  # the unit's FSRs and its padding slot
     assert st["phases"] == (2 if gs else 1)
     assert st["rows"] * 32 >= st["real_segments"]
 
