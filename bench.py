@@ -241,19 +241,37 @@ def run_branch(args, rank, world):
                                  reqs[:64])
     bpu = tune["best"]
 
-    def make_lanes(n_lanes):
-        cap = (n + n_lanes - 1) // n_lanes
-        return {k: m.BatchEngine(precision=1, capacity=cap, bundles_per_unit=bpu) for k in range(n_lanes)}
+    sizes = [size for size, ng, xml, xsl in cases]
 
-    def timed_batch(lanes):
-        """One batch of all cases over the lanes (round robin); device span of
-        the run from CUDA events on every lane's stream, and the results."""
+    def plan_name(plan):
+        if isinstance(plan, int):
+            return f"{plan} round robin"
+        return f"{plan[1]}: largest lattices on {plan[2]} of them"
+
+    def lane_of(plan, i):
+        """Lane of case i: round robin over n lanes, or ("size", n, b): the
+        largest lattices round robin over b lanes of their own and the rest
+        round robin over the other n - b."""
+        if isinstance(plan, int):
+            return i % plan
+        _, nl, nb = plan
+        big = max(sizes)
+        return i % nb if sizes[i] == big else nb + i % (nl - nb)
+
+    def make_lanes(plan):
+        keys = sorted({lane_of(plan, i) for i in range(n)})
+        cap = {k: sum(1 for i in range(n) if lane_of(plan, i) == k) for k in keys}
+        return {k: m.BatchEngine(precision=1, capacity=cap[k], bundles_per_unit=bpu) for k in keys}
+
+    def timed_batch(lanes, plan):
+        """One batch of all cases over the lanes; device span of the run from
+        CUDA events on every lane's stream, and the results."""
         streams = {k: torch.cuda.ExternalStream(e.stream()) for k, e in lanes.items()}
         ev0 = {k: torch.cuda.Event(enable_timing=True) for k in lanes}
         ev1 = {k: torch.cuda.Event(enable_timing=True) for k in lanes}
         for k in lanes:
             ev0[k].record(streams[k])
-        res = run_batch(lanes, [(P, x, i % len(lanes)) for i, (P, x) in enumerate(reqs)], n_pin_max)
+        res = run_batch(lanes, [(P, x, lane_of(plan, i)) for i, (P, x) in enumerate(reqs)], n_pin_max)
         for k in lanes:
             ev1[k].record(streams[k])
         torch.cuda.synchronize()
@@ -266,19 +284,19 @@ def run_branch(args, rank, world):
     # iterations overlap on the GPU (one lane's latency-bound CMFD beside the
     # others' sweeps); the count is measured, not assumed
     lane_ms = {}
-    for nl in (1, 2, 3, 4):
-        L = make_lanes(nl)
-        timed_batch(L)
-        lane_ms[nl] = timed_batch(L)[0]
+    for plan in (1, 2, 3, 4, ("size", 3, 1), ("size", 4, 2), ("size", 5, 2), ("size", 5, 3), ("size", 6, 3)):
+        L = make_lanes(plan)
+        timed_batch(L, plan)
+        lane_ms[plan] = timed_batch(L, plan)[0]
         for e in L.values():
             e.close()
-    n_lanes = min(lane_ms, key=lane_ms.get)
-    lanes = make_lanes(n_lanes)
+    plan = min(lane_ms, key=lane_ms.get)
+    lanes = make_lanes(plan)
     for _ in range(args.warmup):
-        timed_batch(lanes)
+        timed_batch(lanes, plan)
     for e in lanes.values():
         e.set_timing(True)
-    timed_batch(lanes)  # capture the timing graphs outside the timed region
+    timed_batch(lanes, plan)  # capture the timing graphs outside the timed region
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     barrier(world)
     torch.cuda.synchronize()
@@ -292,7 +310,7 @@ def run_branch(args, rank, world):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        sp, results = timed_batch(lanes)
+        sp, results = timed_batch(lanes, plan)
         wall += time.perf_counter() - t0
         span_ms += sp
     launches = m.launch_count() - l0
@@ -336,8 +354,8 @@ def run_branch(args, rank, world):
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": span_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {**CONFIG, "cases": n, "bundles_per_unit": bpu, "lanes": n_lanes, "replicas": world},
-            "lanes_ms_per_batch": lane_ms,
+            "config": {**CONFIG, "cases": n, "bundles_per_unit": bpu, "lanes": plan_name(plan), "replicas": world},
+            "lanes_ms_per_batch": {plan_name(k): v for k, v in lane_ms.items()},
             "sgu_per_s": sgu / (sweep_ms / 1e3), "sgu_per_s_whole_run": world * sgu / (span_ms / 1e3),
             "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int((h1 - h0) / args.steps),
                     "d2h_bytes_per_step": int((d1 - d0) / args.steps)},
