@@ -44,6 +44,8 @@ def _flags(ch: Path):
     cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", f"-I{ch / 'include'}", f"-I{INCLUDE}"]
     nv = [str(ch / "bin" / "nvcc"), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", *ARCH,
           f"-I{INCLUDE}", "--expt-relaxed-constexpr"]
+    # extra nvcc flags, e.g. -DMOCGPU_SWEEP_ROWS=4 to build another sweep chunk shape
+    nv += os.environ.get("MOCGPU_NVCC_EXTRA", "").split()
     return cxx, nv
 
 

@@ -76,9 +76,27 @@ template <> struct Pair<float> {
 template <> struct Pair<double> {
     using T = double2;
 };
+// Chunk shape of the segment rings (build-time: -DMOCGPU_SWEEP_ROWS=...,
+// -DMOCGPU_SWEEP_STAGES=...) and rows per unrolled step.
+#ifndef MOCGPU_SWEEP_ROWS
+#define MOCGPU_SWEEP_ROWS 8
+#endif
+#ifndef MOCGPU_SWEEP_STAGES
+#define MOCGPU_SWEEP_STAGES 2
+#endif
+#ifndef MOCGPU_SWEEP_UNROLL
+#define MOCGPU_SWEEP_UNROLL 4
+#endif
+// -DMOCGPU_SWEEP_MINB=n: the batched kernel (at most 256 threads) is built
+// for n resident CTAs of 256 threads per SM (a register cap)
+#if defined(MOCGPU_SWEEP_MINB) && MOCGPU_SWEEP_MINB > 0
+#define MOCGPU_SWEEP_BOUNDS __launch_bounds__(256, MOCGPU_SWEEP_MINB)
+#else
+#define MOCGPU_SWEEP_BOUNDS
+#endif
 template <typename Real> struct Chunk {
-    static constexpr int rows = 8;   // rows per streamed chunk
-    static constexpr int stages = 2; // chunks in flight per warp ring
+    static constexpr int rows = MOCGPU_SWEEP_ROWS;     // rows per streamed chunk
+    static constexpr int stages = MOCGPU_SWEEP_STAGES; // chunks in flight per warp ring
     static constexpr int tally_copies = 2; // FP64 shared tallies, lane l adds into copy l % tally_copies
     static constexpr bool fixed = sizeof(Real) == 4; // FP32: two-word fixed-point tally (same bytes)
 };
@@ -319,7 +337,7 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
         constexpr int step = FWD ? 32 : -32;
         // Four rows per step: the loads and gathers of the four rows issue
         // back to back; only the psi recurrence that follows is serial.
-        constexpr int UR = 4;
+        constexpr int UR = MOCGPU_SWEEP_UNROLL;
         int k = 0;
         for (; k + UR <= nr; k += UR) {
             Real L[UR];
@@ -528,7 +546,7 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
 // Persistent batched sweep: a fixed grid walks the (solve slot, work unit)
 // list of every active solve, largest units first.
 template <typename Real, int NPOL, bool GS, int CUR>
-__global__ void kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group)
+__global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = *n_items;
