@@ -131,21 +131,20 @@ template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, 
 // add on shared memory is a compare-and-swap loop that retries and serialises
 // the lanes of a warp crossing the same FSR in the same row), they commute,
 // and nothing waits on them. A contribution x, already multiplied by the
-// unit's power-of-two scale (folded into the polar weights), is split
-// exactly as x = hi * 2^20 + lo with hi = floor(x / 2^20) and
-// 0 <= lo <= 2^20 (lo rounded to an integer; its
-// error is half a unit, 2^-51 of the unit's bound below). The scale makes
-// |x| < 2^50 / max_hits, so at most max_hits adds keep the high word within
-// 2^30 + max_hits and the low word within max_hits * 2^20 <= 2^31.
-// Measured slower than the compare-and-swap tally: merging colliding lanes
-// with shuffles first, match-any de-duplication, per-warp copies, global
-// float reductions.
-__device__ __forceinline__ void tally_fixed(int2 *s_fix, int l, float xs)
+// unit's power-of-two scale (folded into the polar weights), is rounded to a
+// 64-bit integer (half a unit of error, 2^-51 of the unit's bound below) and
+// split as x = hi * 2^20 + lo with hi = floor(x / 2^20) and 0 <= lo < 2^20.
+// The scale makes |x| < 2^50 / max_hits, so at most max_hits adds keep the
+// high word within 2^30 + max_hits and the low word below max_hits * 2^20
+// <= 2^31. The float compare-and-swap tally this replaced was itself faster
+// than merging colliding lanes with shuffles first, match-any
+// de-duplication, per-warp copies and global float reductions.
+__device__ __forceinline__ void tally_fixed(int *s_hi, unsigned *s_lo, int l, float xs)
 {
     if (xs != 0.f) {
-        const float hf = floorf(xs * 0x1p-20f);
-        atomicAdd(&s_fix[l].x, (int)hf);
-        atomicAdd(reinterpret_cast<unsigned *>(&s_fix[l].y), (unsigned)__float2int_rn(fmaf(hf, -0x1p20f, xs)));
+        const long long v = __float2ll_rn(xs); // exact: |xs| < 2^50 and xs has 24 significant bits
+        atomicAdd(s_hi + l, (int)(v >> 20));
+        atomicAdd(s_lo + l, (unsigned)v & 0xFFFFFu);
     }
 }
 
@@ -171,7 +170,8 @@ template <typename Real, int NPOL> struct UnitCtx {
     const uint16_t *ring_fsr; // [ST][CH][32] unit-local FSR ids
     const R2 *s_sq;           // (Sigma_t, qbar) per unit FSR
     Real *s_tal;              // FP64 tally copy of this lane
-    int2 *s_fix;              // FP32 fixed-point tally
+    int *s_hi;                // FP32 fixed-point tally: high words
+    unsigned *s_lo;           // and low words (separate arrays: lanes spread over all banks)
     Real *psi_in, *psi_out;
     double *cur, *sfl;
     const int (*s_off)[kMaxPolar];
@@ -309,7 +309,7 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
                 psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
                 S1 = fmaf(U.wt[p], psi[p], S1);
             }
-            tally_fixed(U.s_fix, l, S - S1);
+            tally_fixed(U.s_hi, U.s_lo, l, S - S1);
             S = S1;
         } else {
             Real acc = 0;
@@ -399,14 +399,16 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     unsigned char *ring = smem_raw + (size_t)warp * ring_bytes<Real>();
     R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real>());
     Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // FP64: [TC][max_local]
-    int2 *s_fix = reinterpret_cast<int2 *>(s_sq + fv.max_local);  // FP32: [max_local] (hi, lo)
+    int *s_hi = reinterpret_cast<int *>(s_sq + fv.max_local);      // FP32: [max_local] high words
+    unsigned *s_lo = reinterpret_cast<unsigned *>(s_hi + fv.max_local); // and [max_local] low words
 
     UnitCtx<Real, NPOL> U;
     U.ring_len = reinterpret_cast<const Real *>(ring);
     U.ring_fsr = reinterpret_cast<const uint16_t *>(ring + ST * CH * 32 * sizeof(Real));
     U.s_sq = s_sq;
     U.s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
-    U.s_fix = s_fix;
+    U.s_hi = s_hi;
+    U.s_lo = s_lo;
     U.psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
     U.psi_out = (Real *)st.psi_out;
     U.cur = st.cur + (size_t)group * g.n_surf;
@@ -458,7 +460,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             s_sq[i] = R2{sg[j], qq[j]};
             if constexpr (FIXED) {
                 mbits = max(mbits, __float_as_uint(fabsf((float)qq[j])));
-                s_fix[i] = make_int2(0, 0);
+                s_hi[i] = 0;
+                s_lo[i] = 0u;
             } else {
 #pragma unroll
                 for (int cc = 0; cc < TC; cc++) s_tal0[(size_t)cc * fv.max_local + i] = (Real)0;
@@ -522,8 +525,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
         Real v;
         if constexpr (FIXED) {
-            const int2 w = s_fix[i];
-            const long long x = (long long)w.x * (1ll << 20) + (long long)(unsigned)w.y;
+            const long long x = (long long)s_hi[i] * (1ll << 20) + (long long)s_lo[i];
             v = (Real)(__ll2float_rn(x) * inv_scale);
         } else {
             v = s_tal0[i];
