@@ -84,6 +84,9 @@ template <> struct Pair<double> {
 #ifndef MOCGPU_SWEEP_STAGES
 #define MOCGPU_SWEEP_STAGES 2
 #endif
+#ifndef MOCGPU_TALLY_BITS
+#define MOCGPU_TALLY_BITS 50
+#endif
 #ifndef MOCGPU_SWEEP_UNROLL
 #define MOCGPU_SWEEP_UNROLL 4
 #endif
@@ -109,6 +112,13 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// Shared bytes per unit FSR: the (Sigma_t, qbar) pair and the tally (FP32:
+// fixed-point high and low words; FP64: the tally copies).
+template <typename Real> __host__ __device__ constexpr size_t fsr_slot_bytes()
+{
+    return sizeof(Real) == 4 ? 2 * sizeof(float) + 2 * 4 : (2 + Chunk<Real>::tally_copies) * sizeof(Real);
+}
+
 // Bytes of one warp's ring buffer (two chunks of lengths and local FSR ids).
 template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
 {
@@ -131,20 +141,28 @@ template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, 
 // add on shared memory is a compare-and-swap loop that retries and serialises
 // the lanes of a warp crossing the same FSR in the same row), they commute,
 // and nothing waits on them. A contribution x, already multiplied by the
-// unit's power-of-two scale (folded into the polar weights), is rounded to a
-// 64-bit integer (half a unit of error, 2^-51 of the unit's bound below) and
-// split as x = hi * 2^20 + lo with hi = floor(x / 2^20) and 0 <= lo < 2^20.
-// The scale makes |x| < 2^50 / max_hits, so at most max_hits adds keep the
-// high word within 2^30 + max_hits and the low word below max_hits * 2^20
-// <= 2^31. The float compare-and-swap tally this replaced was itself faster
-// than merging colliding lanes with shuffles first, match-any
-// de-duplication, per-warp copies and global float reductions.
-__device__ __forceinline__ void tally_fixed(int *s_hi, unsigned *s_lo, int l, float xs)
+// unit's power-of-two scale (folded into the polar weights), is an integer
+// when |x| >= 2^23 (24 significant bits) and is split exactly as
+// x = hi * 2^20 + lo with hi = floor(x / 2^20) and 0 <= lo < 2^20. The scale
+// makes |x| < 2^50 / max_hits, so at most max_hits adds keep the high word
+// within 2^30 + max_hits and the low word below max_hits * 2^20 <= 2^31.
+// Smaller contributions, more than 2^27 / max_hits below the unit's bound
+// (fluxes many decades below the unit's largest, as deep in a reflector
+// next to a vacuum face), are added straight to the FSR's FP32 tally in
+// global memory (a native float reduction), so every contribution keeps its
+// FP32 precision. The float compare-and-swap tally
+// this replaced was itself faster than merging colliding lanes with
+// shuffles first, match-any de-duplication, per-warp copies and global
+// float reductions.
+__device__ __forceinline__ void tally_fixed(int *s_hi, unsigned *s_lo, float *tally, const int *lf, float inv, int l,
+                                            float xs)
 {
-    if (xs != 0.f) {
-        const long long v = __float2ll_rn(xs); // exact: |xs| < 2^50 and xs has 24 significant bits
+    if (fabsf(xs) >= 0x1p23f) {
+        const long long v = __float2ll_rn(xs); // exact: 2^23 <= |xs| < 2^50 is an integer
         atomicAdd(s_hi + l, (int)(v >> 20));
         atomicAdd(s_lo + l, (unsigned)v & 0xFFFFFu);
+    } else if (xs != 0.f) {
+        atomicAdd(tally + lf[l], xs * inv); // below 2^23 units (rare): straight to the FSR's FP32 tally
     }
 }
 
@@ -158,7 +176,7 @@ __device__ __forceinline__ void fixed_scale(float m, float sum_w, int hits, floa
 {
     const float bound = 2.f * m * sum_w * (float)hits;
     const int E = (int)((__float_as_uint(bound) >> 23) & 0xFFu) - 126; // bound < 2^E (normal bound)
-    const int se = max(-126, min(100, 50 - E)); // capped so that weight * scale stays finite
+    const int se = max(-126, min(100, MOCGPU_TALLY_BITS - E)); // capped so that weight * scale stays finite
     scale = __uint_as_float((unsigned)(se + 127) << 23);
     inv = __uint_as_float((unsigned)(127 - se) << 23);
 }
@@ -172,6 +190,9 @@ template <typename Real, int NPOL> struct UnitCtx {
     Real *s_tal;              // FP64 tally copy of this lane
     int *s_hi;                // FP32 fixed-point tally: high words
     unsigned *s_lo;           // and low words (separate arrays: lanes spread over all banks)
+    float *tally;             // the solve's FP32 FSR tally (contributions below the fixed-point range)
+    const int *lf;            // unit-local -> global FSR ids
+    float inv_scale;          // 1 / the unit's fixed-point scale
     Real *psi_in, *psi_out;
     double *cur, *sfl;
     const int (*s_off)[kMaxPolar];
@@ -309,7 +330,7 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
                 psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
                 S1 = fmaf(U.wt[p], psi[p], S1);
             }
-            tally_fixed(U.s_hi, U.s_lo, l, S - S1);
+            tally_fixed(U.s_hi, U.s_lo, U.tally, U.lf, U.inv_scale, l, S - S1);
             S = S1;
         } else {
             Real acc = 0;
@@ -512,6 +533,9 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         fixed_scale(__uint_as_float(mb), sum_w, fv.max_hits, scale, inv_scale);
 #pragma unroll
         for (int p = 0; p < NPOL; p++) U.wt[p] *= scale;
+        U.tally = (float *)st.tally;
+        U.lf = lf;
+        U.inv_scale = inv_scale;
     }
 
     const int ntasks = 2 * u.n_bundles;
@@ -562,7 +586,7 @@ __global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *item
 template <typename Real> static size_t batched_smem(int bundles_per_unit, int max_local)
 {
     return (size_t)(2 * bundles_per_unit) * ring_bytes<Real>() +
-           (size_t)max_local * ((2 + Chunk<Real>::tally_copies) * sizeof(Real));
+           (size_t)max_local * fsr_slot_bytes<Real>();
 }
 
 template <typename Real, int NPOL, bool GS, int CUR> static void prepare_batched(size_t smem)
@@ -639,7 +663,7 @@ template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int
 template <typename Real> size_t fast_sweep_smem(const FastView &fv)
 {
     int nwarps = 2 * fv.bundles_per_unit;
-    return (size_t)nwarps * ring_bytes<Real>() + (size_t)fv.max_local * ((2 + Chunk<Real>::tally_copies) * sizeof(Real));
+    return (size_t)nwarps * ring_bytes<Real>() + (size_t)fv.max_local * fsr_slot_bytes<Real>();
 }
 template size_t fast_sweep_smem<float>(const FastView &);
 template size_t fast_sweep_smem<double>(const FastView &);

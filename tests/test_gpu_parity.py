@@ -226,3 +226,24 @@ def test_time_sweep_reports_launches():
     before = m.launch_count()
     S.sweep(0)
     assert m.launch_count() - before >= 2
+
+
+def test_mixed_wide_flux_range_matches_fp64():
+    # mini-core with a 21 cm reflector and vacuum faces at coarse tracking:
+    # the group fluxes span more than 20 decades, so a work unit's tally
+    # takes contributions far below its largest one (the FP32 sweep's
+    # fixed-point tally must hand those to its FP32 side path)
+    xml, xsl = W.minicore(n_azi=2, spacing=0.1)
+    P = m.Problem(xml, xsl)
+    res, pins, flux = {}, {}, {}
+    for precision in (0, 1):
+        S = m.MoCSweeper(P, precision)
+        res[precision] = m.EigenSolver(P, sweeper=S).solve()
+        pins[precision] = S.pin_powers()
+        flux[precision] = S.flux()
+        S.close()
+    assert res[0]["converged"] and res[1]["converged"]
+    assert flux[0].max() / flux[0][flux[0] > 0].min() > 1e20
+    assert (flux[1] > 0).all()
+    assert pcm(res[1]["k"], res[0]["k"]) < PCM_TOL
+    assert max_pin_err(pins[1], pins[0]) < PIN_TOL
