@@ -383,8 +383,11 @@ void BatchEngine::capture()
         }
     tev_used_ = 0;
     const int64_t l0 = launch_count();
+    const size_t n_ctr = (size_t)std::max(shape_.max_g, 1) * n_inner_ * 2;
+    if (d_ctr_.n < n_ctr) d_ctr_.alloc(n_ctr);
     MOCGPU_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     try {
+        MOCGPU_CUDA(cudaMemsetAsync(d_ctr_.p, 0, n_ctr * sizeof(int), stream_));
         if (cmfd_) {
             launch_b_pin_flux(b, stream_);
             launch_b_homogenize(b, stream_);
@@ -403,14 +406,15 @@ void BatchEngine::capture()
                 for (int ph = 0; ph < 2; ph++) {
                     const int2 *items = d_items_.p + (size_t)ph * shape_.items_cap;
                     const int *nit = d_nitems_.p + (size_t)g * 2 + ph;
+                    int *ctr = d_ctr_.p + ((size_t)g * n_inner_ + inner) * 2 + ph;
                     if (timing_)
                         MOCGPU_CUDA(cudaEventRecordWithFlags(tev_[2 * tev_used_], stream_, cudaEventRecordExternal));
                     if (precision_ == 0)
                         launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
-                                               shape_.max_local, stream_);
+                                               shape_.max_local, ctr, stream_);
                     else
                         launch_b_sweep<float>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
-                                              shape_.max_local, stream_);
+                                              shape_.max_local, ctr, stream_);
                     if (timing_) {
                         MOCGPU_CUDA(
                             cudaEventRecordWithFlags(tev_[2 * tev_used_ + 1], stream_, cudaEventRecordExternal));

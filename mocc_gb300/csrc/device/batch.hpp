@@ -150,6 +150,7 @@ class BatchEngine {
     DevBuf<int> d_act_, d_nact_;
     DevBuf<int2> d_items_;
     DevBuf<int> d_nitems_;
+    DevBuf<int> d_ctr_; // per sweep launch of a replay: next-item counter of the persistent sweep
     DevBuf<double> d_sum_;
     double *h_sum_ = nullptr; // pinned summary
     DevBuf<double> d_pins_;    // [cap][pins_stride_] pin powers of the last replay

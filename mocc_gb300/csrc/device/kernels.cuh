@@ -157,7 +157,7 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
 template <typename Real>
 void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
-                    bool cur, int pol, int bundles_per_unit, int max_local, cudaStream_t s);
+                    bool cur, int pol, int bundles_per_unit, int max_local, int *counter, cudaStream_t s);
 // Sets the shared-memory limit of the batched sweep ahead of graph capture.
 template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local);
 void note_launches(int64_t n); // adds replayed launches to launch_count()

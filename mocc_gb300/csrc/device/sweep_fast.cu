@@ -570,16 +570,24 @@ __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, i
 }
 
 // Persistent batched sweep: a fixed grid walks the (solve slot, work unit)
-// list of every active solve, largest units first.
+// list of every active solve, largest units first. Each CTA starts on item
+// blockIdx.x and then takes the next untaken item from a counter (zeroed
+// once per graph replay), so CTAs that drew short units take more of them
+// and the launch ends with little tail.
 template <typename Real, int NPOL, bool GS, int CUR>
-__global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group)
+__global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *items, const int *n_items, int group,
+                                                  int *counter)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int s_next;
     const int n = *n_items;
-    for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    int it = blockIdx.x;
+    while (it < n) {
         const int2 item = items[it];
         sweep_unit<Real, NPOL, GS, CUR>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y, smem_raw);
-        __syncthreads();
+        if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);
+        __syncthreads(); // also: the next unit may overwrite this one's shared data
+        it = s_next;
     }
 }
 
@@ -601,7 +609,7 @@ template <typename Real, int NPOL, bool GS, int CUR> static void prepare_batched
 
 template <typename Real, int NPOL, bool GS, int CUR>
 static void launch_batched(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group,
-                           int bundles_per_unit, int max_local, cudaStream_t s)
+                           int bundles_per_unit, int max_local, int *counter, cudaStream_t s)
 {
     auto k = kb_sweep_fast<Real, NPOL, GS, CUR>;
     const int nwarps = 2 * bundles_per_unit;
@@ -613,7 +621,7 @@ static void launch_batched(const BatchViews &b, const int2 *items, const int *n_
     MOCGPU_CUDA(cudaGetDevice(&dev));
     MOCGPU_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     int grid = std::max(1, std::min(max_items, sms * std::max(1, per_sm)));
-    k<<<grid, 32 * nwarps, smem, s>>>(b, items, n_items, group);
+    k<<<grid, 32 * nwarps, smem, s>>>(b, items, n_items, group, counter);
 }
 
 template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local)
@@ -632,20 +640,20 @@ template void prepare_b_sweep<double>(int, int, int);
 
 template <typename Real>
 void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
-                    bool cur, int pol, int bundles_per_unit, int max_local, cudaStream_t s)
+                    bool cur, int pol, int bundles_per_unit, int max_local, int *counter, cudaStream_t s)
 {
     if (max_items <= 0) return;
     note_launch_external();
 #define MOCGPU_B(NP)                                                                                                 \
     if (pol == NP) {                                                                                                 \
         if (gs && !cur) launch_batched<Real, NP, true, 0>(b, items, n_items, max_items, group, bundles_per_unit,  \
-                                                              max_local, s);                                         \
+                                                              max_local, counter, s);                                         \
         else if (gs && cur) launch_batched<Real, NP, true, 2>(b, items, n_items, max_items, group,               \
-                                                                 bundles_per_unit, max_local, s);                     \
+                                                                 bundles_per_unit, max_local, counter, s);                     \
         else if (!gs && !cur) launch_batched<Real, NP, false, 0>(b, items, n_items, max_items, group,           \
-                                                                     bundles_per_unit, max_local, s);                 \
+                                                                     bundles_per_unit, max_local, counter, s);                 \
         else launch_batched<Real, NP, false, 2>(b, items, n_items, max_items, group, bundles_per_unit, max_local,  \
-                                                   s);                                                               \
+                                                   counter, s);                                                               \
         return;                                                                                                      \
     }
     MOCGPU_B(1)
@@ -656,9 +664,9 @@ void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, 
     throw Error(1, "unsupported number of polar angles per track set");
 }
 template void launch_b_sweep<float>(const BatchViews &, const int2 *, const int *, int, int, bool, bool, int, int, int,
-                                    cudaStream_t);
+                                    int *, cudaStream_t);
 template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int *, int, int, bool, bool, int, int,
-                                     int, cudaStream_t);
+                                     int, int *, cudaStream_t);
 
 template <typename Real> size_t fast_sweep_smem(const FastView &fv)
 {
