@@ -167,14 +167,34 @@ __device__ __forceinline__ double spmv_row(const double *__restrict__ m, const d
 }
 
 // b_g = (chi_g fs + sum_{g'!=g} S(g<-g') phi_g') V
+// sum over gg != skip of a[gg * sa] * b[gg * sb] in order of gg, with the
+// loads of eight groups issued together (the CMFD CTA is latency-bound:
+// a loop of dependent load-multiply-adds waits out one memory latency per
+// group)
+__device__ __forceinline__ double group_dot(const double *a, int sa, const double *b, int sb, int G, int skip)
+{
+    double s = 0.0;
+    for (int g0 = 0; g0 < G; g0 += 8) {
+        double x[8], y[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int gg = g0 + j;
+            const bool ok = gg < G && gg != skip;
+            x[j] = ok ? a[(size_t)gg * sa] : 0.0;
+            y[j] = ok ? b[(size_t)gg * sb] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) s += x[j] * y[j];
+    }
+    return s;
+}
+
 __device__ void build_source(const CmfdView &c, int g, double *b)
 {
     const int n = c.n_cell, G = c.G;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double s = c.xsch[(size_t)i * G + g] * c.fs[i];
-        const double *row = c.scat + ((size_t)i * G + g) * G;
-        for (int gg = 0; gg < G; gg++)
-            if (gg != g) s += row[gg] * c.flux[(size_t)gg * n + i];
+        s += group_dot(c.scat + ((size_t)i * G + g) * G, 1, c.flux + i, n, G, g);
         b[i] = s * cell_vol(c, i);
     }
 }
@@ -277,19 +297,15 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
 __device__ void fission_source(const CmfdView &c, double k)
 {
     const int n = c.n_cell, G = c.G;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double f = 0.0;
-        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
-        c.fs[i] = f * (1.0 / k);
-    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        c.fs[i] = group_dot(c.xsnf + (size_t)i * G, 1, c.flux + i, n, G, -1) * (1.0 / k);
 }
 
 __device__ double total_fission(const CmfdView &c, Blk &B)
 {
     const int n = c.n_cell, G = c.G;
     double f = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        for (int g = 0; g < G; g++) f += c.xsnf[(size_t)i * G + g] * c.flux[(size_t)g * n + i];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) f += group_dot(c.xsnf + (size_t)i * G, 1, c.flux + i, n, G, -1);
     return B.sum(f);
 }
 
@@ -467,7 +483,7 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     }
 }
 
-__global__ void __launch_bounds__(512) k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
+__global__ void __launch_bounds__(512, 1) k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
 
 // One CTA per active solve of a batch; the coarse-current flag and the CMFD
 // iteration count live in each solve's scalar block.
