@@ -134,6 +134,39 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def l2_copy_gbs():
+    """Copy bandwidth of a buffer that stays in L2 (two 32 MB halves, read +
+    write bytes, best of 20 batches of 50 copies, CUDA events): the ceiling
+    of a kernel whose data is L2-resident."""
+    import torch
+    a = torch.empty(32 << 20, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+    b.copy_(a)
+    best = 0.0
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(50):
+            b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2 * a.numel() * 50 / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return best
+
+
+def secondary_ceilings(achieved_gbs, sgu_per_s, clk):
+    """The sweep against the two other ceilings of its path: the L2 copy
+    bandwidth (its data is L2-resident on the branch workload) and the
+    exponential throughput (6 ex2 per segment-group update, 16 per clock per
+    SM nominal, at the SM clock sampled during the run)."""
+    l2 = l2_copy_gbs()
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    sfu = 16 * 152 * mhz * 1e6 / 6
+    return {"l2_copy_gbs": l2, "frac_of_l2": achieved_gbs / l2 if achieved_gbs else None,
+            "sfu_sgu_per_s": sfu, "frac_of_sfu": sgu_per_s / sfu if sgu_per_s else None,
+            "how": "l2: copy of a 32 MB buffer (read + write bytes), best of 20 x 50, CUDA events; sfu: nominal"}
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -377,7 +410,8 @@ def run_branch(args, rank, world):
                          "kernel": "kb_sweep_fast",
                          "bytes_per_launch": sweep_bytes / max(sweep_launches, 1),
                          "ms_per_launch": sweep_ms / max(sweep_launches, 1), "peak_source": peak_kind,
-                         "sweep_share_of_replay": sweep_ms / replay_ms},
+                         "sweep_share_of_replay": sweep_ms / replay_ms,
+                         "secondary": secondary_ceilings(achieved, sgu / (sweep_ms / 1e3), clk)},
             "tuning": tune, "clocks": clk, "gpu_launches": int(launches),
             "outer_iterations": int(sum(r["iterations"] for r in results))}
 
@@ -420,22 +454,34 @@ def run_branch(args, rank, world):
     if rank == 0 and not args.no_cpu:
         import oracle
         sample = oracle_sample(cases)
-        errs, tcpu, cores = [], 0.0, None
+        errs, tcpu, cores, sgu = [], 0.0, None, 0
         for i, xml, xsl in sample:
-            O = oracle.OracleSolver(m.Problem(xml, xsl))
+            Po = m.Problem(xml, xsl)
+            O = oracle.OracleSolver(Po)
             t = time.perf_counter()
             ro = O.solve()
             tcpu += time.perf_counter() - t
             cores = O.threads
+            sgu += ro["sweeps"] * Po.sizes["nseg"]
             errs.append((cases[i][0], pcm(results[i]["k"], ro["k"]), max_pin_err(results[i]["pin_powers"],
                                                                                   O.pin_powers())))
         line["accuracy"] = {"vs": "FP64 CPU oracle, same inputs", "cases": [
             {"size": s, "k_err_pcm": e, "max_pin_err": p} for s, e, p in errs],
             "k_err_pcm_max": max(e for _, e, _ in errs), "max_pin_err": max(p for _, _, p in errs),
             "tolerance": {"k_pcm": 10.0, "pin": 1e-3}}
+        # one thread, on the 3x3 case of the sample
+        i3, xml3, xsl3 = next(c for c in sample if cases[c[0]][0] == 3)
+        P3 = m.Problem(xml3, xsl3)
+        O1 = oracle.OracleSolver(P3, n_threads=1)
+        t = time.perf_counter()
+        r1 = O1.solve()
+        t1 = time.perf_counter() - t
         line["cpu_baseline"] = {"value": len(sample) / tcpu, "unit": "solves/s", "cores": cores, "kind": "port",
                                 "sample": "one full FP64 solve of one case of each lattice size (1x1, 3x3, 7x7, "
-                                          "17x17) with all host threads"}
+                                          "17x17) with all host threads",
+                                "sgu_per_s": sgu / tcpu,
+                                "single_thread": {"sample": "the 3x3 case", "solves_per_s": 1.0 / t1,
+                                                  "sgu_per_s": r1["sweeps"] * P3.sizes["nseg"] / t1}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -504,7 +550,9 @@ def run_single(args, rank, world):
                            "mixed_vs_fp64_pcm": pcm(r["k"], r64["k"]), "mixed_vs_fp64_pin": max_pin_err(pins, pins64)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": None, "kernel": "k_sweep_fast",
-                         "peak_source": peak_kind},
+                         "peak_source": peak_kind,
+                         "secondary": secondary_ceilings(achieved, P.sizes["nseg"] / (ms / 20 / 1e3) if nl else None,
+                                                         clk)},
             "clocks": clk, "gpu_launches": int(launches)}
     if rank == 0 and not args.no_cpu:
         import oracle

@@ -181,3 +181,22 @@ def test_retired_handles_are_reused_without_allocation():
     again = _run(E, [P, P, P, P])
     assert E.stats()["bytes_in_use"] == used  # the two pooled handles served all four solves
     assert all(abs(r["k"] - first[0]["k"]) < 1e-11 for r in again)
+
+
+def test_mixed_group_counts_in_one_batch_match_oracle():
+    # 7- and 23-group solves in one engine: a solve with G groups takes part
+    # only in the first G group launches of a replay
+    cases = [W.lattice_case(size, 8, 0.05, "mixed", seed=1007 if ng == 23 else 1000, n_group=ng,
+                            mod_factor=mf, fuel_nf_factor=1.0)
+             for size, ng, mf in ((3, 23, 0.95), (1, 7, 1.05), (3, 7, 1.0), (1, 23, 1.08))]
+    probs = [m.Problem(x, s) for x, s in cases]
+    assert sorted(P.sizes["ngroup"] for P in probs) == [7, 7, 23, 23]
+    E = m.BatchEngine(precision=1, capacity=4)
+    res = _run(E, probs)
+    for P, r in zip(probs, res):
+        assert r["error"] == 0, r["message"]
+        O = oracle.OracleSolver(P)
+        ref = O.solve()
+        assert r["converged"] == 1
+        assert pcm(r["k"], ref["k"]) < 10.0
+        assert max_pin_err(r["pin_powers"], O.pin_powers()) < 1e-3
