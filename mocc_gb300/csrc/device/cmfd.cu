@@ -6,6 +6,7 @@
 // single warp, so every reduction is a shuffle tree and every barrier a warp
 // barrier; larger meshes use 4 to 16 warps with one block barrier per
 // reduction. Work vectors live in shared memory when they fit.
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -483,6 +484,410 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     }
 }
 
+// ---------------------------------------------------------------------------
+// CMFD of one solve on a thread-block cluster: the CTAs of the cluster split
+// the coarse cells into contiguous slices and each keeps its slice of every
+// work vector and of the current group's operator in its shared memory. A
+// matrix row whose neighbour lies in another CTA's slice reads it from that
+// CTA's shared memory (distributed shared memory); every block sum is
+// completed across the cluster by writing each CTA's total into every CTA's
+// exchange slots and adding the slots in rank order after a cluster barrier,
+// so all CTAs hold bit-identical sums and take the same branches at every
+// loop test (the barriers of the cluster stay matched). Data one CTA writes to
+// global memory for another (fixed-up fluxes, surface coefficients, inverse
+// diagonals) is read back through L2 (ld.global.cg) after a cluster barrier.
+// The FP64 work of a BiCGSTAB iteration is spread over several SMs' FP64
+// pipes, which is what bounds the one-CTA solve of a single large mesh.
+namespace {
+
+__device__ __forceinline__ unsigned cl_rank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cl_nrank()
+{
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;\n" : "=r"(r));
+    return r;
+}
+// Barrier of all threads of the cluster (a warp may arrive diverged, after
+// loops of uneven trip counts: it reconverges first).
+__device__ __forceinline__ void cl_sync()
+{
+    __syncwarp();
+    asm volatile("barrier.cluster.arrive.release;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory");
+}
+// shared-memory address `p` (of this CTA's layout) in CTA `rank` of the cluster
+__device__ __forceinline__ unsigned peer_addr(const void *p, unsigned rank)
+{
+    unsigned a = (unsigned)__cvta_generic_to_shared(p), r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ double ld_peer(const double *p, unsigned rank)
+{
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(peer_addr(p, rank)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_peer(double *p, unsigned rank, double v)
+{
+    asm volatile("st.shared::cluster.f64 [%0], %1;\n" ::"r"(peer_addr(p, rank)), "d"(v) : "memory");
+}
+
+// The cluster as one team: cells [lo, hi) belong to this CTA.
+struct Team {
+    Blk B;
+    unsigned rank, size;
+    int slice, lo, hi;
+    double *xch; // [2][2][16] exchange slots (double-buffered, two values)
+    int xb = 0;
+    __device__ void sync() const { cl_sync(); }
+    // cluster sums; every CTA adds the same per-CTA totals in rank order
+    __device__ double sum(double a)
+    {
+        a = B.sum(a);
+        double *s = xch + xb * 32;
+        if (threadIdx.x < size) st_peer(s + rank, threadIdx.x, a);
+        cl_sync();
+        double t = 0.0;
+        for (unsigned r = 0; r < size; r++) t += s[r];
+        xb ^= 1;
+        return t;
+    }
+    __device__ void sum2(double &a, double &b)
+    {
+        B.sum2(a, b);
+        double *s = xch + xb * 32;
+        if (threadIdx.x < size) {
+            st_peer(s + rank, threadIdx.x, a);
+            st_peer(s + 16 + rank, threadIdx.x, b);
+        }
+        cl_sync();
+        double ta = 0.0, tb = 0.0;
+        for (unsigned r = 0; r < size; r++) {
+            ta += s[r];
+            tb += s[16 + r];
+        }
+        a = ta;
+        b = tb;
+        xb ^= 1;
+    }
+    // value of slice vector v at cell j (this CTA's or a peer's slice)
+    __device__ __forceinline__ double at(const double *v, int j) const
+    {
+        if (j >= lo && j < hi) return v[j - lo];
+        const unsigned o = (unsigned)(j / slice);
+        return ld_peer(v + (j - (int)o * slice), o);
+    }
+};
+
+// Row i (a cell of this CTA) of A D^-1 applied to the slice vector x; m holds
+// this CTA's rows of the column-scaled operator, [6][slice].
+__device__ __forceinline__ double spmv_row_team(const Team &T, const double *m, const double *x, int i, int n, int nx)
+{
+    const int li = i - T.lo, s = T.slice;
+    double v = x[li];
+    const int ix = i % nx;
+    if (ix > 0) v += m[s + li] * T.at(x, i - 1);
+    if (ix < nx - 1) v += m[2 * s + li] * T.at(x, i + 1);
+    if (i >= nx) v += m[3 * s + li] * T.at(x, i - nx);
+    if (i + nx < n) v += m[4 * s + li] * T.at(x, i + nx);
+    return v;
+}
+
+// bicgstab() on the team's slices: the same iterates and stopping test.
+__device__ int bicgstab_team(const CmfdView &c, Team &T, const double *m, const double *b, double *x, double tol,
+                             int max_it, double *w, double &rr0)
+{
+    const int n = c.n_cell, nx = c.nx, s = T.slice, lo = T.lo, hi = T.hi;
+    double *r = w, *r0 = w + s, *p = w + 2 * s, *v = w + 3 * s, *sv = w + 4 * s, *t = w + 5 * s;
+    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) x[i - lo] *= m[i - lo];
+    T.sync();
+    double rr = 0.0, bb = 0.0;
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+        const int li = i - lo;
+        double ri = b[li] - spmv_row_team(T, m, x, i, n, nx);
+        r[li] = ri;
+        r0[li] = ri;
+        p[li] = 0.0;
+        v[li] = 0.0;
+        rr += ri * ri;
+        bb += b[li] * b[li];
+    }
+    T.sum2(rr, bb);
+    rr0 = rr;
+    if (bb == 0.0) {
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) x[i - lo] = 0.0;
+        T.sync();
+        return 0;
+    }
+    double r0_sq = rr, rho = 1.0, alpha = 1.0, om = 1.0;
+    const double tol2 = tol * tol * bb;
+    int it = 0, restarts = 0;
+    double rho_new = rr;
+    while (rr > tol2 && it < max_it) {
+        double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0_sq) {
+            T.sync();
+            double acc = 0.0;
+            for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+                const int li = i - lo;
+                double ri = b[li] - spmv_row_team(T, m, x, i, n, nx);
+                r[li] = ri;
+                r0[li] = ri;
+                acc += ri * ri;
+            }
+            acc = T.sum(acc);
+            rho = r0_sq = acc;
+            if (restarts++ == 0) it = 0;
+        }
+        const double beta = (rho / rho_old) * (alpha / om);
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const int li = i - lo;
+            p[li] = r[li] + beta * (p[li] - om * v[li]);
+        }
+        T.sync();
+        double r0v = 0.0;
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const int li = i - lo;
+            const double vi = spmv_row_team(T, m, p, i, n, nx);
+            v[li] = vi;
+            r0v += r0[li] * vi;
+        }
+        r0v = T.sum(r0v);
+        alpha = rho / r0v;
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const int li = i - lo;
+            sv[li] = r[li] - alpha * v[li];
+        }
+        T.sync();
+        double tt = 0.0, ts = 0.0;
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const int li = i - lo;
+            const double ti = spmv_row_team(T, m, sv, i, n, nx);
+            t[li] = ti;
+            tt += ti * ti;
+            ts += ti * sv[li];
+        }
+        T.sum2(tt, ts);
+        om = (tt > 0.0) ? ts / tt : 0.0;
+        double nrr = 0.0, nrho = 0.0;
+        for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
+            const int li = i - lo;
+            x[li] += alpha * p[li] + om * sv[li];
+            double ri = sv[li] - om * t[li];
+            r[li] = ri;
+            nrr += ri * ri;
+            nrho += r0[li] * ri;
+        }
+        T.sum2(nrr, nrho);
+        rr = nrr;
+        rho_new = nrho;
+        it++;
+    }
+    T.sync();
+    for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) x[i - lo] *= m[5 * s + i - lo];
+    T.sync();
+    return it;
+}
+
+} // namespace
+
+__device__ void cmfd_body_cluster(CmfdView c)
+{
+    extern __shared__ __align__(16) double sm[];
+    const int n = c.n_cell, G = c.G, ns = c.n_surf;
+    Team T;
+    T.B.nw = blockDim.x >> 5;
+    T.B.scratch = sm; // 128 doubles
+    T.xch = sm + 128; // 64 doubles
+    T.rank = cl_rank();
+    T.size = cl_nrank();
+    T.slice = (n + (int)T.size - 1) / (int)T.size;
+    T.lo = min(n, (int)T.rank * T.slice);
+    T.hi = min(n, T.lo + T.slice);
+    const int s = T.slice, lo = T.lo, hi = T.hi, bd = blockDim.x, tid = threadIdx.x;
+    // slice vectors: b, x, 6 BiCGSTAB vectors; the current group's operator rows
+    double *b = sm + 192, *x = b + s, *w = x + s, *ms = w + 6 * s;
+    double k = *c.k;
+    if (c.fixup)
+        for (int g = 0; g < G; g++)
+            for (int i = lo + tid; i < hi; i += bd) c.flux[(size_t)g * n + i] = fmax(c.flux[(size_t)g * n + i], 0.0);
+    T.sync();
+
+    // surface coupling coefficients (cmfd.cpp:404-499), surfaces dealt over the cluster
+    for (int idx = (int)T.rank * bd + tid; idx < G * ns; idx += (int)T.size * bd) {
+        int g = idx / ns, is = idx % ns;
+        int c1, c2, nrm;
+        surf_info(c, is, c1, c2, nrm);
+        int lo_bc = (nrm == X_NORM) ? c.bc[WEST] : (nrm == Y_NORM) ? c.bc[SOUTH] : c.bc[BOTTOM];
+        int hi_bc = (nrm == X_NORM) ? c.bc[EAST] : (nrm == Y_NORM) ? c.bc[NORTH] : c.bc[TOP];
+        double d1 = (c1 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c1 * G + g])) / thickness(c, c1, nrm)
+                              : (lo_bc == (int)BoundaryType::VACUUM ? 0.5 / 2.0 : 0.0);
+        double d2 = (c2 > -1) ? (1.0 / (3.0 * c.xstr[(size_t)c2 * G + g])) / thickness(c, c2, nrm)
+                              : (hi_bc == (int)BoundaryType::VACUUM ? 0.5 / 2.0 : 0.0);
+        double dt = 2.0 * d1 * d2 / (d1 + d2);
+        double stil = (d1 > 0.0) ? d1 / (d1 + d2) : d2 / (d1 + d2);
+        double dh = 0.0, sh = 0.0;
+        if (nrm != Z_NORM && c.has_radial) {
+            double j = c.cur[(size_t)g * ns + is];
+            double sfc = c.sflux[(size_t)g * ns + is];
+            double fl = c1 >= 0 ? __ldcg(c.flux + (size_t)g * n + c1) : 0.0;
+            double fr = c2 >= 0 ? __ldcg(c.flux + (size_t)g * n + c2) : 0.0;
+            dh = (j + dt * (fr - fl)) / (fl + fr);
+            if (!isfinite(dh)) dh = 0.0;
+            sh = (c1 >= 0) ? (sfc - stil * fl - (1.0 - stil) * fr) / (fl + fr) : (sfc - stil * fr) / fr;
+        }
+        c.d_tilde[idx] = dt;
+        c.s_tilde[idx] = stil;
+        c.d_hat[idx] = dh;
+        c.s_hat[idx] = sh;
+    }
+    T.sync();
+    // 5-point operator per group (cmfd.cpp:506-544), this CTA's rows
+    for (int g = 0; g < G; g++)
+        for (int i = lo + tid; i < hi; i += bd) {
+            const double *dt = c.d_tilde + (size_t)g * ns;
+            const double *dh = c.d_hat + (size_t)g * ns;
+            double diag = cell_vol(c, i) * c.xsrm[(size_t)i * G + g];
+            const int surfs[6] = {EAST, NORTH, WEST, SOUTH, TOP, BOTTOM};
+            for (int k6 = 0; k6 < 6; k6++) {
+                int sd = surfs[k6];
+                int sf = coarse_surf(c, i, sd);
+                double h = __ldcg(dh + sf);
+                if (sd == WEST || sd == SOUTH || sd == BOTTOM) h = -h;
+                diag += area(c, i, sd) * (__ldcg(dt + sf) + h);
+            }
+            double *m = c.mat + (size_t)g * 6 * n;
+            m[i] = (diag != 0.0) ? diag : 1.0;
+            m[(size_t)5 * n + i] = (diag != 0.0) ? 1.0 / diag : 1.0; // Jacobi preconditioner
+            const int offs[4] = {WEST, EAST, SOUTH, NORTH};
+            for (int q = 0; q < 4; q++) {
+                int sd = offs[q];
+                double v = 0.0;
+                if (neighbor(c, i, sd) >= 0) {
+                    int sf = coarse_surf(c, i, sd);
+                    double h = __ldcg(dh + sf);
+                    if (sd == WEST || sd == SOUTH) h = -h;
+                    v = area(c, i, sd) * (h - __ldcg(dt + sf));
+                }
+                m[(size_t)(q + 1) * n + i] = v;
+            }
+        }
+    T.sync();
+    // column scaling by the neighbour's inverse diagonal (neighbours' rows may be a peer's)
+    for (int g = 0; g < G; g++)
+        for (int i = lo + tid; i < hi; i += bd) {
+            const int ix = i % c.nx;
+            double *m = c.mat + (size_t)g * 6 * n;
+            const double *dinv = m + (size_t)5 * n;
+            if (ix > 0) m[(size_t)n + i] *= __ldcg(dinv + i - 1);
+            if (ix < c.nx - 1) m[(size_t)2 * n + i] *= __ldcg(dinv + i + 1);
+            if (i >= c.nx) m[(size_t)3 * n + i] *= __ldcg(dinv + i - c.nx);
+            if (i + c.nx < n) m[(size_t)4 * n + i] *= __ldcg(dinv + i + c.nx);
+        }
+    T.sync();
+
+    // fission source (own cells) and total fission (own cells' share)
+    auto fis_src = [&](double kk) {
+        for (int i = lo + tid; i < hi; i += bd)
+            c.fs[i] = group_dot(c.xsnf + (size_t)i * G, 1, c.flux + i, n, G, -1) * (1.0 / kk);
+    };
+    auto tot_fis = [&]() {
+        double f = 0.0;
+        for (int i = lo + tid; i < hi; i += bd) f += group_dot(c.xsnf + (size_t)i * G, 1, c.flux + i, n, G, -1);
+        return f;
+    };
+    auto source = [&](int g) {
+        for (int i = lo + tid; i < hi; i += bd) {
+            double sv = c.xsch[(size_t)i * G + g] * c.fs[i];
+            sv += group_dot(c.scat + ((size_t)i * G + g) * G, 1, c.flux + i, n, G, g);
+            b[i - lo] = sv * cell_vol(c, i);
+        }
+    };
+    fis_src(k);
+    double tfis = T.sum(tot_fis());
+    double r0 = 0.0;
+    for (int g = 0; g < G; g++) {
+        source(g);
+        // ||M_g x - b_g||^2 with x the group flux (A_ij = m_ij d_j off the diagonal)
+        const double *m = c.mat + (size_t)g * 6 * n;
+        const double *xg = c.flux + (size_t)g * n;
+        double acc = 0.0;
+        for (int i = lo + tid; i < hi; i += bd) {
+            const int ix = i % c.nx;
+            double v = m[i] * xg[i];
+            if (ix > 0) v += m[n + i] * (__ldcg(m + i - 1) * __ldcg(xg + i - 1));
+            if (ix < c.nx - 1) v += m[2 * n + i] * (__ldcg(m + i + 1) * __ldcg(xg + i + 1));
+            if (i >= c.nx) v += m[3 * n + i] * (__ldcg(m + i - c.nx) * __ldcg(xg + i - c.nx));
+            if (i + c.nx < n) v += m[4 * n + i] * (__ldcg(m + i + c.nx) * __ldcg(xg + i + c.nx));
+            const double d = v - b[i - lo];
+            acc += d * d;
+        }
+        r0 += T.sum(acc);
+    }
+    r0 = sqrt(r0) / (double)(n * G);
+    const double tol = c.resid_reduction * r0;
+
+    int iter = 0, bic_its = 0;
+    double psi_err = 1.0, ri = 0.0, k_old = k;
+    while (true) {
+        iter++;
+        for (int i = lo + tid; i < hi; i += bd) c.fs_old[i] = c.fs[i];
+        fis_src(k);
+        double tfis_old = tfis;
+        ri = 0.0;
+        for (int g = 0; g < G; g++) {
+            const double *mg = c.mat + (size_t)g * 6 * n;
+            double *fg = c.flux + (size_t)g * n;
+            T.sync();
+            for (int q = 0; q < 6; q++)
+                for (int i = lo + tid; i < hi; i += bd) ms[q * s + i - lo] = mg[(size_t)q * n + i];
+            source(g);
+            for (int i = lo + tid; i < hi; i += bd) x[i - lo] = fg[i];
+            T.sync();
+            double rr0 = 0.0;
+            bic_its += bicgstab_team(c, T, ms, b, x, tol, 150, w, rr0);
+            ri += rr0;
+            for (int i = lo + tid; i < hi; i += bd) fg[i] = x[i - lo];
+        }
+        T.sync();
+        ri = sqrt(ri) / (double)(n * G);
+        tfis = T.sum(tot_fis());
+        k_old = k;
+        k = k * tfis / tfis_old;
+        double pe = 0.0;
+        for (int i = lo + tid; i < hi; i += bd) {
+            double e = c.fs[i] - c.fs_old[i];
+            pe += e * e;
+        }
+        psi_err = sqrt(T.sum(pe));
+        if ((fabs(k - k_old) < c.k_tol && psi_err < c.psi_tol && ri / r0 < c.resid_reduction) || iter > c.max_iter)
+            break;
+    }
+    for (int g = 0; g < G; g++)
+        for (int i = lo + tid; i < hi; i += bd)
+            if (c.flux[(size_t)g * n + i] < 0.0) c.flux[(size_t)g * n + i] = -c.flux[(size_t)g * n + i];
+    T.sync();
+    if (T.rank == 0 && tid == 0) {
+        *c.k = k;
+        c.stats[0] = iter;
+        c.stats[1] = r0;
+        c.stats[2] = ri / r0;
+        c.stats[3] = psi_err;
+        c.stats[4] = bic_its;
+        if (!isfinite(k)) atomicOr(c.status, (unsigned)DEV_NAN);
+    }
+}
+
+__global__ void __launch_bounds__(512, 1) kc_cmfd_solve(CmfdView c) { cmfd_body_cluster(c); }
+
 __global__ void __launch_bounds__(512, 1) k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
 
 // One CTA per active solve of a batch; the coarse-current flag and the CMFD
@@ -536,8 +941,55 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
     kb_cmfd_solve<<<b.cap, 32 * nw, smem, s>>>(b, in_smem);
 }
 
+// Meshes above MOCGPU_CMFD_CLUSTER_MIN cells are solved by a cluster of CTAs,
+// one slice of about MOCGPU_CMFD_CLUSTER_CELLS cells each (at most 8 CTAs).
+// Measured on the 17x17 assembly (289 cells): one CTA 188 ms per solve,
+// clusters of 2, 3, 4 and 8 CTAs 228, 195, 198 and 248 ms (the cluster
+// barriers and remote reads outweigh the FP64 work they spread); on the
+// 68x68 mini-core (4624 cells) a cluster of 8 takes the solve from 4.6 s to
+// 1.4 s.
+#ifndef MOCGPU_CMFD_CLUSTER_MIN
+#define MOCGPU_CMFD_CLUSTER_MIN 1024
+#endif
+#ifndef MOCGPU_CMFD_CLUSTER_CELLS
+#define MOCGPU_CMFD_CLUSTER_CELLS 128
+#endif
+constexpr int kClusterCmfdMinCells = MOCGPU_CMFD_CLUSTER_MIN;
+
+static void launch_cmfd_cluster(const CmfdView &c, cudaStream_t s)
+{
+    const int cl = std::max(2, std::min(8, (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
+    const int slice = (c.n_cell + cl - 1) / cl;
+    const int nw = cmfd_warps(slice);
+    const size_t smem = (size_t)(192 + 14 * slice) * sizeof(double);
+    if (smem > 200 * 1024) throw Error(21, "CMFD mesh too large for the cluster solve");
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = smem;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl);
+    cfg.blockDim = dim3(32 * nw);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    note_launch_external();
+    MOCGPU_CUDA(cudaLaunchKernelEx(&cfg, kc_cmfd_solve, c));
+}
+
 void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
 {
+    if (c.n_cell > kClusterCmfdMinCells) {
+        launch_cmfd_cluster(c, s);
+        return;
+    }
     const int nw = cmfd_warps(c.n_cell);
     size_t smem = 0;
     const int in_smem = cmfd_smem_mode(c.n_cell, &smem);

@@ -247,7 +247,6 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         fv.lfsr = blfsr_.p;
         fv.local_fsr = local_fsr_.p;
         fv.bundles_per_unit = tpu / 32;
-        fv.split = 1;
         fv.max_local = L.max_local;
         fv.max_hits = L.max_hits;
         if (precision != 0 && L.max_hits > kMaxTallyHits)

@@ -98,8 +98,7 @@ struct FastView {
     const void *len; // Real [rows][32]
     const uint16_t *lfsr;
     const int *local_fsr;
-    int bundles_per_unit; // warps per CTA = bundles_per_unit * (split ? 2 : 1)
-    int split;            // forward and backward on separate warps
+    int bundles_per_unit; // warps per CTA = 2 * bundles_per_unit (forward and backward on separate warps)
     int max_local;
     int max_hits; // most tally adds on one unit FSR in one group sweep (bounds the fixed-point tally)
 };

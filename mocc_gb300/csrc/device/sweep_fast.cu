@@ -1,16 +1,19 @@
 // Bundled work-unit MoC sweep (the sweep of moc_sweeper_kernel.inc.hpp:36-180,
 // rearranged for the GPU).
 //
-// One CTA per work unit. The unit's FSR cross sections and sources are staged
-// into shared memory as (Sigma_t, qbar) pairs and the unit's FSR tally lives
-// in shared memory (fixed point in the FP32 path, see tally_fixed); one warp
-// sweeps one bundle of 32 tracks in one direction,
-// one track per lane, all polar angles of the azimuth in registers (the
-// forward and the backward pass of a bundle run on two warps). Each warp
-// streams its bundle's segment rows through a double-buffered shared-memory
-// ring with 16-byte cp.async copies, chunk c+1 landing while chunk c is swept.
-// After the bundles, the unit's tally is added to the global FSR tally with
-// one atomic per touched FSR.
+// One CTA per work unit (a few bundles of 32 tracks of one azimuthal set).
+// The unit's FSR cross sections and sources are staged into shared memory as
+// (Sigma_t, qbar) pairs and the unit's FSR tally lives in shared memory
+// (fixed point in the FP32 path, see tally_fixed). One warp sweeps one bundle
+// in one direction, one track per lane, all polar angles of the azimuth in
+// registers (the forward and the backward pass of a bundle run on two warps,
+// each a template instance of its own). Each warp streams its bundle's
+// segment rows through a shared-memory ring with 16-byte cp.async copies,
+// the next chunk landing while the current one is swept. After the bundles,
+// the unit's tally is added to the global FSR tally with one atomic per
+// touched FSR. The single-solve kernel launches one CTA per unit of a phase;
+// the batched kernel is persistent over the (solve, unit) items of all
+// active solves.
 #include <algorithm>
 #include <climits>
 
@@ -130,7 +133,7 @@ template <typename Real> __host__ __device__ constexpr size_t ring_bytes()
 // the same FSR in the same row; even and odd lanes therefore add into two
 // copies of the tally (summed when the unit ends). Padding lanes carry a zero
 // contribution and skip the add.
-template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc, int)
+template <typename Real> __device__ __forceinline__ void tally_add(Real *s_tal, int l, Real acc)
 {
     if (acc != (Real)0) atomicAdd(s_tal + l, acc);
 }
@@ -340,7 +343,7 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
                 psi[p] -= d;
                 acc += d * U.wt[p];
             }
-            tally_add(U.s_tal, l, acc, lane);
+            tally_add(U.s_tal, l, acc);
         }
     };
 

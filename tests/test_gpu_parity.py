@@ -126,6 +126,29 @@ def test_cmfd_solve_fp64():
     assert np.allclose(S.flux(), O.flux(), rtol=1e-8)
 
 
+def test_cmfd_solve_cluster_fp64():
+    # 36x36 pin mesh (1296 cells): the single-solve CMFD runs on a cluster of
+    # CTAs, each with a slice of the cells
+    xml, xsl = W.minicore(n_lat=9, n_azi=2, spacing=0.1, precision="double")
+    P, S, O = _pair(xml, xsl, 0)
+    assert P.sizes["npin"] > 1024
+    S.initialize()
+    O.initialize()
+    S.set_coarse_data(True)
+    O.set_coarse_data(True)
+    fs = O.calc_fission_source(1.0)
+    S.set_fission_source(fs)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        O.source_group(g)
+        S.sweep(g)
+        O.sweep(g)
+    ka = S.cmfd_solve(1.0)
+    kb = O.cmfd_solve(1.0)
+    assert abs(ka - kb) / kb < 1e-9
+    assert np.allclose(S.flux(), O.flux(), rtol=1e-8)
+
+
 @pytest.mark.parametrize("kernel", [0, 1])
 @pytest.mark.parametrize("gs", [1, 0])
 def test_eigen_fp64_matches_oracle(kernel, gs):
