@@ -947,26 +947,39 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
 // clusters of 2, 3, 4 and 8 CTAs 228, 195, 198 and 248 ms (the cluster
 // barriers and remote reads outweigh the FP64 work they spread); on the
 // 68x68 mini-core (4624 cells) a cluster of 8 takes the solve from 4.6 s to
-// 1.4 s.
+// 1.4 s (16 CTAs: 1.36 s; 1, 2, 8 or 16 warps per CTA instead of 4: 2.9,
+// 2.0, 1.7 and 3.2 s).
 #ifndef MOCGPU_CMFD_CLUSTER_MIN
 #define MOCGPU_CMFD_CLUSTER_MIN 1024
 #endif
 #ifndef MOCGPU_CMFD_CLUSTER_CELLS
 #define MOCGPU_CMFD_CLUSTER_CELLS 128
 #endif
+#ifndef MOCGPU_CMFD_CLUSTER_MAX
+#define MOCGPU_CMFD_CLUSTER_MAX 8 // CTAs per cluster; above 8 needs the non-portable cluster size
+#endif
+#ifndef MOCGPU_CMFD_CLUSTER_WARPS
+#define MOCGPU_CMFD_CLUSTER_WARPS 0 // warps per CTA, 0: from the slice size
+#endif
 constexpr int kClusterCmfdMinCells = MOCGPU_CMFD_CLUSTER_MIN;
 
 static void launch_cmfd_cluster(const CmfdView &c, cudaStream_t s)
 {
-    const int cl = std::max(2, std::min(8, (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
+    const int cl = std::max(2, std::min(MOCGPU_CMFD_CLUSTER_MAX,
+                                        (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
     const int slice = (c.n_cell + cl - 1) / cl;
-    const int nw = cmfd_warps(slice);
+    const int nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cmfd_warps(slice);
     const size_t smem = (size_t)(192 + 14 * slice) * sizeof(double);
     if (smem > 200 * 1024) throw Error(21, "CMFD mesh too large for the cluster solve");
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = smem;
+    }
+    static bool nonportable = false;
+    if (cl > 8 && !nonportable) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        nonportable = true;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cl);
