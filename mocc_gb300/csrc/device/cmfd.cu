@@ -2,10 +2,13 @@
 // the 5-point operator per group, then the CMFD power iteration with one
 // preconditioned BiCGSTAB solve per group.
 //
-// One CTA runs a whole CMFD solve. Tiny meshes (up to 64 cells) run on a
+// One CTA runs a whole CMFD solve (cmfd_body: every solve of a batch, and
+// single solves up to 1024 cells). Tiny meshes (up to 64 cells) run on a
 // single warp, so every reduction is a shuffle tree and every barrier a warp
 // barrier; larger meshes use 4 to 16 warps with one block barrier per
-// reduction. Work vectors live in shared memory when they fit.
+// reduction. Work vectors live in shared memory when they fit. A single
+// solve of a larger mesh runs on a thread-block cluster instead
+// (cmfd_body_cluster, below).
 #include <algorithm>
 #include <mutex>
 #include <string>
