@@ -161,9 +161,11 @@ __device__ __forceinline__ void tally_fixed(int *s_hi, unsigned *s_lo, float *ta
                                             float xs)
 {
     if (fabsf(xs) >= 0x1p23f) {
-        const long long v = __float2ll_rn(xs); // exact: 2^23 <= |xs| < 2^50 is an integer
-        atomicAdd(s_hi + l, (int)(v >> 20));
-        atomicAdd(s_lo + l, (unsigned)v & 0xFFFFFu);
+        // 2^23 <= |xs| < 2^50 is an integer: the split is exact, in FP32 and
+        // 32-bit conversions (a 64-bit conversion would run on the FP64 pipe)
+        const float hf = floorf(xs * 0x1p-20f);
+        atomicAdd(s_hi + l, (int)hf);
+        atomicAdd(s_lo + l, (unsigned)(int)fmaf(hf, -0x1p20f, xs));
     } else if (xs != 0.f) {
         atomicAdd(tally + lf[l], xs * inv); // below 2^23 units (rare): straight to the FSR's FP32 tally
     }
