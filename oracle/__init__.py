@@ -83,7 +83,7 @@ def load():
             ("orc_flux_residual", I, [V, DP]), ("orc_get_flux", I, [V, DP]), ("orc_set_flux", I, [V, DP]),
             ("orc_get_pin_flux_1g", I, [V, I, DP]), ("orc_set_pin_flux_1g", I, [V, I, DP, DP]),
             ("orc_pin_powers", I, [V, DP]), ("orc_get_coarse_currents", I, [V, DP, DP]),
-            ("orc_cmfd_solve", I, [V, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
+            ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_table_exp", D, [D]),
         ]:
             fn = getattr(lib, name)
@@ -208,6 +208,12 @@ class OracleSolver:
         sfl = np.empty((self.n_group, self.n_surf))
         _chk(self._lib.orc_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
         return cur, sfl
+
+    def homogenized_nu_fission(self):
+        """Pin-homogenised nu-Sigma_f of the current flux, [n_pin (FSR order)][G]."""
+        out = np.empty((self.n_pin, self.n_group))
+        _chk(self._lib.orc_homogenized_nu_fission(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def cmfd_solve(self, k):
         kk = C.c_double(k)

@@ -961,6 +961,16 @@ int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux)
             }
     });
 }
+int orc_homogenized_nu_fission(orc_solver *s, double *out)
+{
+    return guard([&] {
+        // pin-homogenised nu-Sigma_f of the current flux, [n_pin in FSR order][G]
+        s->homogenize();
+        for (int ip = 0; ip < s->p.n_pin; ip++)
+            for (int g = 0; g < s->G; g++)
+                out[(size_t)ip * s->G + g] = s->hxsnf[(size_t)s->p.pin_cell[ip] * s->G + g];
+    });
+}
 int orc_cmfd_solve(orc_solver *s, double *k)
 {
     return guard([&] { s->do_cmfd(*k); });

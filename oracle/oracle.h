@@ -96,6 +96,9 @@ int orc_get_pin_flux_1g(orc_solver *s, int g, double *out);
 int orc_set_pin_flux_1g(orc_solver *s, int g, const double *in, double *resid);
 int orc_pin_powers(orc_solver *s, double *out);
 int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux);
+/* XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363) of the current
+ * flux; writes the pins' nu-Sigma_f, [n_pin, in FSR order][G] */
+int orc_homogenized_nu_fission(orc_solver *s, double *out);
 int orc_cmfd_solve(orc_solver *s, double *k);
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out);
 /* exponential table check: value of MOCC's table exponential at x */

@@ -5,6 +5,8 @@ Reads (as text) the reference test sources and their geometry inputs:
                                            simple_ray / big_ray coarse data
   src/sweepers/moc/tests/6x5.xml, large.xml, square.xml (geometries)
   src/sweepers/moc/tests/test_RayData.cpp  volume-conservation test setup
+  src/core/tests/test_XSMeshHomogenized.cpp, 2x3_1.xml, 2x3_2.xml
+                                           pin-homogenised nu-Sigma_f
 and writes tests/golden/reference_known_answers.json. Material libraries are
 not copied: the tests attach a synthetic library under the same names.
 
@@ -55,6 +57,18 @@ def main(root):
     assert "0.1764 * 4.0 * PI" in rd and 'order=\\"4\\"' in rd and 'spacing=\\"0.01\\"' in rd
     out["raydata_volume"] = {"ang_quad": '<ang_quad type="ls" order="4" />', "spacing": 0.01,
                              "area_4pi": 0.1764, "tol": 1e-14}
+    # XSMeshHomogenized: pin-homogenised nu-Sigma_f (group 1) of the 2x3
+    # UO2/MOX lattice and of solid UO2 pins (src/core/tests)
+    ct = Path(root) / "src/core/tests"
+    hom = (ct / "test_XSMeshHomogenized.cpp").read_text()
+    body = hom[hom.index("for (int ilat = 0; ilat < 96; ilat++)"):]
+    body = body[:body.index("}")]
+    pattern = [float(v) for v in re.findall(r"CHECK_CLOSE\(([0-9.eE+-]+), xs_mesh\[ilat \* 6 \+ \d\]", body)]
+    solid = float(re.search(r"CHECK_CLOSE\(([0-9.eE+-]+), xs_mesh\[i\]\.xsmacnf\(0\)", hom).group(1))
+    assert len(pattern) == 6
+    out["xsmesh_homogenized"] = {"lattice_xml": (ct / "2x3_2.xml").read_text(),
+                                 "solid_xml": (ct / "2x3_1.xml").read_text(),
+                                 "nu_fission_pattern": pattern, "solid_uo2_nu_fission": solid, "tol": 1e-6}
     dst = Path(__file__).resolve().parent / "reference_known_answers.json"
     dst.write_text(json.dumps(out, indent=1))
     print("wrote", dst)

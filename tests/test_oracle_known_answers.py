@@ -173,3 +173,42 @@ def test_vacuum_core_with_corner_crossings_converges():
     r0 = oracle.OracleSolver(P, cmfd=0).solve()
     assert r["converged"] and r["iterations"] < 20
     assert abs(r["k"] - r0["k"]) / r0["k"] < 2e-5  # CMFD accelerates, it does not move k
+
+
+def test_homogenized_nu_fission_xsmesh_known_answers(golden, ref_xsl):
+    """test_XSMeshHomogenized.cpp: pin-homogenised nu-Sigma_f of a 2x3 lattice
+    of UO2 and MOX pins (cylindrical fuel in moderator) and of solid UO2 pins,
+    volume-weighted (flat flux). The reference's values are for the C5G7
+    library: 0.0115752 for a UO2 pin against 2.005998e-2 for solid UO2 gives
+    the fuel's area fraction, which holds for any library; each lattice's pins
+    take the reference's MOX/UO2 pattern."""
+    h = golden["xsmesh_homogenized"]
+    solver = ('<solver type="eigenvalue" k_tol="1e-6" psi_tol="1e-5" max_iter="10"><sweeper type="moc" n_inner="1">'
+              '<ang_quad type="ls" order="4" /><rays spacing="0.05" /></sweeper></solver>')
+    # MOX with a larger nu-Sigma_f than UO2, as in C5G7
+    ref_xsl = (m.synthetic_xsl(1, 7, 2, fuel_nf_scale=[1.0, 1.3]).replace("fuel1", "UO2-3.3")
+               .replace("fuel2", "MOX-4.3").replace("moderator", "Moderator"))
+    pat = h["nu_fission_pattern"]
+    frac_ref = min(pat) / h["solid_uo2_nu_fission"]
+    for key, solid in (("lattice_xml", False), ("solid_xml", True)):
+        P = m.Problem(solver + h[key], ref_xsl)
+        O = oracle.OracleSolver(P)
+        O.initialize()  # flat flux: volume weighting
+        hom = O.homogenized_nu_fission()[:, 0]
+        G = P.sizes["ngroup"]
+        xsnf = P.export("xsnf").reshape(-1, G)[:, 0]
+        first = P.export("pin_first_reg")[:-1]
+        fuel_nf = xsnf[P.export("fsr_mat")[first]]
+        assert P.sizes["npin"] == 72 and np.all(fuel_nf > 0)
+        if solid:
+            assert np.allclose(hom, fuel_nf, rtol=1e-12)
+            continue
+        assert np.allclose(hom / fuel_nf, frac_ref, rtol=1e-4)
+        # the reference lists each 2x3 lattice's pins row by row from the
+        # bottom; here pins are located by their coarse cell (x fastest)
+        nx = P.sizes["nx"]
+        cell = P.export("pin_cell")
+        j = (cell // nx % 3) * 2 + (cell % nx % 2)
+        mox = np.array(pat)[j] == max(pat)
+        assert 0 < mox.sum() < mox.size
+        assert np.ptp(hom[mox]) < 1e-12 and np.ptp(hom[~mox]) < 1e-12 and hom[mox][0] > hom[~mox][0]
