@@ -158,6 +158,14 @@ int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in /* [n_
 int mocgpu_pin_powers(mocgpu_sweeper *s, double *out);
 /* CoarseData current and surface flux after the last current sweep, [G][n_surf] */
 int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux);
+/* TransportSweeper::get_homogenized_xsmesh (transport_sweeper.hpp:184) with
+ * XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363): homogenises
+ * the current flux on the device, one region per pin, and copies out the
+ * transport, nu-fission, fission, chi and removal cross sections
+ * [n_pin][G] and the scattering matrix [n_pin][G (to)][G (from)], pins in
+ * coarse-cell order (x fastest). Any output pointer may be NULL. */
+int mocgpu_homogenized_xs(mocgpu_sweeper *s, double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm,
+                          double *scat);
 /* EigenSolver::do_cmfd (eigen_solver.cpp:263-291) incl. CMFD::solve
  * (cmfd.cpp:171-279); k is read and updated */
 int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);

@@ -118,6 +118,7 @@ def load_library(build: bool = True):
         "mocgpu_set_pin_flux_1g": (I, [P, I, DP, DP]),
         "mocgpu_pin_powers": (I, [P, DP]),
         "mocgpu_get_coarse_currents": (I, [P, DP, DP]),
+        "mocgpu_homogenized_xs": (I, [P, DP, DP, DP, DP, DP, DP]),
         "mocgpu_cmfd_solve": (I, [P, DP]),
         "mocgpu_eigen_solve": (I, [P, I, C.POINTER(_Result)]),
         "mocgpu_sweeper_bytes": (I, [P, I64P, DP]),
@@ -363,6 +364,17 @@ class MoCSweeper:
         sfl = np.empty((self.n_group, self.n_surf))
         _check(self._lib.mocgpu_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
         return cur, sfl
+
+    def homogenized_xs(self) -> dict:
+        """Pin-homogenised cross sections of the current flux (MOCC's
+        get_homogenized_xsmesh): xstr, xsnf, xsf, xsch, xsrm [n_pin][G] and
+        scat [n_pin][G (to)][G (from)], pins in coarse-cell order."""
+        shp = (self.n_pin, self.n_group)
+        out = {k: np.empty(shp) for k in ("xstr", "xsnf", "xsf", "xsch", "xsrm")}
+        out["scat"] = np.empty(shp + (self.n_group,))
+        _check(self._lib.mocgpu_homogenized_xs(self._h, *(_dp(out[k]) for k in
+                                                          ("xstr", "xsnf", "xsf", "xsch", "xsrm", "scat"))))
+        return out
 
     def cmfd_solve(self, k: float) -> float:
         kk = C.c_double(k)

@@ -460,6 +460,11 @@ int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surfa
         sw(s).get_currents(current, surface_flux);
     });
 }
+int mocgpu_homogenized_xs(mocgpu_sweeper *s, double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm,
+                          double *scat)
+{
+    return guarded([&] { sw(s).homogenized_xs(xstr, xsnf, xsf, xsch, xsrm, scat); });
+}
 int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k)
 {
     return guarded([&] {

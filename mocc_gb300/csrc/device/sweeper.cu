@@ -440,6 +440,20 @@ void Sweeper::get_currents(double *cur, double *sfl) const
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
 }
 
+// XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363) of the current
+// flux, copied out per pin (coarse-cell order)
+void Sweeper::homogenized_xs(double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm, double *scat)
+{
+    launch_homogenize(gv_, phi_.p, cv_, stream_);
+    const size_t n = (size_t)cv_.n_cell * cv_.G * sizeof(double);
+    const double *src[5] = {cv_.xstr, cv_.xsnf, cv_.xsf, cv_.xsch, cv_.xsrm};
+    double *dst[5] = {xstr, xsnf, xsf, xsch, xsrm};
+    for (int i = 0; i < 5; i++)
+        if (dst[i]) MOCGPU_CUDA(copy_async(dst[i], src[i], n, cudaMemcpyDeviceToHost, stream_));
+    if (scat) MOCGPU_CUDA(copy_async(scat, cv_.scat, n * cv_.G, cudaMemcpyDeviceToHost, stream_));
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
 // EigenSolver::do_cmfd (eigen_solver.cpp:263-291): coarse flux from the
 // fine flux, homogenise, CMFD solve, then rescale the fine flux.
 void Sweeper::cmfd_solve(double &k)

@@ -67,6 +67,8 @@ class Sweeper {
     double set_pin_flux(int g, const double *in);
     void pin_powers(double *out) const; // [ny][nx], normalised to n_fuel
     void get_currents(double *cur, double *sflux) const;
+    // pin-homogenised cross sections of the current flux, [n_pin][G] and [n_pin][G][G]
+    void homogenized_xs(double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm, double *scat);
     void set_coarse_enabled(bool on) { coarse_enabled_ = on; }
     bool coarse_enabled() const { return coarse_enabled_; }
     bool has_radial() const { return has_radial_; }

@@ -126,6 +126,26 @@ def test_cmfd_solve_fp64():
     assert np.allclose(S.flux(), O.flux(), rtol=1e-8)
 
 
+def test_homogenized_xs_matches_oracle():
+    # get_homogenized_xsmesh: the device homogenisation of a non-flat flux
+    P, S, O = _pair(*W.pin3x3(), 0)
+    S.initialize()
+    O.initialize()
+    fs = O.calc_fission_source(1.0)
+    S.set_fission_source(fs)
+    for g in range(P.sizes["ngroup"]):
+        S.source_group(g)
+        O.source_group(g)
+        S.sweep(g)
+        O.sweep(g)
+    h = S.homogenized_xs()
+    ref = O.homogenized_nu_fission()  # pins in FSR order
+    cell = P.export("pin_cell")
+    assert np.allclose(h["xsnf"][cell], ref, rtol=1e-12, atol=0)
+    assert np.all(h["xstr"] > 0) and np.all(h["xsrm"] <= h["xstr"])
+    assert np.allclose(h["xsrm"], h["xstr"] - np.einsum("pgg->pg", h["scat"]), rtol=1e-12)
+
+
 def test_cmfd_solve_cluster_fp64():
     # 36x36 pin mesh (1296 cells): the single-solve CMFD runs on a cluster of
     # CTAs, each with a slice of the cells
