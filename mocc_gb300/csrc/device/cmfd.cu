@@ -342,8 +342,9 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     const int n = c.n_cell, G = c.G, ns = c.n_surf;
     // work vectors: b, x (group flux copy), 8 BiCGSTAB vectors
     double *vec = vec_in_smem ? sm + 128 : c.vec;
-    // mode 2: the current group's operator is also staged in shared memory
-    double *ms = (vec_in_smem == 2) ? sm + 128 + 10 * n : nullptr;
+    // mode 2: the current group's operator is also staged in shared memory;
+    // mode 3: every group's operator, staged once after it is built
+    double *ms = (vec_in_smem >= 2) ? sm + 128 + 10 * n : nullptr;
     double *b = vec, *x = vec + n, *w = vec + 2 * n;
     double k = *c.k;
     if (c.fixup)
@@ -421,6 +422,8 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
         if (i + c.nx < n) m[(size_t)4 * n + i] *= dinv[i + c.nx];
     }
     B.sync();
+    if (vec_in_smem == 3)
+        for (int i = threadIdx.x; i < 6 * n * G; i += blockDim.x) ms[i] = c.mat[i];
 
     fission_source(c, k);
     B.sync();
@@ -447,7 +450,9 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             const double *m = c.mat + (size_t)g * 6 * n;
             double *fg = c.flux + (size_t)g * n;
             B.sync();
-            if (ms) {
+            if (vec_in_smem == 3) {
+                m = ms + (size_t)g * 6 * n;
+            } else if (ms) {
                 for (int i = threadIdx.x; i < 6 * n; i += blockDim.x) ms[i] = m[i];
                 m = ms;
             }
@@ -918,12 +923,18 @@ static int cmfd_warps(int n_cell)
     return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
 
-// Shared-memory mode of a CMFD CTA: 2 = work vectors and the current group's
+// Shared-memory mode of a CMFD CTA: 3 = work vectors and every group's
+// operator (only when `all_groups` > 0 groups are asked for: a single solve,
+// whose CTA has its SM to itself), 2 = work vectors and the current group's
 // operator, 1 = work vectors only, 0 = nothing (vectors in global memory).
-static int cmfd_smem_mode(int n_cell, size_t *bytes)
+static int cmfd_smem_mode(int n_cell, size_t *bytes, int all_groups = 0)
 {
     const size_t base = 128 * sizeof(double), lim = 200 * 1024;
     const size_t vec = (size_t)10 * n_cell * sizeof(double), op = (size_t)6 * n_cell * sizeof(double);
+    if (all_groups > 0 && base + vec + op * all_groups <= lim) {
+        *bytes = base + vec + op * all_groups;
+        return 3;
+    }
     int mode = (base + vec + op <= lim) ? 2 : (base + vec <= lim) ? 1 : 0;
     *bytes = base + (mode >= 1 ? vec : 0) + (mode == 2 ? op : 0);
     return mode;
@@ -1008,7 +1019,7 @@ void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
     }
     const int nw = cmfd_warps(c.n_cell);
     size_t smem = 0;
-    const int in_smem = cmfd_smem_mode(c.n_cell, &smem);
+    const int in_smem = cmfd_smem_mode(c.n_cell, &smem, c.G);
     static size_t configured = 0;
     if (smem > 48 * 1024 && smem > configured) {
         MOCGPU_CUDA(cudaFuncSetAttribute(k_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
