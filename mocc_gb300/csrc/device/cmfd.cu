@@ -707,7 +707,7 @@ __device__ int bicgstab_team(const CmfdView &c, Team &T, const double *m, const 
 
 } // namespace
 
-__device__ void cmfd_body_cluster(CmfdView c)
+__device__ void cmfd_body_cluster(CmfdView c, int all_groups)
 {
     extern __shared__ __align__(16) double sm[];
     const int n = c.n_cell, G = c.G, ns = c.n_surf;
@@ -722,6 +722,7 @@ __device__ void cmfd_body_cluster(CmfdView c)
     T.hi = min(n, T.lo + T.slice);
     const int s = T.slice, lo = T.lo, hi = T.hi, bd = blockDim.x, tid = threadIdx.x;
     // slice vectors: b, x, 6 BiCGSTAB vectors; the current group's operator rows
+    // ms: the current group's rows, or with all_groups every group's rows [G][6][slice]
     double *b = sm + 192, *x = b + s, *w = x + s, *ms = w + 6 * s;
     double k = *c.k;
     if (c.fixup)
@@ -801,6 +802,11 @@ __device__ void cmfd_body_cluster(CmfdView c)
             if (i + c.nx < n) m[(size_t)4 * n + i] *= __ldcg(dinv + i + c.nx);
         }
     T.sync();
+    if (all_groups)
+        for (int g = 0; g < G; g++)
+            for (int q = 0; q < 6; q++)
+                for (int i = lo + tid; i < hi; i += bd)
+                    ms[((size_t)g * 6 + q) * s + i - lo] = c.mat[((size_t)g * 6 + q) * n + i];
 
     // fission source (own cells) and total fission (own cells' share)
     auto fis_src = [&](double kk) {
@@ -855,13 +861,15 @@ __device__ void cmfd_body_cluster(CmfdView c)
             const double *mg = c.mat + (size_t)g * 6 * n;
             double *fg = c.flux + (size_t)g * n;
             T.sync();
-            for (int q = 0; q < 6; q++)
-                for (int i = lo + tid; i < hi; i += bd) ms[q * s + i - lo] = mg[(size_t)q * n + i];
+            const double *mrows = ms + (all_groups ? (size_t)g * 6 * s : 0);
+            if (!all_groups)
+                for (int q = 0; q < 6; q++)
+                    for (int i = lo + tid; i < hi; i += bd) ms[q * s + i - lo] = mg[(size_t)q * n + i];
             source(g);
             for (int i = lo + tid; i < hi; i += bd) x[i - lo] = fg[i];
             T.sync();
             double rr0 = 0.0;
-            bic_its += bicgstab_team(c, T, ms, b, x, tol, 150, w, rr0);
+            bic_its += bicgstab_team(c, T, mrows, b, x, tol, 150, w, rr0);
             ri += rr0;
             for (int i = lo + tid; i < hi; i += bd) fg[i] = x[i - lo];
         }
@@ -894,7 +902,10 @@ __device__ void cmfd_body_cluster(CmfdView c)
     }
 }
 
-__global__ void __launch_bounds__(512, 1) kc_cmfd_solve(CmfdView c) { cmfd_body_cluster(c); }
+__global__ void __launch_bounds__(512, 1) kc_cmfd_solve(CmfdView c, int all_groups)
+{
+    cmfd_body_cluster(c, all_groups);
+}
 
 __global__ void __launch_bounds__(512, 1) k_cmfd_solve(CmfdView c, int vec_in_smem) { cmfd_body(c, vec_in_smem); }
 
@@ -961,8 +972,8 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
 // clusters of 2, 3, 4 and 8 CTAs 228, 195, 198 and 248 ms (the cluster
 // barriers and remote reads outweigh the FP64 work they spread); on the
 // 68x68 mini-core (4624 cells) a cluster of 8 takes the solve from 4.6 s to
-// 1.4 s (16 CTAs: 1.36 s; 1, 2, 8 or 16 warps per CTA instead of 4: 2.9,
-// 2.0, 1.7 and 3.2 s).
+// 1.40 s, 16 CTAs with every group's operator rows in shared memory to
+// 1.35 s (1, 2, 8 or 16 warps per CTA instead of 4: 2.9, 2.0, 1.7 and 3.2 s).
 #ifndef MOCGPU_CMFD_CLUSTER_MIN
 #define MOCGPU_CMFD_CLUSTER_MIN 1024
 #endif
@@ -970,45 +981,71 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
 #define MOCGPU_CMFD_CLUSTER_CELLS 128
 #endif
 #ifndef MOCGPU_CMFD_CLUSTER_MAX
-#define MOCGPU_CMFD_CLUSTER_MAX 8 // CTAs per cluster; above 8 needs the non-portable cluster size
+#define MOCGPU_CMFD_CLUSTER_MAX 16 // CTAs per cluster; above 8 is a non-portable size, checked per launch
 #endif
 #ifndef MOCGPU_CMFD_CLUSTER_WARPS
 #define MOCGPU_CMFD_CLUSTER_WARPS 0 // warps per CTA, 0: from the slice size
 #endif
 constexpr int kClusterCmfdMinCells = MOCGPU_CMFD_CLUSTER_MIN;
 
-static void launch_cmfd_cluster(const CmfdView &c, cudaStream_t s)
+// Cluster shape of a mesh: CTAs, warps per CTA, shared bytes, and whether
+// every group's operator rows fit in shared memory.
+struct ClusterShape {
+    int cl, nw, all_groups;
+    size_t smem;
+};
+static ClusterShape cluster_shape(const CmfdView &c, int max_cl)
 {
-    const int cl = std::max(2, std::min(MOCGPU_CMFD_CLUSTER_MAX,
-                                        (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
-    const int slice = (c.n_cell + cl - 1) / cl;
-    const int nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cmfd_warps(slice);
-    const size_t smem = (size_t)(192 + 14 * slice) * sizeof(double);
-    if (smem > 200 * 1024) throw Error(21, "CMFD mesh too large for the cluster solve");
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
-    static bool nonportable = false;
-    if (cl > 8 && !nonportable) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        nonportable = true;
-    }
+    ClusterShape sh;
+    sh.cl = std::max(2, std::min(max_cl, (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
+    const int slice = (c.n_cell + sh.cl - 1) / sh.cl;
+    sh.nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cmfd_warps(slice);
+    const size_t lim = 200 * 1024, all = (size_t)(192 + 8 * slice + 6 * c.G * slice) * sizeof(double);
+    sh.all_groups = all <= lim ? 1 : 0;
+    sh.smem = sh.all_groups ? all : (size_t)(192 + 14 * slice) * sizeof(double);
+    return sh;
+}
+
+static cudaLaunchConfig_t cluster_config(const ClusterShape &sh, cudaStream_t s, cudaLaunchAttribute *attr)
+{
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cl);
-    cfg.blockDim = dim3(32 * nw);
-    cfg.dynamicSmemBytes = smem;
+    cfg.gridDim = dim3(sh.cl);
+    cfg.blockDim = dim3(32 * sh.nw);
+    cfg.dynamicSmemBytes = sh.smem;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.x = sh.cl;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    return cfg;
+}
+
+static void launch_cmfd_cluster(const CmfdView &c, cudaStream_t s)
+{
+    static bool attrs_set = false;
+    if (!attrs_set) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (MOCGPU_CMFD_CLUSTER_MAX > 8)
+            MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        attrs_set = true;
+    }
+    ClusterShape sh = cluster_shape(c, MOCGPU_CMFD_CLUSTER_MAX);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = cluster_config(sh, s, attr);
+    if (sh.cl > 8) {
+        // a cluster above the portable 8 CTAs only where this GPU can place one
+        int fits = 0;
+        if (cudaOccupancyMaxActiveClusters(&fits, kc_cmfd_solve, &cfg) != cudaSuccess || fits < 1) {
+            (void)cudaGetLastError();
+            sh = cluster_shape(c, 8);
+            cfg = cluster_config(sh, s, attr);
+        }
+    }
+    if (sh.smem > 200 * 1024) throw Error(21, "CMFD mesh too large for the cluster solve");
     note_launch_external();
-    MOCGPU_CUDA(cudaLaunchKernelEx(&cfg, kc_cmfd_solve, c));
+    MOCGPU_CUDA(cudaLaunchKernelEx(&cfg, kc_cmfd_solve, c, sh.all_groups));
 }
 
 void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
