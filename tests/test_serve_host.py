@@ -1,0 +1,122 @@
+"""Host logic of the request loop and the autotuner, on CPU with a stand-in
+engine: requests are submitted only once their arrival time has passed,
+every result comes back to the request that asked for it, lanes that are
+still busy do not block the others, and the autotuner keeps the work-unit
+shape with the least device time per solve."""
+import time
+
+from mocc_gb300.serve import Request, poisson_arrivals, run_batch, serve
+from mocc_gb300.tune import tune_bundles_per_unit
+
+
+class FakeEngine:
+    """The BatchEngine calls serve() makes: each solve needs `outers` outer
+    iterations; an iteration launched with launch() completes after
+    `poll_delay` polls."""
+
+    def __init__(self, outers=3, poll_delay=2, t0=None, replay_ms=1.0):
+        self.outers, self.poll_delay, self.replay_ms = outers, poll_delay, replay_ms
+        self.t0 = t0 if t0 is not None else time.perf_counter()
+        self.next_id, self.active, self.done, self.taken = 0, {}, {}, set()
+        self.submits, self.in_flight, self.polls, self.replays, self.closed = [], False, 0, 0, False
+
+    def submit(self, problem, xsl=None):
+        i = self.next_id
+        self.next_id += 1
+        self.active[i] = (problem, xsl, 0)
+        self.submits.append((problem, time.perf_counter() - self.t0))
+        return i
+
+    def launch(self):
+        assert not self.in_flight
+        self.in_flight, self.polls = True, 0
+
+    def poll(self):
+        self.polls += 1
+        return self.polls >= self.poll_delay
+
+    def finish(self):
+        assert self.in_flight
+        self.in_flight = False
+        self.replays += 1
+        for i, (p, x, n) in list(self.active.items()):
+            if n + 1 >= self.outers:
+                del self.active[i]
+                self.done[i] = (p, x)
+            else:
+                self.active[i] = (p, x, n + 1)
+
+    def step(self):
+        self.launch()
+        self.polls = self.poll_delay
+        self.finish()
+        return len(self.active)
+
+    def run(self):
+        while self.active:
+            self.step()
+
+    def ready(self):
+        return [i for i in self.done if i not in self.taken]
+
+    def take(self, i, n_pin_max=0):
+        if i not in self.done or i in self.taken:
+            return None
+        self.taken.add(i)
+        p, x = self.done[i]
+        return {"id": i, "error": 0, "problem": p, "xsl": x, "converged": 1}
+
+    def stats(self):
+        return {"replay_ms": self.replays * self.replay_ms}
+
+    def close(self):
+        self.closed = True
+
+
+def test_requests_wait_for_arrival_and_results_match_requests():
+    t0 = time.perf_counter()
+    lanes = {"a": FakeEngine(outers=3, t0=t0), "b": FakeEngine(outers=5, poll_delay=4, t0=t0)}
+    arr = poisson_arrivals(40, rate=2000.0, seed=3)
+    reqs = [Request(problem=("p", i), xsl=f"x{i}", arrival=float(a), lane="a" if i % 3 else "b")
+            for i, a in enumerate(arr)]
+    rep = serve(lanes, reqs)
+    assert rep.n == 40 and len(rep.results) == 40
+    for i, r in enumerate(rep.results):
+        assert r["problem"] == ("p", i) and r["xsl"] == f"x{i}"
+    assert all(lat >= 0.0 for lat in rep.latencies_s)
+    # no request reached an engine before it arrived
+    arrival = {("p", i): a for i, a in enumerate(arr)}
+    for eng in lanes.values():
+        for prob, t in eng.submits:
+            assert t >= arrival[prob] - 1e-6
+    assert sorted(len(e.submits) for e in lanes.values()) == [14, 26]
+
+
+def test_busy_lane_does_not_block_the_other():
+    # lane "slow" needs many polls per iteration; lane "fast" finishes its
+    # solves while "slow" is still on its first iterations
+    slow, fast = FakeEngine(outers=4, poll_delay=50), FakeEngine(outers=2, poll_delay=1)
+    reqs = [Request(("s", 0), None, 0.0, "slow")] + [Request(("f", i), None, 0.0, "fast") for i in range(5)]
+    rep = serve({"slow": slow, "fast": fast}, reqs)
+    assert all(r is not None for r in rep.results)
+    assert max(rep.latencies_s[1:]) <= rep.latencies_s[0]
+    assert fast.replays >= 2 and slow.replays == 4
+
+
+def test_run_batch_single_engine_returns_job_order():
+    eng = FakeEngine(outers=2)
+    res = run_batch(eng, [(("j", i), None, 0) for i in range(7)])
+    assert [r["problem"] for r in res] == [("j", i) for i in range(7)]
+
+
+def test_autotuner_keeps_the_fastest_shape():
+    made = {}
+
+    def make(bpu):
+        made[bpu] = FakeEngine(outers=2, replay_ms={1: 3.0, 2: 1.0, 4: 2.0}[bpu])
+        return made[bpu]
+
+    out = tune_bundles_per_unit(make, [(("s", i), None) for i in range(4)])
+    assert out["best"] == 2
+    assert set(out["ms_per_solve"]) == {1, 2, 4}
+    assert all(e.closed for e in made.values())
