@@ -453,7 +453,17 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
             if (vec_in_smem == 3) {
                 m = ms + (size_t)g * 6 * n;
             } else if (ms) {
-                for (int i = threadIdx.x; i < 6 * n; i += blockDim.x) ms[i] = m[i];
+                // 16-byte asynchronous copies, all in flight at once (a loop
+                // of loads and stores waits out one memory latency per pass);
+                // both arrays start 16-byte aligned and 6n doubles are whole
+                // 16-byte chunks
+                const int nc = 3 * n;
+                for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+                    const unsigned d = (unsigned)__cvta_generic_to_shared(ms + 2 * i);
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(m + 2 * i) : "memory");
+                }
+                asm volatile("cp.async.commit_group;\n" ::: "memory");
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 m = ms;
             }
             build_source(c, g, b);

@@ -200,3 +200,18 @@ def test_mixed_group_counts_in_one_batch_match_oracle():
         assert r["converged"] == 1
         assert pcm(r["k"], ref["k"]) < 10.0
         assert max_pin_err(r["pin_powers"], O.pin_powers()) < 1e-3
+
+
+def test_23_group_assembly_in_a_batch_matches_oracle():
+    # a 17x17 lattice with 23 groups: the CMFD operator of every group does
+    # not fit in shared memory, so each group's is copied in per group solve
+    xml, xsl = W.lattice_case(17, 8, 0.05, "mixed", seed=1007, n_group=23, mod_factor=1.02, fuel_nf_factor=0.98)
+    P = m.Problem(xml, xsl)
+    assert P.sizes["ngroup"] == 23 and P.sizes["npin"] == 289
+    r = _run(m.BatchEngine(precision=1, capacity=2), [P])[0]
+    assert r["error"] == 0, r["message"]
+    O = oracle.OracleSolver(P)
+    ref = O.solve()
+    assert r["converged"] == 1
+    assert pcm(r["k"], ref["k"]) < 10.0
+    assert max_pin_err(r["pin_powers"], O.pin_powers()) < 1e-3
