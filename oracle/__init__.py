@@ -83,7 +83,8 @@ def load():
             ("orc_flux_residual", I, [V, DP]), ("orc_get_flux", I, [V, DP]), ("orc_set_flux", I, [V, DP]),
             ("orc_get_pin_flux_1g", I, [V, I, DP]), ("orc_set_pin_flux_1g", I, [V, I, DP, DP]),
             ("orc_pin_powers", I, [V, DP]), ("orc_get_coarse_currents", I, [V, DP, DP]),
-            ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
+            ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
+            ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_table_exp", D, [D]),
         ]:
             fn = getattr(lib, name)
@@ -214,6 +215,17 @@ class OracleSolver:
         out = np.empty((self.n_pin, self.n_group))
         _chk(self._lib.orc_homogenized_nu_fission(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
+
+    def cmfd_system(self):
+        """The unsolved CMFD system of the current state: op [G][5][n_cell]
+        (diagonal, W, E, S, N), nu-Sigma_f and chi [n_cell][G], scattering
+        [n_cell][G (to)][G (from)], cell volumes [n_cell]."""
+        n, G = self.n_pin, self.n_group
+        op, nf, ch = np.empty((G, 5, n)), np.empty((n, G)), np.empty((n, G))
+        sc, vol = np.empty((n, G, G)), np.empty(n)
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        _chk(self._lib.orc_cmfd_system(self._h, dp(op), dp(nf), dp(ch), dp(sc), dp(vol)))
+        return {"op": op, "xsnf": nf, "xsch": ch, "scat": sc, "vol": vol}
 
     def cmfd_solve(self, k):
         kk = C.c_double(k)

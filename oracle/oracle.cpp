@@ -971,6 +971,31 @@ int orc_homogenized_nu_fission(orc_solver *s, double *out)
                 out[(size_t)ip * s->G + g] = s->hxsnf[(size_t)s->p.pin_cell[ip] * s->G + g];
     });
 }
+int orc_cmfd_system(orc_solver *s, double *op, double *xsnf, double *xsch, double *scat, double *vol)
+{
+    return guard([&] {
+        // the CMFD system CMFD::solve would iterate on from the current state
+        // (EigenSolver::do_cmfd's coarse flux, homogenisation, setup_solve)
+        const int n = s->ncell, G = s->G;
+        std::vector<double> pf(n);
+        for (int g = 0; g < G; g++) {
+            s->get_pin_flux_1g(g, pf.data());
+            for (int i = 0; i < n; i++) s->cflux[(size_t)i * G + g] = pf[i];
+        }
+        if (s->o.cmfd_negative_fixup)
+            for (double &v : s->cflux) v = std::max(v, 0.0);
+        s->homogenize();
+        s->cmfd_setup();
+        const std::vector<double> *rows[5] = {&s->mdiag, &s->mW, &s->mE, &s->mS, &s->mN};
+        for (int g = 0; g < G; g++)
+            for (int q = 0; q < 5; q++)
+                for (int i = 0; i < n; i++) op[((size_t)g * 5 + q) * n + i] = (*rows[q])[(size_t)g * n + i];
+        std::copy(s->hxsnf.begin(), s->hxsnf.end(), xsnf);
+        std::copy(s->hxsch.begin(), s->hxsch.end(), xsch);
+        std::copy(s->hscat.begin(), s->hscat.end(), scat);
+        for (int i = 0; i < n; i++) vol[i] = s->cell_volume(i);
+    });
+}
 int orc_cmfd_solve(orc_solver *s, double *k)
 {
     return guard([&] { s->do_cmfd(*k); });

@@ -99,6 +99,12 @@ int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux);
 /* XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363) of the current
  * flux; writes the pins' nu-Sigma_f, [n_pin, in FSR order][G] */
 int orc_homogenized_nu_fission(orc_solver *s, double *out);
+/* The CMFD system of the current state (coarse flux from the pin flux,
+ * homogenisation, CMFD::setup_solve, cmfd.cpp:333-553), unsolved: op
+ * [G][5][n_cell] (diagonal, west, east, south, north couplings), the
+ * homogenised nu-Sigma_f and chi [n_cell][G], scattering [n_cell][G][G]
+ * (to, from) and cell volumes [n_cell]. */
+int orc_cmfd_system(orc_solver *s, double *op, double *xsnf, double *xsch, double *scat, double *vol);
 int orc_cmfd_solve(orc_solver *s, double *k);
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out);
 /* exponential table check: value of MOCC's table exponential at x */
