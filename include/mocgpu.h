@@ -177,7 +177,11 @@ int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
  * before any stream capture. Meshes over 8192 coarse cells fail with
  * MOCGPU_ERR_CAPACITY. Nothing in the array needs to start at zero. The
  * array is shared by every handle in the process: calls that overlap in time
- * on one device race on it and must be serialised by the caller. */
+ * on one device race on it and must be serialised by the caller. This entry
+ * point always runs the single-CTA solver; mocgpu_cmfd_solve moves meshes
+ * above 1024 cells to a thread-block cluster, so between 1025 and 8192
+ * cells this one is several times slower (about 3.4x on a 68x68 mesh). A
+ * refused call queues no work and leaves the handle unchanged. */
 int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k);
 /* EigenSolver::solve (eigen_solver.cpp:131-223): the whole power iteration.
  * max_outer < 0 uses <solver max_iter>. */

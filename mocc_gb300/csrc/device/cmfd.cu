@@ -975,11 +975,7 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s)
     // 1267 solves/s over four lanes, although the CTAs leave less room for
     // other lanes' sweep CTAs on their SMs)
     const int in_smem = cmfd_smem_mode(max_cell, &smem, MOCGPU_BATCH_CMFD_ALL_GROUPS ? b.max_g : 0);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(kb_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
+    ensure_smem_limit((const void *)kb_cmfd_solve, smem);
     note_launch_external();
     kb_cmfd_solve<<<b.cap, 32 * nw, smem, s>>>(b, in_smem);
 }
@@ -1042,13 +1038,9 @@ static cudaLaunchConfig_t cluster_config(const ClusterShape &sh, cudaStream_t s,
 
 static void launch_cmfd_cluster(const CmfdView &c, cudaStream_t s)
 {
-    static bool attrs_set = false;
-    if (!attrs_set) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        if (MOCGPU_CMFD_CLUSTER_MAX > 8)
-            MOCGPU_CUDA(cudaFuncSetAttribute(kc_cmfd_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        attrs_set = true;
-    }
+    ensure_smem_limit((const void *)kc_cmfd_solve, 200 * 1024);
+    if (MOCGPU_CMFD_CLUSTER_MAX > 8)
+        raise_func_attr((const void *)kc_cmfd_solve, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     ClusterShape sh = cluster_shape(c, MOCGPU_CMFD_CLUSTER_MAX);
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t cfg = cluster_config(sh, s, attr);
@@ -1075,11 +1067,7 @@ void launch_cmfd_solve(const CmfdView &c, cudaStream_t s)
     const int nw = cmfd_warps(c.n_cell);
     size_t smem = 0;
     const int in_smem = cmfd_smem_mode(c.n_cell, &smem, c.G);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(k_cmfd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
+    ensure_smem_limit((const void *)k_cmfd_solve, smem);
     note_launch_external();
     k_cmfd_solve<<<1, 32 * nw, smem, s>>>(c, in_smem);
 }

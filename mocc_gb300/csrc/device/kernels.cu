@@ -4,6 +4,9 @@
 // is this project's own.
 #include <atomic>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "kernels.cuh"
 
@@ -27,6 +30,26 @@ void copy_bytes(int64_t *h2d, int64_t *d2h)
 {
     *h2d = g_h2d.load();
     *d2h = g_d2h.load();
+}
+
+// Function attributes are per device: remember what was set for each
+// (kernel, device, attribute) and raise it only when a launch needs more.
+void raise_func_attr(const void *kernel, cudaFuncAttribute attr, int value)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, int>, int> set;
+    int dev = 0;
+    MOCGPU_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    int &cur = set[std::make_tuple(kernel, dev, (int)attr)];
+    if (value > cur) {
+        MOCGPU_CUDA(cudaFuncSetAttribute(kernel, attr, value));
+        cur = value;
+    }
+}
+void ensure_smem_limit(const void *kernel, size_t bytes)
+{
+    if (bytes > 48 * 1024) raise_func_attr(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 // ---------------------------------------------------------------------------

@@ -195,6 +195,10 @@ void launch_flux_residual(const GeomView &g, const StateView &st, double *out, c
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);
 void set_exp_constants(double min, double space, double rspace);
 int64_t launch_count();
+// Kernel attributes are set per device; these set them on the current device
+// once per (kernel, attribute) and value, safely from several host threads.
+void raise_func_attr(const void *kernel, cudaFuncAttribute attr, int value);
+void ensure_smem_limit(const void *kernel, size_t bytes); // dynamic shared memory above 48 KB
 void copy_bytes(int64_t *h2d, int64_t *d2h); // host<->device bytes moved so far
 
 } // namespace mocgpu

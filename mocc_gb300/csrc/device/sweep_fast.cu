@@ -84,6 +84,15 @@ template <> struct Pair<double> {
 #else
 #define MOCGPU_SWEEP_BOUNDS
 #endif
+// The fixed-point tally's words cannot wrap: a contribution below
+// 2^TALLY_BITS / max_hits adds less than 2^(TALLY_BITS - 20) / max_hits + 1 to
+// the signed high word and less than 2^20 to the unsigned low word, so
+// max_hits adds keep the high word below 2^(TALLY_BITS - 20) + max_hits and
+// the low word below max_hits * 2^20. Both must stay inside 32-bit words.
+static_assert(MOCGPU_TALLY_BITS - 20 <= 30, "fixed-point tally: the high word would overflow");
+static_assert((long long)kMaxTallyHits * (1ll << 20) <= (1ll << 31), "fixed-point tally: the low word would wrap");
+static_assert((1ll << (MOCGPU_TALLY_BITS - 20)) + kMaxTallyHits < (1ll << 31),
+              "fixed-point tally: the high word would overflow");
 template <typename Real> struct Chunk {
     static constexpr int rows = MOCGPU_SWEEP_ROWS;     // rows per streamed chunk
     static constexpr int stages = MOCGPU_SWEEP_STAGES; // chunks in flight per warp ring
@@ -589,12 +598,7 @@ template <typename Real> static size_t batched_smem(int bundles_per_unit, int ma
 
 template <typename Real, int NPOL, bool GS, int CUR> static void prepare_batched(size_t smem)
 {
-    auto k = kb_sweep_fast<Real, NPOL, GS, CUR>;
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
+    ensure_smem_limit((const void *)kb_sweep_fast<Real, NPOL, GS, CUR>, smem);
 }
 
 template <typename Real, int NPOL, bool GS, int CUR>
@@ -672,11 +676,7 @@ static void launch_one(const GeomView &g, const FastView &fv, const StateView &s
 {
     auto k = k_sweep_fast<Real, NPOL, GS, CUR>;
     size_t smem = fast_sweep_smem<Real>(fv);
-    static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        MOCGPU_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = smem;
-    }
+    ensure_smem_limit((const void *)k, smem);
     int threads = 64 * fv.bundles_per_unit;
     k<<<wu1 - wu0, threads, smem, s>>>(g, fv, st, group, wu0);
 }

@@ -477,6 +477,11 @@ void Sweeper::cmfd_solve(double &k)
 
 void Sweeper::cmfd_solve_static(double &k)
 {
+    // refuse an oversized mesh before any work is queued, so that a refused
+    // call leaves the handle's coarse flux and homogenised data untouched
+    if (cv_.n_cell > static_cmfd_max_cells())
+        throw Error(21, "coarse mesh has " + std::to_string(cv_.n_cell) + " cells; the static CMFD scratch holds " +
+                            std::to_string(static_cmfd_max_cells()));
     launch_pin_flux(gv_, phi_.p, cflux_.p, stream_);
     launch_homogenize(gv_, phi_.p, cv_, stream_);
     cv_.has_radial = has_radial_ ? 1 : 0;

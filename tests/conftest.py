@@ -31,7 +31,13 @@ def golden():
 
 @pytest.fixture(scope="session")
 def ref_xsl():
-    """Synthetic library whose material names match MOCC's test inputs."""
-    import mocc_gb300 as m
-    return (m.synthetic_xsl(1, 7, 2).replace("fuel1", "UO2-3.3").replace("fuel2", "MOX-4.3")
-            .replace("moderator", "Moderator"))
+    """MOCC's own 7-group C5G7 library (the c5g7.xsl of its tests and
+    examples), copied into tests/golden by make_golden.py."""
+    return (ROOT / "tests" / "golden" / "c5g7.xsl").read_text()
+
+
+@pytest.fixture(scope="session")
+def ref_example():
+    """MOCC's example inputs, unchanged: name -> XML text."""
+    g = ROOT / "tests" / "golden"
+    return {"3x3": (g / "example_3x3.xml").read_text(), "c5g7_2d": (g / "example_c5g7_2d.xml").read_text()}

@@ -7,10 +7,17 @@ Reads (as text) the reference test sources and their geometry inputs:
   src/sweepers/moc/tests/test_RayData.cpp  volume-conservation test setup
   src/core/tests/test_XSMeshHomogenized.cpp, 2x3_1.xml, 2x3_2.xml
                                            pin-homogenised nu-Sigma_f
-and writes tests/golden/reference_known_answers.json. Material libraries are
-not copied: the tests attach a synthetic library under the same names.
+and writes tests/golden/reference_known_answers.json. It also copies the
+reference's own inputs that the tests run unchanged:
+  examples/c5g7.xsl      the 7-group library of MOCC's tests and examples
+                         (src/core/tests/c5g7.xsl and
+                         src/sweepers/moc/tests/c5g7.xsl are the same file)
+  examples/3x3.xml       3x3 UO2/MOX pins with a reflector, vacuum faces
+  examples/c5g7_2d.xml   the 2-D quarter core of the same benchmark
+into tests/golden/ under the names c5g7.xsl, example_3x3.xml and
+example_c5g7_2d.xml.
 
-Usage: python tests/golden/make_golden.py /path/to/mocc/checkout
+Usage: python tests/golden/make_golden.py <path of a MOCC checkout>
 """
 import json
 import re
@@ -69,10 +76,20 @@ def main(root):
     out["xsmesh_homogenized"] = {"lattice_xml": (ct / "2x3_2.xml").read_text(),
                                  "solid_xml": (ct / "2x3_1.xml").read_text(),
                                  "nu_fission_pattern": pattern, "solid_uo2_nu_fission": solid, "tol": 1e-6}
-    dst = Path(__file__).resolve().parent / "reference_known_answers.json"
+    here = Path(__file__).resolve().parent
+    dst = here / "reference_known_answers.json"
     dst.write_text(json.dumps(out, indent=1))
     print("wrote", dst)
+    lib = (Path(root) / "examples/c5g7.xsl").read_bytes()
+    for other in ("src/core/tests/c5g7.xsl", "src/sweepers/moc/tests/c5g7.xsl"):
+        assert (Path(root) / other).read_bytes() == lib, other
+    for src, name in (("examples/c5g7.xsl", "c5g7.xsl"), ("examples/3x3.xml", "example_3x3.xml"),
+                      ("examples/c5g7_2d.xml", "example_c5g7_2d.xml")):
+        (here / name).write_bytes((Path(root) / src).read_bytes())
+        print("copied", src, "->", here / name)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(__doc__)
+    main(sys.argv[1])

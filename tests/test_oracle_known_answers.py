@@ -4,8 +4,8 @@
 * test_MoC_IHM.cpp: infinite homogeneous medium -- after one sweep per group
   from the analytic spectrum the FSR flux equals the spectrum within 0.5 %
 * test_MoCSweeper.cpp: get -> set -> get pin flux is the identity
-The material of the IHM case is the synthetic fuel (the test's logic holds for
-any cross sections).
+The IHM case uses MOCC's own UO2-3.3 from its C5G7 library, as the reference
+test does.
 """
 import math
 
@@ -70,9 +70,11 @@ def test_ihm_analytic_spectrum(ref_xsl):
 
 
 def test_ihm_eigenvalue_converges_to_k_inf(ref_xsl):
-    P = ihm_problem(ref_xsl, n_inner=2)
+    # C5G7's UO2-3.3 scatters strongly with upscatter in the thermal groups:
+    # ten inner iterations per group keep the power iteration short
+    P = ihm_problem(ref_xsl, n_inner=10)
     k_ref, _ = analytic_spectrum(P)
-    r = oracle.OracleSolver(P).solve()
+    r = oracle.OracleSolver(P, max_iter=1000).solve()
     assert r["converged"]
     assert abs(r["k"] - k_ref) / k_ref < 5e-5
 
@@ -177,42 +179,30 @@ def test_vacuum_core_with_corner_crossings_converges():
 
 
 def test_homogenized_nu_fission_xsmesh_known_answers(golden, ref_xsl):
-    """test_XSMeshHomogenized.cpp: pin-homogenised nu-Sigma_f of a 2x3 lattice
-    of UO2 and MOX pins (cylindrical fuel in moderator) and of solid UO2 pins,
-    volume-weighted (flat flux). The reference's values are for the C5G7
-    library: 0.0115752 for a UO2 pin against 2.005998e-2 for solid UO2 gives
-    the fuel's area fraction, which holds for any library; each lattice's pins
-    take the reference's MOX/UO2 pattern."""
+    """test_XSMeshHomogenized.cpp with MOCC's own C5G7 library: flat-flux
+    (volume-weighted) pin-homogenised group-1 nu-Sigma_f of the 2x3
+    UO2/MOX lattice (0.0125521 for a MOX pin, 0.0115752 for a UO2 pin) and
+    of solid UO2 pins (2.005998e-2), each to the reference's 1e-6."""
     h = golden["xsmesh_homogenized"]
     solver = ('<solver type="eigenvalue" k_tol="1e-6" psi_tol="1e-5" max_iter="10"><sweeper type="moc" n_inner="1">'
               '<ang_quad type="ls" order="4" /><rays spacing="0.05" /></sweeper></solver>')
-    # MOX with a larger nu-Sigma_f than UO2, as in C5G7
-    ref_xsl = (m.synthetic_xsl(1, 7, 2, fuel_nf_scale=[1.0, 1.3]).replace("fuel1", "UO2-3.3")
-               .replace("fuel2", "MOX-4.3").replace("moderator", "Moderator"))
     pat = h["nu_fission_pattern"]
-    frac_ref = min(pat) / h["solid_uo2_nu_fission"]
+    assert sorted(set(pat)) == [0.0115752, 0.0125521]
     for key, solid in (("lattice_xml", False), ("solid_xml", True)):
         P = m.Problem(solver + h[key], ref_xsl)
         O = oracle.OracleSolver(P)
         O.initialize()  # flat flux: volume weighting
         hom = O.homogenized_nu_fission()[:, 0]
-        G = P.sizes["ngroup"]
-        xsnf = P.export("xsnf").reshape(-1, G)[:, 0]
-        first = P.export("pin_first_reg")[:-1]
-        fuel_nf = xsnf[P.export("fsr_mat")[first]]
-        assert P.sizes["npin"] == 72 and np.all(fuel_nf > 0)
+        assert P.sizes["npin"] == 72
         if solid:
-            assert np.allclose(hom, fuel_nf, rtol=1e-12)
+            assert np.all(np.abs(hom - h["solid_uo2_nu_fission"]) < h["tol"])
             continue
-        assert np.allclose(hom / fuel_nf, frac_ref, rtol=1e-4)
         # the reference lists each 2x3 lattice's pins row by row from the
         # bottom; here pins are located by their coarse cell (x fastest)
         nx = P.sizes["nx"]
         cell = P.export("pin_cell")
         j = (cell // nx % 3) * 2 + (cell % nx % 2)
-        mox = np.array(pat)[j] == max(pat)
-        assert 0 < mox.sum() < mox.size
-        assert np.ptp(hom[mox]) < 1e-12 and np.ptp(hom[~mox]) < 1e-12 and hom[mox][0] > hom[~mox][0]
+        assert np.all(np.abs(hom - np.array(pat)[j]) < h["tol"])
 
 
 @pytest.mark.parametrize("case", ["lattice7", "core_vacuum"])
