@@ -73,6 +73,11 @@ def parse():
     ap.add_argument("--cases", type=int, default=N_CASES)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle legs")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="for profilers: one untimed run of the workload, then one more inside an NVTX range "
+                         "named mocgpu_timed (branch256: one batch of --cases solves in one engine; assembly17 / "
+                         "minicore: one solve); prints a JSON summary, no benchmark line")
+    ap.add_argument("--bundles-per-unit", type=int, default=1, help="work-unit shape for --profile-once")
     return ap.parse_args()
 
 
@@ -575,8 +580,61 @@ def run_single(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def profile_once(args):
+    """One untimed run, then one inside the NVTX range ``mocgpu_timed`` so
+    that a profiler can restrict itself to the second, e.g.
+
+        ncu --nvtx --nvtx-include "mocgpu_timed/" --metrics gpu__time_duration.sum \\
+            --clock-control none --csv --log-file launches.csv python bench.py --profile-once --cases 256
+    """
+    import torch
+
+    import mocc_gb300 as m
+    from mocc_gb300 import workloads as W
+    m.load_library()
+    if args.workload in SINGLE:
+        P = m.Problem(*getattr(W, args.workload)(precision="mixed"))
+        S = m.MoCSweeper(P, 1)
+        E = m.EigenSolver(P, sweeper=S)
+        E.solve()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("mocgpu_timed")
+        t = time.perf_counter()
+        r = E.solve()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"workload": args.workload, "wall_s": wall, "k": r["k"], "iterations": r["iterations"],
+                          "converged": r["converged"]}))
+        return 0 if r["converged"] else 1
+    cases, bases, reqs = branch_workload(args.cases)
+    E = m.BatchEngine(precision=1, capacity=max(1, args.cases), bundles_per_unit=args.bundles_per_unit)
+
+    def batch():
+        ids = [E.submit(P, x) for P, x in reqs]
+        E.run()
+        return [E.take(i) for i in ids]
+
+    batch()
+    torch.cuda.synchronize()
+    s0 = E.stats()
+    torch.cuda.nvtx.range_push("mocgpu_timed")
+    t = time.perf_counter()
+    res = batch()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t
+    torch.cuda.nvtx.range_pop()
+    s1 = E.stats()
+    ok = all(r["error"] == 0 and r["converged"] for r in res)
+    print(json.dumps({"cases": args.cases, "wall_s": wall, "replay_ms": s1["replay_ms"] - s0["replay_ms"],
+                      "replays": s1["graph_replays"] - s0["graph_replays"], "all_converged": ok}))
+    return 0 if ok else 1
+
+
 def main():
     args = parse()
+    if args.profile_once:
+        raise SystemExit(profile_once(args))
     rank, world = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, world)

@@ -395,16 +395,26 @@ void launch_zero_radial_currents(const GeomView &g, const StateView &st, int gro
 {
     MOCGPU_CUDA(cudaMemsetAsync(st.cur + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
     MOCGPU_CUDA(cudaMemsetAsync(st.sflux + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
+    MOCGPU_CUDA(cudaMemsetAsync(st.cur32, 0, sizeof(float) * 2 * g.n_surf, s));
 }
 
-// Currents per unit area on the x/y-normal surfaces (moc_current_worker.hpp:272-318).
+// Currents per unit area on the x/y-normal surfaces (moc_current_worker.hpp:272-318),
+// with the FP32 sweep's tallies folded in (and cleared for the next group).
+__device__ __forceinline__ void normalize_surface(const GeomView &g, const StateView &st, int group, int i,
+                                                  const double *area)
+{
+    const size_t k = (size_t)group * g.n_surf + i;
+    st.cur[k] = (st.cur[k] + (double)st.cur32[i]) / area[i];
+    st.sflux[k] = (st.sflux[k] + (double)st.sfl32[i]) / area[i];
+    st.cur32[i] = 0.f;
+    st.sfl32[i] = 0.f;
+}
 __global__ void k_normalize_currents(GeomView g, StateView st, int group, const double *area)
 {
     int i = g.nx * g.ny + blockIdx.x * blockDim.x + threadIdx.x;
     int end = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx + g.nx * g.ny;
     if (i >= end) return;
-    st.cur[(size_t)group * g.n_surf + i] /= area[i];
-    st.sflux[(size_t)group * g.n_surf + i] /= area[i];
+    normalize_surface(g, st, group, i, area);
 }
 void launch_normalize_currents(const GeomView &g, const StateView &st, int group, const double *area, cudaStream_t s)
 {
@@ -716,6 +726,8 @@ __global__ void kb_zero_currents(BatchViews b, int group)
     if (i >= g.n_surf || group >= g.G) return;
     st.cur[(size_t)group * g.n_surf + i] = 0.0;
     st.sflux[(size_t)group * g.n_surf + i] = 0.0;
+    st.cur32[i] = 0.f;
+    st.sfl32[i] = 0.f;
 }
 void launch_b_zero_currents(const BatchViews &b, int group, cudaStream_t s)
 {
@@ -734,8 +746,7 @@ __global__ void kb_normalize_currents(BatchViews b, int group)
     int end = (g.nx + 1) * g.ny + (g.ny + 1) * g.nx + g.nx * g.ny;
     if (blockIdx.x == 0 && threadIdx.x == 0) st.red[RED_HAS_RADIAL] = 1.0;
     if (i >= end) return;
-    st.cur[(size_t)group * g.n_surf + i] /= area[i];
-    st.sflux[(size_t)group * g.n_surf + i] /= area[i];
+    normalize_surface(g, st, group, i, area);
 }
 void launch_b_normalize_currents(const BatchViews &b, int group, cudaStream_t s)
 {

@@ -59,6 +59,10 @@ struct StateView {
     void *qbar, *sigt, *tally; // Real
     void *psi_in, *psi_out;    // Real
     double *cur, *sflux;       // [G][n_surf]
+    // FP32 sweep: the crossing currents and surface fluxes of the group being
+    // tallied, [n_surf] each (native float reductions), folded into cur and
+    // sflux by the normalisation and cleared
+    float *cur32, *sfl32;
     double *cflux;             // coarse (pin) flux [G][n_pin]
     double *red;               // per-solve scalars and reduction scratch (64 doubles)
     unsigned *status;

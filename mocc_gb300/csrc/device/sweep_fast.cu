@@ -192,7 +192,9 @@ template <typename Real, int NPOL> struct UnitCtx {
     const int *lf;            // unit-local -> global FSR ids
     float inv_scale;          // 1 / the unit's fixed-point scale
     Real *psi_in, *psi_out;
-    double *cur, *sfl;
+    double *cur, *sfl;        // FP64 sweep: the group's currents and surface fluxes
+    float *cur32, *sfl32;     // FP32 sweep: their FP32 tallies
+    float csgn[2];            // FP32: current of a crossing = csgn[normal] * S (sign and 1 / scale)
     const int (*s_off)[kMaxPolar];
     const int (*s_tgt)[kMaxPolar][2];
     int ny_set;
@@ -287,17 +289,31 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
             int c = ev0.y;
             int surf = c >> 1;
             bool ynorm = c & 1;
-            // partial current and surface flux of this crossing in the
-            // sweep precision, accumulated in FP64 (the hardware conversion
-            // measured 2 % faster per batch than widening with integer ops)
-            Real jc = 0, fc = 0;
+            if constexpr (FIXED) {
+                // MOCC's current weight of a crossing (moc_current_worker.hpp:
+                // 176-181) is the tally weight w_p with the sign of the
+                // direction's x or y cosine, so the current is that sign times
+                // S = sum_p w_p psi_p (kept for the tally); FP32 tallies with
+                // native float reductions, folded into the FP64 currents when
+                // they are normalised
+                const float cs = ynorm ? U.csgn[1] : U.csgn[0];
+                atomicAdd(U.cur32 + surf, S * (FWD ? cs : -cs));
+                if (CUR == 1) {
+                    float fc = 0.f;
 #pragma unroll
-            for (int p = 0; p < NPOL; p++) {
-                jc += psi[p] * (ynorm ? U.cw[p][1] : U.cw[p][0]);
-                if (CUR == 1) fc += psi[p] * (ynorm ? U.fwt[p][1] : U.fwt[p][0]);
+                    for (int p = 0; p < NPOL; p++) fc += psi[p] * (ynorm ? U.fwt[p][1] : U.fwt[p][0]);
+                    atomicAdd(U.sfl32 + surf, fc);
+                }
+            } else {
+                Real jc = 0, fc = 0;
+#pragma unroll
+                for (int p = 0; p < NPOL; p++) {
+                    jc += psi[p] * (ynorm ? U.cw[p][1] : U.cw[p][0]);
+                    if (CUR == 1) fc += psi[p] * (ynorm ? U.fwt[p][1] : U.fwt[p][0]);
+                }
+                atomicAdd(U.cur + surf, (double)(FWD ? jc : -jc));
+                if (CUR == 1) atomicAdd(U.sfl + surf, (double)fc);
             }
-            atomicAdd(U.cur + surf, (double)(FWD ? jc : -jc));
-            if (CUR == 1) atomicAdd(U.sfl + surf, (double)fc);
             ev++;
             ev0 = ev1;
             ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
@@ -326,7 +342,11 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
             Real S1 = 0;
 #pragma unroll
             for (int p = 0; p < NPOL; p++) {
+#if MOCGPU_PSI_FMA2
+                psi[p] = fmaf(psi[p], E[p], fmaf(-sq.y, E[p], sq.y));
+#else
                 psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
+#endif
                 S1 = fmaf(U.wt[p], psi[p], S1);
             }
             tally_fixed(U.s_hi, U.s_lo, U.tally, U.lf, U.inv_scale, l, S - S1);
@@ -433,6 +453,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     U.psi_out = (Real *)st.psi_out;
     U.cur = st.cur + (size_t)group * g.n_surf;
     U.sfl = st.sflux + (size_t)group * g.n_surf;
+    U.cur32 = st.cur32;
+    U.sfl32 = st.sfl32;
     U.ny_set = g.set_ny[u.set];
 
     // per unit: boundary-flux offsets of every (direction, polar) angle and
@@ -535,6 +557,11 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         U.tally = (float *)st.tally;
         U.lf = lf;
         U.inv_scale = inv_scale;
+        if (CUR) {
+            const SetPolar sp0 = g.sp[u.set * NPOL];
+            U.csgn[0] = copysignf(inv_scale, (float)sp0.cw[0]);
+            U.csgn[1] = copysignf(inv_scale, (float)sp0.cw[1]);
+        }
     }
 
     const int ntasks = 2 * u.n_bundles;

@@ -16,7 +16,7 @@ size_t Sweeper::state_bytes_for(const FlatProblem &f, int precision, int bcpg)
     d += 2 * G * ns;                                      // currents, surface flux
     d += G * nc + 5 * nc * G + nc * G * G + 4 * G * ns;   // coarse flux, homogenised data, coupling
     d += G * 6 * nc + 2 * nc + 12 * nc + 8 + nc + 1 + 64; // CMFD operator, sources, vectors, stats, pins, red
-    return d * sizeof(double) + rb * (3 * n + (G + 1) * (size_t)bcpg) + sizeof(unsigned);
+    return d * sizeof(double) + rb * (3 * n + (G + 1) * (size_t)bcpg) + 2 * ns * sizeof(float) + sizeof(unsigned);
 }
 
 Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shared_ptr<const DeviceGeometry> geo,
@@ -71,6 +71,8 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     sflux_.alloc((size_t)G * f.n_surf);
     cur_.zero(stream_);
     sflux_.zero(stream_);
+    cur32_.alloc((size_t)2 * f.n_surf);
+    cur32_.zero(stream_);
     red_.alloc(64);
     red_.zero(stream_);
     status_.alloc(1);
@@ -112,6 +114,8 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     s.psi_out = psi_out_.p;
     s.cur = cur_.p;
     s.sflux = sflux_.p;
+    s.cur32 = cur32_.p;
+    s.sfl32 = cur32_.p + f.n_surf;
     s.cflux = cflux_.p;
     s.red = red_.p;
     s.status = status_.p;
@@ -246,6 +250,7 @@ void Sweeper::initialize()
     tally_.zero(stream_);
     cur_.zero(stream_);
     sflux_.zero(stream_);
+    cur32_.zero(stream_);
     status_.zero(stream_);
     has_radial_ = false;
     sweeps_done = 0;

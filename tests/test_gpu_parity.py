@@ -217,7 +217,9 @@ def test_corner_exits_small_core(precision):
 @pytest.mark.parametrize("precision", [0, 1])
 def test_ihm_on_gpu(ref_xsl, precision):
     from test_oracle_known_answers import analytic_spectrum, ihm_problem
-    P = ihm_problem(ref_xsl, n_inner=200)
+    # MOCC's 800 inner iterations: C5G7's UO2-3.3 scatters strongly within
+    # the thermal groups, so fewer leave the within-group source unconverged
+    P = ihm_problem(ref_xsl, n_inner=800)
     k_ref, phi = analytic_spectrum(P)
     S = m.MoCSweeper(P, precision)
     n = P.sizes["nfsr"]
