@@ -263,16 +263,24 @@ int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xs
 /* Admits what fits, runs one outer iteration of every active solve, retires
  * finished ones; *n_active = solves still active. */
 int mocgpu_batch_step(mocgpu_batch *b, int *n_active);
-/* mocgpu_batch_step in two halves, so that several engines (each on its own
- * stream) can have outer iterations on the GPU at the same time: launch
- * admits and enqueues one replay and returns at once; finish waits for it
- * and retires finished solves. A launch must be followed by a finish. */
+/* mocgpu_batch_step in two halves: launch admits and enqueues one replay
+ * (one outer iteration of every active solve) and returns at once; finish
+ * waits for the oldest replay in flight and retires the solves it ended.
+ * The convergence test runs on the device and a solve that ends is frozen,
+ * so up to the pipeline depth (default 2) replays may be in flight: the
+ * host reads one replay's summary while the next runs. Several engines,
+ * each on its own stream, overlap on the GPU the same way. A launch beyond
+ * the depth fails with MOCGPU_ERR_ARG. */
 int mocgpu_batch_launch(mocgpu_batch *b, int *n_active);
 int mocgpu_batch_finish(mocgpu_batch *b, int *n_active);
-/* *done = 1 when nothing is in flight or the launched iteration has
+/* replays launch may have in flight, 1..4 (set with none in flight) */
+int mocgpu_batch_set_pipeline_depth(mocgpu_batch *b, int depth);
+/* replays launched and not yet finished */
+int mocgpu_batch_in_flight(mocgpu_batch *b, int *n);
+/* *done = 1 when nothing is in flight or the oldest replay in flight has
  * completed, so that mocgpu_batch_finish would not block. */
 int mocgpu_batch_poll(mocgpu_batch *b, int *done);
-/* Steps until nothing is queued or active. */
+/* Runs with the pipeline full until nothing is queued or active. */
 int mocgpu_batch_run(mocgpu_batch *b);
 /* *ready = 1 and the result (removed from the engine) once solve id is done;
  * pin_powers (may be NULL) receives res->n_pin values. */

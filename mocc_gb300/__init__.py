@@ -134,6 +134,8 @@ def load_library(build: bool = True):
         "mocgpu_batch_launch": (I, [P, IP]),
         "mocgpu_batch_finish": (I, [P, IP]),
         "mocgpu_batch_poll": (I, [P, IP]),
+        "mocgpu_batch_set_pipeline_depth": (I, [P, I]),
+        "mocgpu_batch_in_flight": (I, [P, IP]),
         "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
         "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
         "mocgpu_batch_ready": (I, [P, I64P, I, IP]),
@@ -446,6 +448,7 @@ class BatchEngine:
                                              C.byref(h)))
         self._h = h
         self._keep = {}
+        self.depth = 2
 
     def close(self):
         if getattr(self, "_h", None):
@@ -468,6 +471,16 @@ class BatchEngine:
     def run(self):
         _check(self._lib.mocgpu_batch_run(self._h))
 
+    def set_pipeline_depth(self, depth: int):
+        """Outer iterations launch() may have in flight (1..4, default 2)."""
+        _check(self._lib.mocgpu_batch_set_pipeline_depth(self._h, depth))
+        self.depth = depth
+
+    def in_flight(self) -> int:
+        n = C.c_int()
+        _check(self._lib.mocgpu_batch_in_flight(self._h, C.byref(n)))
+        return n.value
+
     def launch(self) -> int:
         """Enqueues one outer iteration of every active solve; returns at once."""
         n = C.c_int()
@@ -481,7 +494,7 @@ class BatchEngine:
         return bool(d.value)
 
     def finish(self) -> int:
-        """Waits for the launched iteration and retires finished solves."""
+        """Waits for the oldest launched iteration and retires the solves it ended."""
         n = C.c_int()
         _check(self._lib.mocgpu_batch_finish(self._h, C.byref(n)))
         return n.value

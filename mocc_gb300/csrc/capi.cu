@@ -650,6 +650,17 @@ int mocgpu_batch_finish(mocgpu_batch *b, int *n_active)
     });
 }
 
+int mocgpu_batch_set_pipeline_depth(mocgpu_batch *b, int depth)
+{
+    return guarded([&] { eng(b).set_pipeline_depth(depth); });
+}
+int mocgpu_batch_in_flight(mocgpu_batch *b, int *n)
+{
+    return guarded([&] {
+        REQUIRE(n, "null argument");
+        *n = eng(b).in_flight();
+    });
+}
 int mocgpu_batch_poll(mocgpu_batch *b, int *done)
 {
     return guarded([&] {

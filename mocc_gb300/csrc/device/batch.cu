@@ -34,33 +34,53 @@ BatchEngine::BatchEngine(int precision, int capacity, size_t mem_budget, int bun
     d_act_.alloc(cap_);
     d_nact_.alloc(1);
     d_nact_.zero(stream_);
-    d_sum_.alloc((size_t)cap_ * 6);
-    MOCGPU_CUDA(cudaMallocHost((void **)&h_sum_, sizeof(double) * 6 * (size_t)cap_));
-    MOCGPU_CUDA(cudaEventCreate(&rep0_));
-    MOCGPU_CUDA(cudaEventCreate(&rep1_));
+    d_sum_.alloc((size_t)cap_ * kSummaryStride);
+    ring_.resize(4);
+    captured_.resize(4);
+    for (Ring &r : ring_) {
+        MOCGPU_CUDA(cudaEventCreate(&r.e0));
+        MOCGPU_CUDA(cudaEventCreate(&r.e1));
+        MOCGPU_CUDA(cudaEventCreateWithFlags(&r.e2, cudaEventDisableTiming));
+        MOCGPU_CUDA(cudaMallocHost((void **)&r.h_sum, sizeof(double) * kSummaryStride * (size_t)cap_));
+    }
     MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+// Waits for every replay in flight (they stay queued for finish()); needed
+// before freeing or moving device memory those replays may read.
+void BatchEngine::drain()
+{
+    if (!flights_.empty()) MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void BatchEngine::set_pipeline_depth(int d)
+{
+    if (d < 1 || d > (int)ring_.size()) MOCGPU_THROW(1, "pipeline depth must be in [1, 4]");
+    if (!flights_.empty()) MOCGPU_THROW(1, "change the pipeline depth with no replay in flight");
+    depth_ = d;
 }
 
 void BatchEngine::set_timing(bool on)
 {
     if (on == timing_) return;
+    if (!flights_.empty()) MOCGPU_THROW(1, "change timing with no replay in flight");
     timing_ = on;
-    captured_ = Shape{}; // force a new capture
-    if (exec_) {
-        cudaGraphExecDestroy(exec_);
-        exec_ = nullptr;
-    }
+    for (Shape &c : captured_) c = Shape{}; // force new captures
 }
 
 BatchEngine::~BatchEngine()
 {
-    if (exec_) cudaGraphExecDestroy(exec_);
-    if (graph_) cudaGraphDestroy(graph_);
-    if (h_sum_) cudaFreeHost(h_sum_);
-    if (h_pins_) cudaFreeHost(h_pins_);
-    for (cudaEvent_t e : tev_) cudaEventDestroy(e);
-    if (rep0_) cudaEventDestroy(rep0_);
-    if (rep1_) cudaEventDestroy(rep1_);
+    cudaStreamSynchronize(stream_);
+    for (Ring &r : ring_) {
+        if (r.exec) cudaGraphExecDestroy(r.exec);
+        if (r.graph) cudaGraphDestroy(r.graph);
+        if (r.h_sum) cudaFreeHost(r.h_sum);
+        if (r.h_pins) cudaFreeHost(r.h_pins);
+        for (cudaEvent_t e : r.tev) cudaEventDestroy(e);
+        if (r.e0) cudaEventDestroy(r.e0);
+        if (r.e1) cudaEventDestroy(r.e1);
+        if (r.e2) cudaEventDestroy(r.e2);
+    }
 }
 
 double BatchEngine::now() const { return wall_seconds() - t0_; }
@@ -148,7 +168,9 @@ bool BatchEngine::try_admit(Pending &p)
     if (reuse) need_state = 0;
     if (in_use_ + need_geo + need_state > budget_) {
         // release pooled handles of other geometries, then resident
-        // geometries that no solve uses
+        // geometries that no solve uses (replays in flight may still read a
+        // retired solve's flags: let them end first)
+        drain();
         for (auto it = pool_.begin(); it != pool_.end() && in_use_ + need_geo + need_state > budget_; ++it) {
             if (it->first == p.P.get()) continue;
             while (!it->second.empty() && in_use_ + need_geo + need_state > budget_) {
@@ -194,10 +216,6 @@ bool BatchEngine::try_admit(Pending &p)
     S.geo = geo;
     S.key = p.P.get();
     S.id = p.id;
-    S.max_iter = p.P->opts.max_iter;
-    S.min_iter = p.P->opts.min_iter;
-    S.k_tol = p.P->opts.k_tol;
-    S.psi_tol = p.P->opts.psi_tol;
     S.iterations = 0;
     S.t_submit = p.t_submit;
     S.t_admit = now();
@@ -208,11 +226,17 @@ bool BatchEngine::try_admit(Pending &p)
     Sweeper &sw = *S.sw;
     sw.set_coarse_enabled(cmfd_);
     sw.initialize();
-    double init[16] = {0};
-    init[RED_K - RED_K] = 1.0;                          // RED_K
-    init[RED_K_PREV - RED_K] = 1.0;                     // RED_K_PREV
-    init[RED_N_FISSILE - RED_K] = (double)sw.n_fissile(); // RED_N_FISSILE
-    MOCGPU_CUDA(copy_async(sw.state().red + RED_K, init, sizeof(double) * 14, cudaMemcpyHostToDevice, stream_));
+    // per-solve scalars RED_K .. RED_MAX_ITER, with the convergence test's
+    // parameters (<solver k_tol psi_tol min_iter max_iter>) for kb_retire
+    double init[RED_MAX_ITER - RED_K + 1] = {0};
+    init[RED_K - RED_K] = 1.0;
+    init[RED_K_PREV - RED_K] = 1.0;
+    init[RED_N_FISSILE - RED_K] = (double)sw.n_fissile();
+    init[RED_K_TOL - RED_K] = p.P->opts.k_tol;
+    init[RED_PSI_TOL - RED_K] = p.P->opts.psi_tol;
+    init[RED_MIN_ITER - RED_K] = (double)p.P->opts.min_iter;
+    init[RED_MAX_ITER - RED_K] = (double)p.P->opts.max_iter;
+    MOCGPU_CUDA(copy_async(sw.state().red + RED_K, init, sizeof(init), cudaMemcpyHostToDevice, stream_));
     sw.calc_fission_source(1.0);
 
     // shape of the captured graph
@@ -228,30 +252,32 @@ bool BatchEngine::try_admit(Pending &p)
     return true;
 }
 
-void BatchEngine::retire(int slot, int error, const std::string &msg, bool converged, double k, double ek, double ep,
-                         int64_t cmfd_its)
+void BatchEngine::retire(int slot, int error, const std::string &msg, bool converged, const double *row,
+                         const double *pins, int pins_stride)
 {
     Slot &S = slots_[slot];
     BatchResult r;
     r.id = S.id;
     r.error = error;
     r.message = msg;
-    r.k = k;
-    r.iterations = S.iterations;
+    r.k = row[0];
+    r.iterations = (int)row[7];
     r.converged = converged ? 1 : 0;
-    r.error_k = ek;
-    r.error_psi = ep;
-    r.cmfd_iterations = cmfd_its;
+    r.error_k = row[1];
+    r.error_psi = row[2];
+    r.cmfd_iterations = (int64_t)row[4];
     r.t_submit = S.t_submit;
     r.t_admit = S.t_admit;
+    st_.outer_iterations += r.iterations;
     if (!error) {
         // fission-rate pin powers normalised to the fuel pin count, from the
-        // last replay's read-back (transport_sweeper.cpp:140-193)
+        // read-back of the replay that ended the solve (transport_sweeper.cpp:
+        // 140-193; later replays leave the row as it is)
         const FlatProblem &f = S.sw->flat();
-        const double *row = h_pins_ + (size_t)slot * pins_stride_;
-        const double scale = f.n_fuel_2d / row[f.n_pin];
+        const double *pr = pins + (size_t)slot * pins_stride;
+        const double scale = f.n_fuel_2d / pr[f.n_pin];
         r.pin_powers.resize(f.n_pin);
-        for (int i = 0; i < f.n_pin; i++) r.pin_powers[i] = row[i] * scale;
+        for (int i = 0; i < f.n_pin; i++) r.pin_powers[i] = pr[i] * scale;
     }
     r.t_done = now();
     done_[r.id] = std::move(r);
@@ -292,6 +318,7 @@ void BatchEngine::rebuild_lists()
     }
     const int items_cap = std::max(1, max_items_phase_ * cap_);
     if (items_cap > shape_.items_cap) shape_.items_cap = items_cap;
+    if ((size_t)shape_.items_cap * 2 > d_items_.n || (size_t)shape_.max_g * 2 > d_nitems_.n) drain();
     if ((size_t)shape_.items_cap * 2 > d_items_.n) d_items_.alloc((size_t)shape_.items_cap * 2);
     if ((size_t)shape_.max_g * 2 > d_nitems_.n) d_nitems_.alloc((size_t)std::max(shape_.max_g, 1) * 2);
 
@@ -338,16 +365,18 @@ void BatchEngine::rebuild_lists()
 }
 
 // One outer iteration of every active solve (EigenSolver::step,
-// eigen_solver.cpp:225-253), captured once per batch shape.
-void BatchEngine::capture()
+// eigen_solver.cpp:225-253), captured once per batch shape into ring r's
+// graph (timed graphs carry events of their own).
+void BatchEngine::capture(int r)
 {
-    if (exec_) {
-        cudaGraphExecDestroy(exec_);
-        exec_ = nullptr;
+    Ring &R = ring_[r];
+    if (R.exec) {
+        cudaGraphExecDestroy(R.exec);
+        R.exec = nullptr;
     }
-    if (graph_) {
-        cudaGraphDestroy(graph_);
-        graph_ = nullptr;
+    if (R.graph) {
+        cudaGraphDestroy(R.graph);
+        R.graph = nullptr;
     }
     BatchViews b{};
     b.gv = d_gv_.p;
@@ -366,25 +395,27 @@ void BatchEngine::capture()
     if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local);
     else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local);
     // pin powers of every active solve, read back with the summary
-    pins_stride_ = shape_.max_pin + 1;
-    if ((size_t)cap_ * pins_stride_ > d_pins_.n) {
+    if (shape_.max_pin + 1 > pins_stride_ || (size_t)cap_ * (shape_.max_pin + 1) > d_pins_.n) {
+        drain();
+        pins_stride_ = shape_.max_pin + 1;
         d_pins_.alloc((size_t)cap_ * pins_stride_);
-        if (h_pins_) cudaFreeHost(h_pins_);
-        h_pins_ = nullptr;
-        MOCGPU_CUDA(cudaMallocHost((void **)&h_pins_, sizeof(double) * (size_t)cap_ * pins_stride_));
     }
 
     const int n_sweeps = shape_.max_g * n_inner_ * 2;
+    R.timed = timing_;
     if (timing_)
-        while ((int)tev_.size() < 2 * n_sweeps) {
+        while ((int)R.tev.size() < 2 * n_sweeps) {
             cudaEvent_t e;
             MOCGPU_CUDA(cudaEventCreate(&e));
-            tev_.push_back(e);
+            R.tev.push_back(e);
         }
-    tev_used_ = 0;
+    R.tev_used = 0;
     const int64_t l0 = launch_count();
     const size_t n_ctr = (size_t)std::max(shape_.max_g, 1) * n_inner_ * 2;
-    if (d_ctr_.n < n_ctr) d_ctr_.alloc(n_ctr);
+    if (d_ctr_.n < n_ctr) {
+        drain();
+        d_ctr_.alloc(n_ctr);
+    }
     MOCGPU_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed));
     try {
         MOCGPU_CUDA(cudaMemsetAsync(d_ctr_.p, 0, n_ctr * sizeof(int), stream_));
@@ -408,7 +439,7 @@ void BatchEngine::capture()
                     const int *nit = d_nitems_.p + (size_t)g * 2 + ph;
                     int *ctr = d_ctr_.p + ((size_t)g * n_inner_ + inner) * 2 + ph;
                     if (timing_)
-                        MOCGPU_CUDA(cudaEventRecordWithFlags(tev_[2 * tev_used_], stream_, cudaEventRecordExternal));
+                        MOCGPU_CUDA(cudaEventRecordWithFlags(R.tev[2 * R.tev_used], stream_, cudaEventRecordExternal));
                     if (precision_ == 0)
                         launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
                                                shape_.max_local, ctr, stream_);
@@ -417,8 +448,8 @@ void BatchEngine::capture()
                                               shape_.max_local, ctr, stream_);
                     if (timing_) {
                         MOCGPU_CUDA(
-                            cudaEventRecordWithFlags(tev_[2 * tev_used_ + 1], stream_, cudaEventRecordExternal));
-                        tev_used_++;
+                            cudaEventRecordWithFlags(R.tev[2 * R.tev_used + 1], stream_, cudaEventRecordExternal));
+                        R.tev_used++;
                     }
                 }
                 if (precision_ == 0) launch_b_epilogue<double>(b, g, !last, stream_);
@@ -428,25 +459,28 @@ void BatchEngine::capture()
         }
         launch_b_k_update(b, stream_);
         launch_b_errors(b, stream_);
-        launch_b_summary(b, d_sum_.p, stream_);
+        // pin powers before the convergence test: a solve that ends in this
+        // replay still gets its final row
         launch_b_pin_powers(b, d_pins_.p, pins_stride_, stream_);
+        launch_b_retire(b, d_sum_.p, stream_);
     } catch (...) {
         cudaGraph_t g = nullptr;
         cudaStreamEndCapture(stream_, &g);
         if (g) cudaGraphDestroy(g);
         throw;
     }
-    MOCGPU_CUDA(cudaStreamEndCapture(stream_, &graph_));
-    MOCGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
-    graph_nodes_ = launch_count() - l0;
-    note_launches(-graph_nodes_); // capture records launches; replays count them
-    captured_ = shape_;
+    MOCGPU_CUDA(cudaStreamEndCapture(stream_, &R.graph));
+    MOCGPU_CUDA(cudaGraphInstantiate(&R.exec, R.graph, 0));
+    R.nodes = launch_count() - l0;
+    note_launches(-R.nodes); // capture records launches; replays count them
+    captured_[r] = shape_;
     st_.captures++;
 }
 
 int BatchEngine::launch()
 {
-    if (in_flight_) MOCGPU_THROW(1, "the previous outer iteration has not been finished");
+    if ((int)flights_.size() >= depth_)
+        MOCGPU_THROW(1, "the pipeline is full: finish() the oldest outer iteration first");
     // continuous batching: fill free slots from the queue, in order
     while (!queue_.empty()) {
         if (try_admit(queue_.front())) {
@@ -470,65 +504,85 @@ int BatchEngine::launch()
     }
     if (lists_dirty_) rebuild_lists();
     if (act_.empty()) return 0;
-    if (!exec_ || shape_ != captured_) capture();
-
-    MOCGPU_CUDA(cudaEventRecord(rep0_, stream_));
-    MOCGPU_CUDA(cudaGraphLaunch(exec_, stream_));
-    MOCGPU_CUDA(cudaEventRecord(rep1_, stream_));
-    note_launches(graph_nodes_);
-    MOCGPU_CUDA(copy_async(h_sum_, d_sum_.p, sizeof(double) * 6 * (size_t)cap_, cudaMemcpyDeviceToHost, stream_));
-    MOCGPU_CUDA(copy_async(h_pins_, d_pins_.p, sizeof(double) * (size_t)cap_ * pins_stride_, cudaMemcpyDeviceToHost,
+    // host buffers rotate over the ring; untimed replays share one graph
+    const int r = (int)(seq_ % ring_.size());
+    const int gr = timing_ ? r : 0;
+    if (!ring_[gr].exec || shape_ != captured_[gr] || ring_[gr].timed != timing_) capture(gr);
+    Ring &R = ring_[r], &GR = ring_[gr];
+    if (R.h_pins_n < (size_t)cap_ * pins_stride_) {
+        if (R.h_pins) cudaFreeHost(R.h_pins);
+        R.h_pins = nullptr;
+        R.h_pins_n = (size_t)cap_ * pins_stride_;
+        MOCGPU_CUDA(cudaMallocHost((void **)&R.h_pins, sizeof(double) * R.h_pins_n));
+    }
+    R.pins_stride = pins_stride_;
+    MOCGPU_CUDA(cudaEventRecord(R.e0, stream_));
+    MOCGPU_CUDA(cudaGraphLaunch(GR.exec, stream_));
+    MOCGPU_CUDA(cudaEventRecord(R.e1, stream_));
+    note_launches(GR.nodes);
+    MOCGPU_CUDA(copy_async(R.h_sum, d_sum_.p, sizeof(double) * kSummaryStride * (size_t)cap_, cudaMemcpyDeviceToHost,
                            stream_));
-    in_flight_ = true;
+    MOCGPU_CUDA(copy_async(R.h_pins, d_pins_.p, sizeof(double) * (size_t)cap_ * pins_stride_, cudaMemcpyDeviceToHost,
+                           stream_));
+    MOCGPU_CUDA(cudaEventRecord(R.e2, stream_));
+    Flight F;
+    F.ring = r;
+    F.timed = timing_;
+    F.graph_ring = gr;
+    for (int s : act_) F.solves.emplace_back(s, slots_[s].id);
+    flights_.push_back(std::move(F));
+    seq_++;
     return (int)act_.size();
 }
 
 int BatchEngine::finish()
 {
-    if (!in_flight_) {
+    if (flights_.empty()) {
         int n = 0;
         for (const Slot &S : slots_) n += S.id >= 0;
         return n;
     }
-    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
-    in_flight_ = false;
+    const Flight F = std::move(flights_.front());
+    flights_.pop_front();
+    Ring &R = ring_[F.ring];
+    // e2 follows the replay's read-back copies (later replays may still run)
+    MOCGPU_CUDA(cudaEventSynchronize(R.e2));
     st_.graph_replays++;
-    st_.outer_iterations += (int64_t)act_.size();
     {
         float ms = 0.f;
-        MOCGPU_CUDA(cudaEventElapsedTime(&ms, rep0_, rep1_));
+        MOCGPU_CUDA(cudaEventElapsedTime(&ms, R.e0, R.e1));
         st_.replay_ms += ms;
     }
-    if (timing_) {
-        for (int i = 0; i < tev_used_; i++) {
+    if (F.timed) {
+        const Ring &GR = ring_[F.graph_ring];
+        for (int i = 0; i < GR.tev_used; i++) {
             float ms = 0.f;
-            MOCGPU_CUDA(cudaEventElapsedTime(&ms, tev_[2 * i], tev_[2 * i + 1]));
+            MOCGPU_CUDA(cudaEventElapsedTime(&ms, GR.tev[2 * i], GR.tev[2 * i + 1]));
             st_.sweep_ms += ms;
         }
-        st_.sweep_launches += tev_used_;
-        for (int s : act_) {
-            const DeviceGeometry &geo = *slots_[s].geo;
+        st_.sweep_launches += GR.tev_used;
+    }
+    for (const auto &sv : F.solves) {
+        const int s = sv.first;
+        Slot &S = slots_[s];
+        if (S.id != sv.second) continue; // retired from an earlier replay's summary
+        const double *o = R.h_sum + (size_t)s * kSummaryStride;
+        const int iters = (int)o[7];
+        if (iters > S.iterations && F.timed) {
+            // the solve ran in this replay (a frozen one keeps its count)
+            const DeviceGeometry &geo = *S.geo;
             st_.sweep_bytes += (double)geo.G * n_inner_ * geo.sweep_bytes();
             st_.sweep_sgu += (int64_t)geo.G * n_inner_ * geo.n_seg;
         }
-    }
-
-    const std::vector<int> act = act_;
-    for (int s : act) {
-        Slot &S = slots_[s];
-        const double *o = h_sum_ + (size_t)s * 6;
-        S.iterations++;
-        const double k = o[0], ek = o[1], ep = o[2];
-        const unsigned status = (unsigned)o[3];
-        const int64_t cits = (int64_t)o[4];
-        if (status & DEV_NONPOSITIVE_PIN_FLUX) {
-            retire(s, 11, "Negative or zero input flux in set_pin_flux", false, k, ek, ep, cits);
-        } else if ((status & DEV_NAN) || !std::isfinite(k)) {
-            retire(s, 12, "Eigenvalue is not a number. Giving up.", false, k, ek, ep, cits);
-        } else if (ek < S.k_tol && ep < S.psi_tol && S.iterations - 1 >= S.min_iter) {
-            retire(s, 0, "", true, k, ek, ep, cits);
-        } else if (S.iterations >= S.max_iter) {
-            retire(s, 0, "", false, k, ek, ep, cits);
+        S.iterations = std::max(S.iterations, iters);
+        switch ((int)o[6]) {
+        case DONE_NONPOSITIVE:
+            retire(s, 11, "Negative or zero input flux in set_pin_flux", false, o, R.h_pins, R.pins_stride);
+            break;
+        case DONE_NAN: retire(s, 12, "Eigenvalue is not a number. Giving up.", false, o, R.h_pins, R.pins_stride); break;
+        case DONE_CONVERGED: retire(s, 0, "", true, o, R.h_pins, R.pins_stride); break;
+        case DONE_MAX_ITER: retire(s, 0, "", false, o, R.h_pins, R.pins_stride); break;
+        default: break;
         }
     }
     int n = 0;
@@ -538,8 +592,8 @@ int BatchEngine::finish()
 
 bool BatchEngine::poll() const
 {
-    if (!in_flight_) return true;
-    cudaError_t e = cudaStreamQuery(stream_);
+    if (flights_.empty()) return true;
+    cudaError_t e = cudaEventQuery(ring_[flights_.front().ring].e2);
     if (e == cudaSuccess) return true;
     if (e == cudaErrorNotReady) return false;
     MOCGPU_CUDA(e);
@@ -554,9 +608,17 @@ int BatchEngine::step()
 
 void BatchEngine::run()
 {
+    // the pipeline stays full: the next replays are on the GPU while the
+    // host reads the oldest one's summary and retires and admits solves
     while (true) {
-        int n = step();
-        if (n == 0 && queue_.empty()) break;
+        while ((int)flights_.size() < depth_) {
+            if (launch() == 0) break;
+        }
+        if (flights_.empty()) {
+            if (queue_.empty()) break;
+            continue; // the queue head was refused; launch() went on to the next
+        }
+        finish();
     }
 }
 

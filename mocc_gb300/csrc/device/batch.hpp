@@ -5,10 +5,13 @@
 // Each solve follows MOCC's EigenSolver::step sequence
 // (src/solvers/eigen_solver.cpp:225-253) with its own k, sources and
 // convergence test; only the launches are shared. Per-solve scalars stay in
-// device memory (StateView::red), so the host reads one small summary per
-// outer iteration. Solves retire as they converge and queued solves take
-// their slots between iterations (continuous batching); admission is gated
-// by a device-memory budget against the solve's segment and state sizes.
+// device memory (StateView::red), and the convergence test itself runs on
+// the device at the end of every replay: a solve that ends is frozen (every
+// later replay skips it), so the host may keep several replays in flight and
+// read each replay's small summary while the next runs. Solves retire as the
+// host reads that they ended, and queued solves take their slots before the
+// next launch (continuous batching); admission is gated by a device-memory
+// budget against the solve's segment and state sizes.
 #pragma once
 
 #include <cstdint>
@@ -63,17 +66,21 @@ class BatchEngine {
     // Admits queued solves that fit, runs one outer iteration of every active
     // solve and retires the finished ones. Returns the number still active.
     int step();
-    // step() in two halves, so that several engines on their own streams can
-    // have their outer iterations on the GPU at the same time: launch()
-    // admits, (re)captures and enqueues one replay and returns at once;
-    // finish() waits for it and retires the finished solves. Both return the
-    // number of active solves.
+    // step() in two halves: launch() admits, (re)captures and enqueues one
+    // replay and returns at once (up to pipeline_depth() replays may be in
+    // flight); finish() waits for the oldest replay in flight and retires the
+    // solves it ended. Both return the number of active solves. Several
+    // engines on their own streams overlap on the GPU the same way.
     int launch();
     int finish();
-    // true when no iteration is in flight or the launched one has completed
-    // (finish() would not block)
+    // true when nothing is in flight or the oldest replay in flight has
+    // completed (finish() would not block)
     bool poll() const;
-    // Steps until nothing is queued or active.
+    int in_flight() const { return (int)flights_.size(); }
+    // replays that launch() may have in flight (1..4, default 2)
+    void set_pipeline_depth(int d);
+    int pipeline_depth() const { return depth_; }
+    // Runs with the pipeline full until nothing is queued or active.
     void run();
     // Finished result of solve `id` (removed from the engine); false if the
     // solve has not finished.
@@ -100,18 +107,42 @@ class BatchEngine {
         std::unique_ptr<Sweeper> sw;
         std::shared_ptr<const DeviceGeometry> geo;
         const Problem *key = nullptr;
-        int max_iter = 0, min_iter = 0, iterations = 0;
-        double k_tol = 0.0, psi_tol = 0.0, t_submit = 0.0, t_admit = 0.0;
+        int iterations = 0; // outer iterations seen in the summaries read so far
+        double t_submit = 0.0, t_admit = 0.0;
         size_t bytes = 0;
+    };
+    // Resources of one replay in flight: its graph (its own when the sweep
+    // launches are timed, whose events must not be re-recorded before they
+    // are read), events around it and pinned copies of its summary and pin
+    // powers.
+    struct Ring {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int64_t nodes = 0;
+        bool timed = false;
+        std::vector<cudaEvent_t> tev; // before/after pairs around sweep launches
+        int tev_used = 0;
+        cudaEvent_t e0 = nullptr, e1 = nullptr; // around the replay
+        cudaEvent_t e2 = nullptr;                // after its read-back copies
+        double *h_sum = nullptr, *h_pins = nullptr;
+        size_t h_pins_n = 0;
+        int pins_stride = 0;
+    };
+    struct Flight {
+        int ring;
+        bool timed;
+        int graph_ring;
+        std::vector<std::pair<int, int64_t>> solves; // (slot, solve id) active at launch
     };
 
     std::shared_ptr<const DeviceGeometry> geometry_for(const Problem &P);
     size_t geometry_estimate(const FlatProblem &f) const;
     bool try_admit(Pending &p);
-    void retire(int slot, int error, const std::string &msg, bool converged, double k, double ek, double ep,
-                int64_t cmfd_its);
+    void retire(int slot, int error, const std::string &msg, bool converged, const double *row, const double *pins,
+                int pins_stride);
     void rebuild_lists();
-    void capture();
+    void capture(int r);
+    void drain();
     void check_config(const Problem &P);
 
     int precision_, cap_, bpu_;
@@ -133,7 +164,9 @@ class BatchEngine {
     // retired solve handles kept for reuse, by geometry
     std::map<const Problem *, std::vector<std::unique_ptr<Sweeper>>> pool_;
     size_t pooled_bytes_ = 0;
-    bool in_flight_ = false;
+    int depth_ = 2;
+    int64_t seq_ = 0;
+    std::deque<Flight> flights_;
     BatchStats st_{};
 
     // batch configuration fixed by the first solve
@@ -151,22 +184,15 @@ class BatchEngine {
     DevBuf<int2> d_items_;
     DevBuf<int> d_nitems_;
     DevBuf<int> d_ctr_; // per sweep launch of a replay: next-item counter of the persistent sweep
-    DevBuf<double> d_sum_;
-    double *h_sum_ = nullptr; // pinned summary
-    DevBuf<double> d_pins_;    // [cap][pins_stride_] pin powers of the last replay
-    double *h_pins_ = nullptr; // pinned copy
+    DevBuf<double> d_sum_;  // [cap][kSummaryStride] summary rows of the last replay
+    DevBuf<double> d_pins_; // [cap][pins_stride_] pin powers of the last replay
     int pins_stride_ = 0;
     std::vector<int> act_;
     bool lists_dirty_ = true;
 
-    // graph and the sizes it was captured for
+    // graphs and the sizes they were captured for
     bool timing_ = false;
-    std::vector<cudaEvent_t> tev_; // before/after pairs around sweep launches
-    int tev_used_ = 0;
-    cudaEvent_t rep0_ = nullptr, rep1_ = nullptr;
-    cudaGraph_t graph_ = nullptr;
-    cudaGraphExec_t exec_ = nullptr;
-    int64_t graph_nodes_ = 0;
+    std::vector<Ring> ring_;
     struct Shape {
         int max_fsr = 0, max_pin = 0, max_surf = 0, max_cell = 0, max_g = 0, max_local = 0, items_cap = 0;
         bool operator!=(const Shape &o) const
@@ -174,7 +200,8 @@ class BatchEngine {
             return max_fsr != o.max_fsr || max_pin != o.max_pin || max_surf != o.max_surf ||
                    max_cell != o.max_cell || max_g != o.max_g || max_local != o.max_local || items_cap != o.items_cap;
         }
-    } shape_, captured_;
+    } shape_;
+    std::vector<Shape> captured_; // per ring
     int max_items_phase_ = 0; // capacity of one (group, phase) item list
 };
 

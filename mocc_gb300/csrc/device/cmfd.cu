@@ -926,6 +926,7 @@ __global__ void __launch_bounds__(512) kb_cmfd_solve(BatchViews b, int vec_in_sm
     if ((int)blockIdx.x >= *b.n_act) return;
     const int slot = b.act[blockIdx.x];
     CmfdView c = b.cv[slot];
+    if (c.red[RED_DONE] != 0.0) return; // finished: frozen
     c.has_radial = (c.red[RED_HAS_RADIAL] != 0.0) ? 1 : 0;
     cmfd_body(c, vec_in_smem); // the CTA's shared memory is sized for the largest mesh of the batch
     if (threadIdx.x == 0) c.red[RED_CMFD_ITS] += c.stats[0];

@@ -632,7 +632,8 @@ void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStr
     if ((int)blockIdx.y >= *b.n_act) return;                                                                         \
     const int slot = b.act[blockIdx.y];                                                                              \
     const GeomView &g = b.gv[slot];                                                                                  \
-    const StateView &st = b.sv[slot];
+    const StateView &st = b.sv[slot];                                                                                \
+    if (st.red[RED_DONE] != 0.0) return; /* finished: frozen */
 
 static dim3 bgrid(int n, int block, int cap) { return dim3((unsigned)((n + block - 1) / block), (unsigned)cap); }
 
@@ -818,6 +819,7 @@ __global__ void kb_k_update(BatchViews b)
     const int slot = b.act[blockIdx.x];
     const GeomView &g = b.gv[slot];
     const StateView &st = b.sv[slot];
+    if (st.red[RED_DONE] != 0.0) return; // finished: frozen
     const int G = g.G;
     double tn = 0.0, to = 0.0;
     for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
@@ -861,6 +863,7 @@ __global__ void kb_errors(BatchViews b)
     const int slot = b.act[blockIdx.x];
     const GeomView &g = b.gv[slot];
     const StateView &st = b.sv[slot];
+    if (st.red[RED_DONE] != 0.0) return; // finished: frozen
     double na = 0, sa = 0, nb = 0, sb = 0;
     for (int r = threadIdx.x; r < g.n_fsr; r += blockDim.x) {
         double a = st.fs[r], c = st.fs_prev[r];
@@ -890,24 +893,38 @@ void launch_b_errors(const BatchViews &b, cudaStream_t s)
     kb_errors<<<b.cap, 256, 0, s>>>(b);
 }
 
-__global__ void kb_summary(BatchViews b, double *out)
+__global__ void kb_retire(BatchViews b, double *out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *b.n_act) return;
     const int slot = b.act[i];
     const StateView &st = b.sv[slot];
-    double *o = out + (size_t)slot * 6;
-    o[0] = st.red[RED_K];
-    o[1] = st.red[RED_ERR_K];
-    o[2] = st.red[RED_ERR_PSI];
-    o[3] = (double)*st.status;
-    o[4] = st.red[RED_CMFD_ITS];
-    o[5] = st.red[RED_HAS_RADIAL];
+    double *red = st.red;
+    if (red[RED_DONE] != 0.0) return; // ended in an earlier replay: its row stays as it was
+    const double it = red[RED_ITERS] + 1.0;
+    red[RED_ITERS] = it;
+    const double k = red[RED_K], ek = red[RED_ERR_K], ep = red[RED_ERR_PSI];
+    const unsigned status = *st.status;
+    int code = DONE_RUNNING;
+    if (status & DEV_NONPOSITIVE_PIN_FLUX) code = DONE_NONPOSITIVE;
+    else if ((status & DEV_NAN) || !isfinite(k)) code = DONE_NAN;
+    else if (ek < red[RED_K_TOL] && ep < red[RED_PSI_TOL] && it - 1.0 >= red[RED_MIN_ITER]) code = DONE_CONVERGED;
+    else if (it >= red[RED_MAX_ITER]) code = DONE_MAX_ITER;
+    red[RED_DONE] = (double)code;
+    double *o = out + (size_t)slot * kSummaryStride;
+    o[0] = k;
+    o[1] = ek;
+    o[2] = ep;
+    o[3] = (double)status;
+    o[4] = red[RED_CMFD_ITS];
+    o[5] = red[RED_HAS_RADIAL];
+    o[6] = (double)code;
+    o[7] = it;
 }
-void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s)
+void launch_b_retire(const BatchViews &b, double *out, cudaStream_t s)
 {
     note_launch();
-    kb_summary<<<(b.cap + 127) / 128, 128, 0, s>>>(b, out);
+    kb_retire<<<(b.cap + 127) / 128, 128, 0, s>>>(b, out);
 }
 
 // Fission-rate pin powers of every active solve (transport_sweeper.cpp:140-193):
@@ -920,6 +937,7 @@ __global__ void kb_pin_powers(BatchViews b, double *out, int stride)
     const int slot = b.act[blockIdx.x];
     const GeomView &g = b.gv[slot];
     const StateView &st = b.sv[slot];
+    if (st.red[RED_DONE] != 0.0) return; // finished: frozen
     double *row = out + (size_t)slot * stride;
     double tot = 0.0;
     for (int ip = threadIdx.x; ip < g.n_pin; ip += blockDim.x) {

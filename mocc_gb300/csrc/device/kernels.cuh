@@ -122,8 +122,22 @@ enum RedSlot {
     RED_ERR_PSI = 26,    // fission-source L2 change
     RED_N_FISSILE = 27,  // fissile FSR count
     RED_HAS_RADIAL = 28, // 1 once the sweep has tallied coarse currents
-    RED_CMFD_ITS = 29    // CMFD iterations accumulated
+    RED_CMFD_ITS = 29,   // CMFD iterations accumulated
+    // batched solves: the convergence test runs on the device, so the host
+    // can keep replays in flight and a finished solve is frozen at once
+    RED_DONE = 30,       // 0 while the solve runs, else how it ended (BatchDone)
+    RED_ITERS = 31,      // outer iterations done
+    RED_K_TOL = 32,      // the solve's <solver k_tol>, psi_tol, min_iter, max_iter
+    RED_PSI_TOL = 33,
+    RED_MIN_ITER = 34,
+    RED_MAX_ITER = 35
 };
+// How a batched solve ended (RED_DONE and the summary row).
+enum BatchDone { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_NONPOSITIVE = 2, DONE_NAN = 3, DONE_MAX_ITER = 4 };
+// Summary row per slot written by the last kernel of a replay: k, error_k,
+// error_psi, status, CMFD iterations, coarse-current flag, BatchDone, outer
+// iterations.
+constexpr int kSummaryStride = 8;
 
 // Arrays of per-solve views for the batched kernels (device memory), and the
 // list of active solve slots. The active list and its length live in device
@@ -153,8 +167,11 @@ void launch_b_homogenize(const BatchViews &b, cudaStream_t s);
 void launch_b_set_pin_flux(const BatchViews &b, cudaStream_t s);
 void launch_b_k_update(const BatchViews &b, cudaStream_t s); // total fission ratio, k, then fs(k)
 void launch_b_errors(const BatchViews &b, cudaStream_t s);   // error_k, error_psi per solve
-// out[slot * 6 + {0..5}] = k, error_k, error_psi, status, CMFD iterations, has_radial
-void launch_b_summary(const BatchViews &b, double *out, cudaStream_t s);
+// Convergence test of every running solve (eigen_solver.cpp:213: k_tol,
+// psi_tol, min_iter; max_iter; non-positive pin flux and NaN end a solve with
+// an error) and its summary row out[slot * kSummaryStride + ...]. Solves that
+// end are frozen: every batched kernel skips them from the next replay on.
+void launch_b_retire(const BatchViews &b, double *out, cudaStream_t s);
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
 // pin powers of every active solve: out[slot * stride + cell], total at n_pin
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);

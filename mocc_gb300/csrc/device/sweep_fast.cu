@@ -610,7 +610,9 @@ __global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *item
     int it = blockIdx.x;
     while (it < n) {
         const int2 item = items[it];
-        sweep_unit<Real, NPOL, GS, CUR>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y, smem_raw);
+        // solves that ended in an earlier replay are frozen (uniform per CTA)
+        if (b.sv[item.x].red[RED_DONE] == 0.0)
+            sweep_unit<Real, NPOL, GS, CUR>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y, smem_raw);
         if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);
         __syncthreads(); // also: the next unit may overwrite this one's shared data
         it = s_next;

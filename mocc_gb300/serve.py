@@ -6,10 +6,12 @@ each is submitted as soon as its arrival time has passed to the engine
 geometry and state fit the device-memory budget, every active solve of a
 lane advances one power iteration per graph replay, and results are
 collected as solves retire. Lanes run on their own CUDA streams and are
-stepped in a pipeline (finish one lane's iteration, launch its next, move
-on), so their iterations overlap on the GPU: solves with few energy groups
-need not wait for the replays of 23-group solves, and one lane's
-latency-bound CMFD phase runs beside another lane's sweeps. Latency is
+stepped in a pipeline (each lane keeps up to its pipeline depth of outer
+iterations in flight; the host collects a lane's oldest finished iteration
+and launches its next, then moves on), so their iterations overlap on the
+GPU: solves with few energy groups need not wait for the replays of
+23-group solves, and one lane's latency-bound CMFD phase runs beside
+another lane's sweeps. Latency is
 measured from a request's arrival time to the moment its result is read on
 the host, so queueing is included.
 """
@@ -61,7 +63,6 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
     t0 = time.perf_counter()
     nxt = 0
     outstanding = {k: {} for k in engines}  # lane -> {solve id: request index}
-    in_flight = {k: False for k in engines}
     lat = [0.0] * len(requests)
     res = [None] * len(requests)
     done = 0
@@ -75,32 +76,39 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
             outstanding[r.lane][engines[r.lane].submit(r.problem, r.xsl)] = i
             nxt += 1
 
+    def harvest(k, eng):
+        nonlocal done
+        for sid in eng.ready():
+            if sid not in outstanding[k]:
+                continue
+            r = eng.take(sid, max_pins)
+            i = outstanding[k].pop(sid)
+            lat[i] = time.perf_counter() - t0 - requests[i].arrival
+            res[i] = r
+            done += 1
+
     while done < len(requests):
         admit_arrivals()
         busy = False
         progressed = False
         for k, eng in engines.items():
-            if in_flight[k]:
-                busy = True
-                if len(engines) > 1 and not eng.poll():
-                    continue  # another lane may be ready: do not block on this one
+            # the oldest iteration in flight first: retire and collect
+            while eng.in_flight() and (len(engines) == 1 and eng.in_flight() >= eng.depth or eng.poll()):
                 progressed = True
                 eng.finish()
-                in_flight[k] = False
-                for sid in eng.ready():
-                    if sid not in outstanding[k]:
-                        continue
-                    r = eng.take(sid, max_pins)
-                    i = outstanding[k].pop(sid)
-                    lat[i] = time.perf_counter() - t0 - requests[i].arrival
-                    res[i] = r
-                    done += 1
+                harvest(k, eng)
                 admit_arrivals()
-            if outstanding[k] and not in_flight[k]:
-                eng.launch()
-                in_flight[k] = True
-                busy = True
+            # keep the lane's pipeline full while it has work
+            while outstanding[k] and eng.in_flight() < eng.depth:
+                if eng.launch() == 0:
+                    break
                 progressed = True
+            if eng.in_flight():
+                busy = True
+            elif outstanding[k]:
+                # nothing active: finished solves not yet read, or refused ones
+                eng.finish()
+                harvest(k, eng)
         if busy and not progressed:
             time.sleep(5e-5)  # every lane is on the GPU
         if not busy and nxt < len(order):
