@@ -247,6 +247,8 @@ typedef struct mocgpu_batch_stats {
     int64_t sweep_launches;
     double sweep_bytes;   /* algorithmic bytes of the timed sweep launches */
     int64_t sweep_sgu;    /* segment-group updates of the timed sweep launches */
+    int64_t trace_hits, trace_misses; /* mocgpu_batch_submit_xml: traces reused / made */
+    double trace_ms, xs_ms;           /* host time tracing / reading cross sections there */
 } mocgpu_batch_stats;
 
 /* precision: 0 FP64 sweep, 1 FP32 sweep (mixed); capacity: solves advanced
@@ -260,6 +262,14 @@ void mocgpu_batch_destroy(mocgpu_batch *b);
  * for p's materials (same names, groups and fissile flags) and the traced
  * geometry of p is shared. *id names the solve in mocgpu_batch_take. */
 int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xsl_text, int64_t *id);
+/* Queues one solve given as MOCC input text (the XML of MOCC's input
+ * processing, src/input_proc.cpp; xsl_text replaces the library file named
+ * by <material_lib path> when not NULL). Requests with the same XML text
+ * share one traced problem and device geometry: RayData
+ * (src/sweepers/moc/ray_data.cpp:67-343) runs for the first of them only,
+ * later ones read just their cross sections. */
+int mocgpu_batch_submit_xml(mocgpu_batch *b, const char *xml_text, const char *xsl_text, const char *base_dir,
+                            int64_t *id);
 /* Admits what fits, runs one outer iteration of every active solve, retires
  * finished ones; *n_active = solves still active. */
 int mocgpu_batch_step(mocgpu_batch *b, int *n_active);

@@ -65,7 +65,9 @@ class _BatchStats(C.Structure):
                 ("capacity", C.c_int), ("geometries", C.c_int), ("bundles_per_unit", C.c_int),
                 ("bytes_in_use", C.c_double), ("bytes_budget", C.c_double), ("geometry_bytes", C.c_double),
                 ("now", C.c_double), ("replay_ms", C.c_double), ("sweep_ms", C.c_double),
-                ("sweep_launches", C.c_int64), ("sweep_bytes", C.c_double), ("sweep_sgu", C.c_int64)]
+                ("sweep_launches", C.c_int64), ("sweep_bytes", C.c_double), ("sweep_sgu", C.c_int64),
+                ("trace_hits", C.c_int64), ("trace_misses", C.c_int64), ("trace_ms", C.c_double),
+                ("xs_ms", C.c_double)]
 
 
 def library_path() -> Path:
@@ -129,6 +131,7 @@ def load_library(build: bool = True):
         "mocgpu_batch_create": (I, [I, I, D, I, C.POINTER(P)]),
         "mocgpu_batch_destroy": (None, [P]),
         "mocgpu_batch_submit": (I, [P, P, CP, I64P]),
+        "mocgpu_batch_submit_xml": (I, [P, CP, CP, CP, I64P]),
         "mocgpu_batch_step": (I, [P, IP]),
         "mocgpu_batch_run": (I, [P]),
         "mocgpu_batch_launch": (I, [P, IP]),
@@ -461,6 +464,14 @@ class BatchEngine:
     def submit(self, problem: Problem, xsl: str | None = None) -> int:
         i = C.c_int64()
         _check(self._lib.mocgpu_batch_submit(self._h, problem.handle, xsl.encode() if xsl else None, C.byref(i)))
+        return i.value
+
+    def submit_xml(self, xml: str, xsl: str | None = None, base_dir: str = "") -> int:
+        """Queues a solve given as MOCC input text; requests with the same XML
+        share one traced problem (only their cross sections are read)."""
+        i = C.c_int64()
+        _check(self._lib.mocgpu_batch_submit_xml(self._h, xml.encode(), xsl.encode() if xsl else None,
+                                                 base_dir.encode(), C.byref(i)))
         return i.value
 
     def step(self) -> int:

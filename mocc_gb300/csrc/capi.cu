@@ -626,6 +626,15 @@ int mocgpu_batch_submit(mocgpu_batch *b, const mocgpu_problem *p, const char *xs
     });
 }
 
+int mocgpu_batch_submit_xml(mocgpu_batch *b, const char *xml_text, const char *xsl_text, const char *base_dir,
+                            int64_t *id)
+{
+    return guarded([&] {
+        REQUIRE(xml_text && id, "null argument");
+        *id = eng(b).submit_xml(xml_text, xsl_text ? xsl_text : "", base_dir ? base_dir : "");
+    });
+}
+
 int mocgpu_batch_step(mocgpu_batch *b, int *n_active)
 {
     return guarded([&] {
@@ -739,6 +748,10 @@ int mocgpu_batch_get_stats(mocgpu_batch *b, mocgpu_batch_stats *out)
         out->sweep_launches = s.sweep_launches;
         out->sweep_bytes = s.sweep_bytes;
         out->sweep_sgu = s.sweep_sgu;
+        out->trace_hits = s.trace_hits;
+        out->trace_misses = s.trace_misses;
+        out->trace_ms = s.trace_ms;
+        out->xs_ms = s.xs_ms;
     });
 }
 

@@ -140,6 +140,30 @@ int64_t BatchEngine::submit(std::shared_ptr<const Problem> P, const CrossSection
     return queue_.back().id;
 }
 
+int64_t BatchEngine::submit_xml(const std::string &xml_text, const std::string &xsl_text,
+                                const std::string &base_dir)
+{
+    std::shared_ptr<const Problem> P;
+    auto it = traced_.find(xml_text);
+    if (it != traced_.end()) {
+        P = it->second;
+        st_.trace_hits++;
+    } else {
+        const double t = now();
+        std::shared_ptr<const Problem> np(Problem::from_xml(xml_text, xsl_text, base_dir).release());
+        st_.trace_ms += 1e3 * (now() - t);
+        st_.trace_misses++;
+        traced_[xml_text] = np;
+        P = np;
+        if (!xsl_text.empty()) return submit(P, nullptr); // traced with these cross sections
+    }
+    if (xsl_text.empty()) return submit(P, nullptr);
+    const double t = now();
+    CrossSections xs = cross_sections_from_xsl(*P, xsl_text);
+    st_.xs_ms += 1e3 * (now() - t);
+    return submit(P, &xs);
+}
+
 bool BatchEngine::try_admit(Pending &p)
 {
     int slot = -1;

@@ -40,6 +40,9 @@ struct BatchResult {
 
 struct BatchStats {
     int64_t submitted = 0, completed = 0, outer_iterations = 0, graph_replays = 0, captures = 0;
+    int64_t trace_hits = 0, trace_misses = 0; // submit_xml: traced problems reused / traced anew
+    double trace_ms = 0.0;                    // host time spent tracing in submit_xml
+    double xs_ms = 0.0;                       // host time spent reading cross sections in submit_xml
     int active = 0, queued = 0, capacity = 0;
     size_t bytes_in_use = 0, bytes_budget = 0, geometry_bytes = 0;
     int geometries = 0, bundles_per_unit = 0;
@@ -63,6 +66,12 @@ class BatchEngine {
     // Queues one solve of `P` (optionally with other cross sections for the
     // same materials). `P` stays referenced until the solve is admitted.
     int64_t submit(std::shared_ptr<const Problem> P, const CrossSections *xs = nullptr);
+    // Queues one solve given as MOCC input text. Solves whose XML text is
+    // the same share one traced problem (and so one device geometry): the
+    // first such request traces it, later ones read only their cross
+    // sections from `xsl_text` (ray_data.cpp:67-343 runs once per lattice
+    // shape, not once per request).
+    int64_t submit_xml(const std::string &xml_text, const std::string &xsl_text, const std::string &base_dir);
     // Admits queued solves that fit, runs one outer iteration of every active
     // solve and retires the finished ones. Returns the number still active.
     int step();
@@ -161,6 +170,8 @@ class BatchEngine {
         int users = 0;
     };
     std::map<const Problem *, GeoEntry> geos_;
+    // traced problems of submit_xml, by their XML text
+    std::map<std::string, std::shared_ptr<const Problem>> traced_;
     // retired solve handles kept for reuse, by geometry
     std::map<const Problem *, std::vector<std::unique_ptr<Sweeper>>> pool_;
     size_t pooled_bytes_ = 0;

@@ -25,7 +25,8 @@ import numpy as np
 
 @dataclass
 class Request:
-    problem: object          # mocc_gb300.Problem whose traced geometry is used
+    problem: object          # mocc_gb300.Problem whose traced geometry is used, or MOCC XML input text
+                             # (the engine traces each distinct text once)
     xsl: str | None = None   # cross sections for its materials (None: its own)
     arrival: float = 0.0     # seconds after the start of the run
     lane: object = 0         # key of the engine that runs it
@@ -73,7 +74,9 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
         while nxt < len(order) and requests[order[nxt]].arrival <= now:
             i = order[nxt]
             r = requests[i]
-            outstanding[r.lane][engines[r.lane].submit(r.problem, r.xsl)] = i
+            eng = engines[r.lane]
+            sid = eng.submit_xml(r.problem, r.xsl) if isinstance(r.problem, str) else eng.submit(r.problem, r.xsl)
+            outstanding[r.lane][sid] = i
             nxt += 1
 
     def harvest(k, eng):

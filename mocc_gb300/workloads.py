@@ -19,9 +19,97 @@ Workloads (sizes as in the benchmark definitions):
 """
 from __future__ import annotations
 
+import math
 import random
 
-from . import synthetic_xsl
+_M64 = (1 << 64) - 1
+
+
+class _SplitMix64:
+    """splitmix64 stream: raw 64-bit draws identical on every host."""
+
+    def __init__(self, seed: int):
+        self.s = (seed * 0x9E3779B97F4A7C15 + 0x632BE59BD9B4E019) & _M64
+
+    def next(self) -> int:
+        self.s = (self.s + 0x9E3779B97F4A7C15) & _M64
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        return z ^ (z >> 31)
+
+    def uniform(self, a: float = 0.0, b: float = 1.0) -> float:
+        u = float(self.next() >> 11) * (1.0 / 9007199254740992.0)
+        return a + (b - a) * u
+
+    def log_uniform(self, a: float, b: float) -> float:
+        return math.exp(self.uniform(math.log(a), math.log(b)))
+
+
+def _material(rng, ng: int, fuel: bool):
+    """Sigma_a, nu-Sigma_f, Sigma_f, chi and the [to][from] scattering matrix
+    of one synthetic material: Sigma_t log-uniform in [0.2, 2.0]; the
+    out-scatter of each group a fraction U[0.4, 0.95] of Sigma_t, split into
+    self-scatter, downscatter to the next two groups and a small upscatter
+    into the last groups only; fuel nu-Sigma_f U[0.005, 0.5] (Sigma_f =
+    nu-Sigma_f / 2.43) and chi in the first groups."""
+    n_chi = max(3, int(math.floor(3.0 * ng / 7.0 + 0.5)))
+    n_up = max(2, int(math.floor(2.0 * ng / 7.0 + 0.5)))
+    nu = 2.43
+    ab, nf, sf, ch = [0.0] * ng, [0.0] * ng, [0.0] * ng, [0.0] * ng
+    sc = [[0.0] * ng for _ in range(ng)]
+    for f in range(ng):
+        st = rng.log_uniform(0.2, 2.0)
+        c = rng.uniform(0.4, 0.95)
+        w = [0.0] * ng
+        w[f] = rng.uniform(0.4, 0.8)
+        for k in (1, 2):
+            if f + k < ng:
+                w[f + k] = rng.uniform(0.05, 0.4) / k
+        if f > 0 and f - 1 >= ng - n_up:
+            w[f - 1] = rng.uniform(0.01, 0.05)
+        wsum = 0.0
+        for v in w:
+            wsum += v
+        for to in range(ng):
+            sc[to][f] = c * st * w[to] / wsum
+        ab[f] = st * (1.0 - c)
+        if fuel:
+            nf[f] = rng.uniform(0.005, 0.5)
+            sf[f] = nf[f] / nu
+            if f < n_chi:
+                ch[f] = rng.uniform(0.1, 1.0)
+    return ab, nf, sf, ch, sc
+
+
+def synthetic_xsl(seed: int, n_group: int = 7, n_fuel: int = 1, fuel_nf_scale=None, mod_factor: float = 1.0,
+                  fuel_nf_factor: float = 1.0) -> str:
+    """Seeded synthetic .xsl library in MOCC's format: materials fuel1..fuelN
+    (one base fuel, nu-Sigma_f and Sigma_f scaled by ``fuel_nf_scale[i] *
+    fuel_nf_factor``) and a moderator (absorption and scattering scaled by
+    ``mod_factor``). Pure Python, so that a CPU-only run can make the same
+    inputs without the GPU library (same text as ``mocgpu_synthetic_xsl``)."""
+    if n_group < 3:
+        raise ValueError("synthetic library needs at least 3 groups")
+    rng = _SplitMix64(seed)
+    ab, nf, sf, ch, sc = _material(rng, n_group, True)
+    mats = []
+    for i in range(n_fuel):
+        k = (fuel_nf_scale[i] if fuel_nf_scale is not None and i < len(fuel_nf_scale) else 1.0)
+        mats.append((f"fuel{i + 1}", ab, [v * (k * fuel_nf_factor) for v in nf], [v * (k * fuel_nf_factor) for v in sf],
+                     ch, sc))
+    mab, mnf, msf, mch, msc = _material(rng, n_group, False)
+    mats.append(("moderator", [v * mod_factor for v in mab], mnf, msf, mch,
+                 [[v * mod_factor for v in row] for row in msc]))
+    out = ["Synthetic macroscopic cross sections\n", f" {n_group} {len(mats)}\n"]
+    out.append("".join(" %.6e" % (2.0e7 * math.pow(1.0e-8, g / n_group)) for g in range(n_group)) + "\n")
+    for name, a, b, c, d, s in mats:
+        out.append(f"XSMACRO {name} 0\n")
+        for g in range(n_group):
+            out.append(" %.17e %.17e %.17e %.17e\n" % (a[g], b[g], c[g], d[g]))
+        for to in range(n_group):
+            out.append("".join(" %.17e" % s[to][f] for f in range(n_group)) + "\n")
+    return "".join(out)
 
 PITCH = 1.26
 

@@ -2,11 +2,17 @@
 
 FP64 OpenMP restatement of MOCC's 2-D MoC eigenvalue path (see oracle.h for
 the routine-by-routine citations). Used by tests/, ``__graft_entry__.smoke``
-and the CPU-baseline leg of ``bench.py`` as the checker; the product never
-loads it.
+and the CPU legs of ``bench.py`` as the checker; the product never loads it.
 
-``build()`` compiles ``oracle/_build/liboracle.so`` from oracle.cpp with
-g++ (``oracle/Makefile`` holds the same recipe).
+``OracleSolver.from_xml(xml, xsl)`` builds the problem with the oracle's own
+restatement of MOCC's input reading, core mesh, quadrature and ray tracer
+(tracer.cpp) and loads nothing of the library it checks; ``Traced`` exposes
+those traced arrays for comparison. ``OracleSolver(problem)`` instead takes
+the flat arrays of a traced ``mocc_gb300.Problem`` (unit checks of one
+routine on exactly the library's geometry).
+
+``build()`` compiles ``oracle/_build/liboracle.so`` from oracle.cpp and
+tracer.cpp with g++ (``oracle/Makefile`` holds the same recipe).
 """
 from __future__ import annotations
 
@@ -51,10 +57,11 @@ class _R(C.Structure):
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "oracle.cpp"
+    srcs = [HERE / "oracle.cpp", HERE / "tracer.cpp"]
     hdr = HERE / "oracle.h"
-    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-fPIC", "-shared", str(src), "-o"]
-    digest = hashlib.sha256(src.read_bytes() + hdr.read_bytes() + " ".join(cmd).encode()).hexdigest()
+    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-fPIC", "-shared"] + [str(x) for x in srcs] + ["-o"]
+    digest = hashlib.sha256(b"".join(x.read_bytes() for x in srcs) + hdr.read_bytes()
+                            + " ".join(cmd).encode()).hexdigest()
     OUT.mkdir(exist_ok=True)
     lib, stamp = OUT / "liboracle.so", OUT / "liboracle.stamp"
     if not force and lib.exists() and stamp.exists() and stamp.read_text() == digest:
@@ -86,6 +93,10 @@ def load():
             ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
             ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_table_exp", D, [D]),
+            ("orc_trace_error", C.c_char_p, []), ("orc_trace", I, [C.c_char_p, C.c_char_p, I, C.POINTER(V)]),
+            ("orc_traced_destroy", None, [V]), ("orc_traced_problem", C.POINTER(_P), [V]),
+            ("orc_traced_options", C.POINTER(_O), [V]),
+            ("orc_traced_array", I, [V, C.c_char_p, C.POINTER(V), C.POINTER(C.c_int64), C.POINTER(I)]),
         ]:
             fn = getattr(lib, name)
             fn.restype = res
@@ -107,30 +118,67 @@ def table_exp(x: float) -> float:
     return load().orc_table_exp(x)
 
 
+class Traced:
+    """A problem traced by the oracle itself from MOCC input text
+    (``mocc_literal``: MOCC's own corner handling of the coarse walk)."""
+
+    def __init__(self, xml: str, xsl: str, mocc_literal: bool = False):
+        lib = load()
+        h = C.c_void_p()
+        if lib.orc_trace(xml.encode(), xsl.encode(), 1 if mocc_literal else 0, C.byref(h)) != 0:
+            raise RuntimeError("oracle tracer: " + lib.orc_trace_error().decode())
+        self._h, self._lib = h, lib
+        self.problem = lib.orc_traced_problem(h).contents
+        o = lib.orc_traced_options(h).contents
+        self.options = {k: getattr(o, k) for k, _ in _O._fields_}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.orc_traced_destroy(self._h)
+            self._h = None
+
+    def array(self, name: str) -> np.ndarray:
+        """Copy of one traced array (the orc_problem field names)."""
+        d, n, kind = C.c_void_p(), C.c_int64(), C.c_int()
+        if self._lib.orc_traced_array(self._h, name.encode(), C.byref(d), C.byref(n), C.byref(kind)) != 0:
+            raise KeyError(name)
+        ct = {0: C.c_int32, 1: C.c_double, 2: C.c_int64}[kind.value]
+        if n.value == 0:
+            return np.zeros(0, dtype=np.dtype(ct))
+        return np.ctypeslib.as_array(C.cast(d, C.POINTER(ct)), shape=(n.value,)).copy()
+
+
 class OracleSolver:
-    """Oracle over the flat arrays of a traced ``mocc_gb300.Problem``."""
+    """FP64 restatement of MOCC's eigenvalue path on one problem: built with
+    the oracle's own tracer (``from_xml``) or over the flat arrays of a
+    traced ``mocc_gb300.Problem``."""
 
     FIELDS = [f for f, t in _P._fields_ if t is C.c_void_p]
 
     def __init__(self, problem, n_threads: int = 0, **option_overrides):
         lib = load()
-        s = problem.sizes
-        self._keep = {f: np.ascontiguousarray(problem.export(f)) for f in self.FIELDS}
-        p = _P()
-        for k, src in (("ng", "ngroup"), ("n_fsr", "nfsr"), ("n_mat", "nmat"), ("ndir_oct", "ndir_oct"),
-                       ("n_ang", "nang"), ("n_sets", "nsets"), ("pol_per_set", "pol_per_set"), ("nx", "nx"),
-                       ("ny", "ny"), ("n_pin", "npin"), ("n_surf", "nsurf"), ("n_fuel_2d", "nfuel"),
-                       ("n_tracks", "ntracks")):
-            setattr(p, k, int(s[src]))
-        p.n_seg = int(s["nseg"])
-        p.hz = float(problem.export("hz")[0])
-        bc = problem.export("bc")
-        for i in range(6):
-            p.bc[i] = int(bc[i])
-        for f, arr in self._keep.items():
-            setattr(p, f, arr.ctypes.data_as(C.c_void_p))
+        if isinstance(problem, Traced):
+            self._traced = problem
+            p = problem.problem
+            opts = dict(problem.options)
+        else:
+            s = problem.sizes
+            self._keep = {f: np.ascontiguousarray(problem.export(f)) for f in self.FIELDS}
+            p = _P()
+            for k, src in (("ng", "ngroup"), ("n_fsr", "nfsr"), ("n_mat", "nmat"), ("ndir_oct", "ndir_oct"),
+                           ("n_ang", "nang"), ("n_sets", "nsets"), ("pol_per_set", "pol_per_set"), ("nx", "nx"),
+                           ("ny", "ny"), ("n_pin", "npin"), ("n_surf", "nsurf"), ("n_fuel_2d", "nfuel"),
+                           ("n_tracks", "ntracks")):
+                setattr(p, k, int(s[src]))
+            p.n_seg = int(s["nseg"])
+            p.hz = float(problem.export("hz")[0])
+            bc = problem.export("bc")
+            for i in range(6):
+                p.bc[i] = int(bc[i])
+            for f, arr in self._keep.items():
+                setattr(p, f, arr.ctypes.data_as(C.c_void_p))
+            opts = dict(problem.options)
         self._p = p
-        opts = dict(problem.options)
         opts.update(option_overrides)
         o = _O(**{k: opts[k] for k, _ in _O._fields_})
         self._o = o
@@ -138,8 +186,14 @@ class OracleSolver:
         _chk(lib.orc_create(C.byref(p), C.byref(o), n_threads, C.byref(h)))
         self._h = h
         self._lib = lib
-        self.n_group, self.n_reg, self.n_pin = int(s["ngroup"]), int(s["nfsr"]), int(s["npin"])
-        self.nx, self.ny, self.n_surf = int(s["nx"]), int(s["ny"]), int(s["nsurf"])
+        self.n_group, self.n_reg, self.n_pin = int(p.ng), int(p.n_fsr), int(p.n_pin)
+        self.nx, self.ny, self.n_surf = int(p.nx), int(p.ny), int(p.n_surf)
+        self.n_seg = int(p.n_seg)
+
+    @classmethod
+    def from_xml(cls, xml: str, xsl: str, n_threads: int = 0, **option_overrides):
+        """The oracle on a problem it traces itself from MOCC input text."""
+        return cls(Traced(xml, xsl), n_threads=n_threads, **option_overrides)
 
     def __del__(self):
         if getattr(self, "_h", None):

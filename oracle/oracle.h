@@ -5,8 +5,10 @@
  * library (tests/, the smoke check and the benchmark's CPU baseline use
  * it); no product code path links, loads or calls it.
  *
- * It restates, on the same flat problem the GPU library uploads (tracks,
- * quadrature, cross sections), these MOCC routines:
+ * It restates these MOCC routines on a flat problem (tracks, quadrature,
+ * cross sections) that it builds itself from the input text (tracer.cpp:
+ * XML and .xsl reading, core mesh, quadrature, modular ray tracing) or,
+ * for unit checks, takes from the library it checks:
  *   sweep1g                    src/sweepers/moc/moc_sweeper_kernel.inc.hpp:36-180
  *   moc::Current               src/sweepers/moc/moc_current_worker.hpp:137-330
  *   BoundaryCondition          src/core/boundary_condition.cpp:87-191
@@ -109,6 +111,22 @@ int orc_cmfd_solve(orc_solver *s, double *k);
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out);
 /* exponential table check: value of MOCC's table exponential at x */
 double orc_table_exp(double x);
+
+/* The oracle's own path from input text to the flat problem (tracer.cpp):
+ * MOCC's XML input and .xsl library read, the core mesh built, the
+ * quadrature modularised and the rays traced. The orc_traced object owns
+ * every array the returned orc_problem points to. */
+typedef struct orc_traced orc_traced;
+const char *orc_trace_error(void);
+/* mocc_literal != 0: MOCC's own corner handling of the coarse walk (see
+ * tracer.cpp) instead of the rule the checked library follows */
+int orc_trace(const char *xml, const char *xsl, int mocc_literal, orc_traced **out);
+void orc_traced_destroy(orc_traced *t);
+const orc_problem *orc_traced_problem(const orc_traced *t);
+const orc_options *orc_traced_options(const orc_traced *t);
+/* one named array of the traced problem (the orc_problem field names):
+ * *kind 0 int32, 1 double, 2 int64 */
+int orc_traced_array(const orc_traced *t, const char *name, const void **data, int64_t *n, int *kind);
 
 #ifdef __cplusplus
 }

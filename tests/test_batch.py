@@ -71,9 +71,9 @@ def test_mixed_batch_matches_oracle():
     probs = [m.Problem(x, s) for x, s in cases]
     E = m.BatchEngine(precision=1, capacity=8, bundles_per_unit=2)
     res = _run(E, probs)
-    for P, r in zip(probs, res):
+    for (x, xs), r in zip(cases, res):
         assert r["error"] == 0, r["message"]
-        O = oracle.OracleSolver(P)
+        O = oracle.OracleSolver.from_xml(x, xs)  # the oracle's own trace of the same input
         ref = O.solve()
         assert r["converged"] == 1
         assert pcm(r["k"], ref["k"]) < 10.0
@@ -193,9 +193,9 @@ def test_mixed_group_counts_in_one_batch_match_oracle():
     assert sorted(P.sizes["ngroup"] for P in probs) == [7, 7, 23, 23]
     E = m.BatchEngine(precision=1, capacity=4)
     res = _run(E, probs)
-    for P, r in zip(probs, res):
+    for (x, xs), r in zip(cases, res):
         assert r["error"] == 0, r["message"]
-        O = oracle.OracleSolver(P)
+        O = oracle.OracleSolver.from_xml(x, xs)  # the oracle's own trace of the same input
         ref = O.solve()
         assert r["converged"] == 1
         assert pcm(r["k"], ref["k"]) < 10.0
@@ -210,8 +210,30 @@ def test_23_group_assembly_in_a_batch_matches_oracle():
     assert P.sizes["ngroup"] == 23 and P.sizes["npin"] == 289
     r = _run(m.BatchEngine(precision=1, capacity=2), [P])[0]
     assert r["error"] == 0, r["message"]
-    O = oracle.OracleSolver(P)
+    O = oracle.OracleSolver.from_xml(xml, xsl)
     ref = O.solve()
     assert r["converged"] == 1
     assert pcm(r["k"], ref["k"]) < 10.0
     assert max_pin_err(r["pin_powers"], O.pin_powers()) < 1e-3
+
+
+def test_requests_given_as_input_text_share_one_trace():
+    # two independently written copies of one lattice input with different
+    # cross sections: the engine traces the lattice once and both solves
+    # run on one device geometry, with the results of separately traced
+    # problems
+    xml, xsl1 = W.lattice_case(3, 8, 0.05, "mixed", seed=1000, mod_factor=0.97)
+    xml2, xsl2 = W.lattice_case(3, 8, 0.05, "mixed", seed=1000, mod_factor=1.04)
+    assert xml2 == xml and xsl1 != xsl2
+    E = m.BatchEngine(precision=1, capacity=4)
+    ids = [E.submit_xml(xml, xsl1), E.submit_xml(xml2, xsl2)]
+    E.run()
+    res = [E.take(i) for i in ids]
+    st = E.stats()
+    assert st["trace_misses"] == 1 and st["trace_hits"] == 1 and st["geometries"] == 1
+    ref = _run(m.BatchEngine(precision=1, capacity=4), [m.Problem(xml, xsl1), m.Problem(xml2, xsl2)])
+    for r, q in zip(res, ref):
+        # float reductions of the currents add in any order: rounding only
+        assert r["error"] == 0 and r["iterations"] == q["iterations"]
+        assert abs(r["k"] - q["k"]) < 1e-9
+        assert np.allclose(r["pin_powers"], q["pin_powers"], rtol=1e-7)

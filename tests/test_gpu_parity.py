@@ -1,4 +1,6 @@
-"""GPU library against the CPU oracle on identical traced problems.
+"""GPU library against the CPU oracle on the same input text (the oracle
+traces it with its own restatement of MOCC's tracer; the two traces agree to
+rounding, tests/test_oracle_tracer.py).
 
 Tolerances: the FP64 path must agree with the FP64 oracle to 1e-10 relative
 per sweep (only the order of floating-point sums differs); the mixed path
@@ -28,11 +30,16 @@ def max_pin_err(p, p_ref):
     return float(np.max(np.abs(p[mask] - p_ref[mask]) / p_ref[mask]))
 
 
+ORACLE_OPTIONS = {k for k, _ in oracle._O._fields_}
+
+
 def _pair(xml, xsl, precision, **opt):
+    """The library's solve and the oracle on its own trace of the same input."""
     P = m.Problem(xml, xsl)
     if opt:
         P.set_options(**opt)
-    return P, m.MoCSweeper(P, precision), oracle.OracleSolver(P)
+    O = oracle.OracleSolver.from_xml(xml, xsl, **{k: v for k, v in opt.items() if k in ORACLE_OPTIONS})
+    return P, m.MoCSweeper(P, precision), O
 
 
 @pytest.mark.parametrize("kernel", [0, 1])

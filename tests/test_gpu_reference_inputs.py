@@ -1,5 +1,6 @@
 """GPU library against the CPU oracle on MOCC's own inputs and on the
-benchmark workloads at their stated sizes.
+benchmark workloads at their stated sizes (the oracle traces every input
+with its own restatement of MOCC's tracer).
 
 * examples/3x3.xml with MOCC's C5G7 library (LS quadrature, rectangular
   reflector mesh, two vacuum faces): full eigenvalue solves;
@@ -35,12 +36,12 @@ def max_pin_err(p, p_ref):
     return float(np.max(np.abs(p[mask] - p_ref[mask]) / p_ref[mask]))
 
 
-def _solve_both(P, precision, max_outer=-1):
+def _solve_both(P, xml, xsl, precision, max_outer=-1):
     S = m.MoCSweeper(P, precision)
     ra = m.EigenSolver(P, sweeper=S).solve(max_outer)
     pa = S.pin_powers()
     S.close()
-    O = oracle.OracleSolver(P)
+    O = oracle.OracleSolver.from_xml(xml, xsl)  # the oracle's own trace of the same input
     rb = O.solve(max_outer)
     return ra, pa, rb, O.pin_powers()
 
@@ -49,7 +50,7 @@ def _solve_both(P, precision, max_outer=-1):
 def test_example_3x3_vs_oracle(ref_example, ref_xsl, precision):
     P = m.Problem(ref_example["3x3"], ref_xsl)
     assert P.sizes["nfsr"] == 1251 and P.sizes["pol_per_set"] == 1
-    ra, pa, rb, pb = _solve_both(P, precision)
+    ra, pa, rb, pb = _solve_both(P, ref_example["3x3"], ref_xsl, precision)
     assert ra["converged"] and rb["converged"]
     if precision == 0:
         assert ra["iterations"] == rb["iterations"]
@@ -64,7 +65,7 @@ def test_example_3x3_vs_oracle(ref_example, ref_xsl, precision):
 def test_example_c5g7_2d_iterates_vs_oracle(ref_example, ref_xsl, precision):
     P = m.Problem(ref_example["c5g7_2d"], ref_xsl)
     assert P.sizes["nfsr"] > 80000 and P.sizes["nseg"] > 9_000_000
-    ra, pa, rb, pb = _solve_both(P, precision, max_outer=3)
+    ra, pa, rb, pb = _solve_both(P, ref_example["c5g7_2d"], ref_xsl, precision, max_outer=3)
     assert ra["iterations"] == rb["iterations"] == 3
     if precision == 0:
         assert abs(ra["k"] - rb["k"]) / rb["k"] < 1e-9
@@ -77,8 +78,9 @@ def test_example_c5g7_2d_iterates_vs_oracle(ref_example, ref_xsl, precision):
 def test_assembly17_fp64_vs_oracle():
     # the plain FP64 path on the 17x17 assembly at its benchmark tracking
     # (16 azimuths per octant, 3 polar angles, 0.03 cm)
-    P = m.Problem(*W.assembly17(precision="double"))
-    ra, pa, rb, pb = _solve_both(P, 0)
+    xml, xsl = W.assembly17(precision="double")
+    P = m.Problem(xml, xsl)
+    ra, pa, rb, pb = _solve_both(P, xml, xsl, 0)
     assert ra["converged"] and rb["converged"]
     assert ra["iterations"] == rb["iterations"]
     assert abs(ra["k"] - rb["k"]) / rb["k"] < 1e-9
@@ -93,7 +95,7 @@ def test_reduced_minicore_vs_oracle(precision):
     xml, xsl = W.minicore(n_lat=9, n_azi=8, spacing=0.05, precision="double")
     P = m.Problem(xml, xsl)
     assert P.sizes["npin"] == 36 * 36
-    ra, pa, rb, pb = _solve_both(P, precision)
+    ra, pa, rb, pb = _solve_both(P, xml, xsl, precision)
     assert ra["converged"] and rb["converged"]
     if precision == 0:
         # the cluster's BiCGSTAB sums in another order than the oracle's and
