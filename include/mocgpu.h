@@ -33,6 +33,7 @@ extern "C" {
 #define MOCGPU_ERR_NONPOSITIVE 11   /* non-positive pin flux in set_pin_flux */
 #define MOCGPU_ERR_NAN 12           /* eigenvalue became NaN */
 #define MOCGPU_ERR_NOT_CONVERGED 13 /* iteration limit reached (result still valid) */
+#define MOCGPU_ERR_CANCELLED 14     /* batched solve cancelled by the caller */
 #define MOCGPU_ERR_CUDA 20          /* CUDA runtime error (out of memory included) */
 #define MOCGPU_ERR_CAPACITY 21      /* over a memory budget or a fixed scratch size */
 #define MOCGPU_ERR_INTERNAL 99
@@ -292,6 +293,16 @@ int mocgpu_batch_in_flight(mocgpu_batch *b, int *n);
 int mocgpu_batch_poll(mocgpu_batch *b, int *done);
 /* Runs with the pipeline full until nothing is queued or active. */
 int mocgpu_batch_run(mocgpu_batch *b);
+/* Cancels solve id (no MOCC counterpart): a queued solve leaves the queue,
+ * an active one its slot; its result then reports MOCGPU_ERR_CANCELLED.
+ * Replays already launched may still advance it (their results are
+ * dropped); the other solves are not disturbed. *found = 0 when id is
+ * unknown or already finished. */
+int mocgpu_batch_cancel(mocgpu_batch *b, int64_t id, int *found);
+/* Test hook (no MOCC counterpart): after `after` more device allocations
+ * the next one fails as out of memory (MOCGPU_ERR_CUDA), once; negative
+ * switches it off. */
+int mocgpu_debug_fail_allocations(int64_t after);
 /* *ready = 1 and the result (removed from the engine) once solve id is done;
  * pin_powers (may be NULL) receives res->n_pin values. */
 int mocgpu_batch_take(mocgpu_batch *b, int64_t id, int *ready, mocgpu_batch_result *res, double *pin_powers,

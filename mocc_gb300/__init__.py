@@ -138,6 +138,8 @@ def load_library(build: bool = True):
         "mocgpu_batch_finish": (I, [P, IP]),
         "mocgpu_batch_poll": (I, [P, IP]),
         "mocgpu_batch_set_pipeline_depth": (I, [P, I]),
+        "mocgpu_batch_cancel": (I, [P, C.c_int64, IP]),
+        "mocgpu_debug_fail_allocations": (I, [C.c_int64]),
         "mocgpu_batch_in_flight": (I, [P, IP]),
         "mocgpu_batch_take": (I, [P, C.c_int64, IP, C.POINTER(_BatchResult), DP, I]),
         "mocgpu_batch_get_stats": (I, [P, C.POINTER(_BatchStats)]),
@@ -410,6 +412,12 @@ def copy_bytes() -> tuple[int, int]:
     return h.value, d.value
 
 
+def fail_allocations_after(n: int):
+    """Test hook: after n more device allocations the next fails as out of
+    memory (once); a negative n switches it off."""
+    _check(load_library().mocgpu_debug_fail_allocations(n))
+
+
 def launch_count() -> int:
     n = C.c_int64()
     _check(load_library().mocgpu_launch_count(C.byref(n)))
@@ -509,6 +517,12 @@ class BatchEngine:
         n = C.c_int()
         _check(self._lib.mocgpu_batch_finish(self._h, C.byref(n)))
         return n.value
+
+    def cancel(self, solve_id: int) -> bool:
+        """Cancels a queued or active solve; its result reports error 14."""
+        f = C.c_int()
+        _check(self._lib.mocgpu_batch_cancel(self._h, solve_id, C.byref(f)))
+        return bool(f.value)
 
     def take(self, solve_id: int, n_pin_max: int = 1 << 16):
         """Result dict of a finished solve (None while it runs)."""

@@ -635,6 +635,19 @@ int mocgpu_batch_submit_xml(mocgpu_batch *b, const char *xml_text, const char *x
     });
 }
 
+int mocgpu_batch_cancel(mocgpu_batch *b, int64_t id, int *found)
+{
+    return guarded([&] {
+        REQUIRE(found, "null argument");
+        *found = eng(b).cancel(id) ? 1 : 0;
+    });
+}
+
+int mocgpu_debug_fail_allocations(int64_t after)
+{
+    return guarded([&] { mocgpu::set_alloc_fault(after); });
+}
+
 int mocgpu_batch_step(mocgpu_batch *b, int *n_active)
 {
     return guarded([&] {

@@ -225,18 +225,26 @@ bool BatchEngine::try_admit(Pending &p)
         in_use_ += geo->bytes();
     }
     GeoEntry &ge = geos_[p.P.get()];
-    ge.users++;
 
     Slot &S = slots_[slot];
     if (reuse) {
         S.sw = std::move(pit->second.back());
         pit->second.pop_back();
-        S.sw->rebind(*p.P, p.xs.get());
         pooled_bytes_ -= S.sw->state_bytes();
+        in_use_ -= S.sw->state_bytes(); // counted again below
+        try {
+            S.sw->rebind(*p.P, p.xs.get());
+        } catch (...) {
+            S.sw.reset(); // the handle's memory is released with it
+            throw;
+        }
     } else {
+        // an allocation failure here leaves the engine as it was: the
+        // request stays at the head of the queue
         S.sw = std::make_unique<Sweeper>(*p.P, precision_, stream_, geo, p.xs.get());
-        in_use_ += S.sw->state_bytes();
     }
+    in_use_ += S.sw->state_bytes();
+    ge.users++;
     S.geo = geo;
     S.key = p.P.get();
     S.id = p.id;
@@ -644,6 +652,46 @@ void BatchEngine::run()
         }
         finish();
     }
+}
+
+bool BatchEngine::cancel(int64_t id)
+{
+    auto done = [&](int64_t sid, double t_submit) {
+        BatchResult r;
+        r.id = sid;
+        r.error = 14;
+        r.message = "solve cancelled";
+        r.t_submit = t_submit;
+        r.t_done = now();
+        done_[sid] = std::move(r);
+        st_.completed++;
+    };
+    for (auto it = queue_.begin(); it != queue_.end(); ++it)
+        if (it->id == id) {
+            done(id, it->t_submit);
+            queue_.erase(it);
+            return true;
+        }
+    for (int s = 0; s < cap_; s++) {
+        Slot &S = slots_[s];
+        if (S.id != id) continue;
+        // frozen on the device for replays launched from now on; the slot is
+        // free for the next admission (stream order keeps the new solve's
+        // initialisation after the replays in flight)
+        static const double flag = (double)DONE_CANCELLED;
+        MOCGPU_CUDA(copy_async(S.sw->state().red + RED_DONE, &flag, sizeof(double), cudaMemcpyHostToDevice, stream_));
+        done(id, S.t_submit);
+        pool_[S.key].push_back(std::move(S.sw));
+        pooled_bytes_ += S.bytes;
+        auto g = geos_.find(S.key);
+        if (g != geos_.end()) g->second.users--;
+        S.geo.reset();
+        S.key = nullptr;
+        S.id = -1;
+        lists_dirty_ = true;
+        return true;
+    }
+    return false;
 }
 
 bool BatchEngine::take_result(int64_t id, BatchResult &out)

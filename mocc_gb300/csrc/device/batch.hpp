@@ -91,6 +91,11 @@ class BatchEngine {
     int pipeline_depth() const { return depth_; }
     // Runs with the pipeline full until nothing is queued or active.
     void run();
+    // Cancels solve `id`: a queued solve leaves the queue, an active one its
+    // slot (replays already launched may still advance it; their results
+    // are dropped). Its result reports error 14. False if `id` is unknown or
+    // already finished.
+    bool cancel(int64_t id);
     // Finished result of solve `id` (removed from the engine); false if the
     // solve has not finished.
     bool take_result(int64_t id, BatchResult &out);

@@ -35,6 +35,12 @@ inline cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemc
     return cudaMemcpyAsync(dst, src, bytes, kind, s);
 }
 
+// Test hook: after `after` more device allocations through DevBuf, the next
+// one fails as if the device were out of memory (negative: never). Lets the
+// host's failure paths be tested without exhausting a GPU.
+void set_alloc_fault(int64_t after);
+bool alloc_fault_due();
+
 template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
@@ -51,6 +57,8 @@ template <typename T> struct DevBuf {
     void alloc(size_t count)
     {
         release();
+        if (count && alloc_fault_due())
+            throw ::mocgpu::Error(20, "CUDA error: out of memory (injected allocation failure)");
         n = count;
         if (count) MOCGPU_CUDA(cudaMalloc(&p, count * sizeof(T)));
     }

@@ -32,6 +32,17 @@ void copy_bytes(int64_t *h2d, int64_t *d2h)
     *d2h = g_d2h.load();
 }
 
+static std::atomic<int64_t> g_alloc_fault{-1};
+void set_alloc_fault(int64_t after) { g_alloc_fault.store(after); }
+bool alloc_fault_due()
+{
+    int64_t v = g_alloc_fault.load();
+    while (v >= 0) {
+        if (g_alloc_fault.compare_exchange_weak(v, v - 1)) return v == 0;
+    }
+    return false;
+}
+
 // Function attributes are per device: remember what was set for each
 // (kernel, device, attribute) and raise it only when a launch needs more.
 void raise_func_attr(const void *kernel, cudaFuncAttribute attr, int value)

@@ -133,7 +133,8 @@ enum RedSlot {
     RED_MAX_ITER = 35
 };
 // How a batched solve ended (RED_DONE and the summary row).
-enum BatchDone { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_NONPOSITIVE = 2, DONE_NAN = 3, DONE_MAX_ITER = 4 };
+enum BatchDone { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_NONPOSITIVE = 2, DONE_NAN = 3, DONE_MAX_ITER = 4,
+                 DONE_CANCELLED = 5 };
 // Summary row per slot written by the last kernel of a replay: k, error_k,
 // error_psi, status, CMFD iterations, coarse-current flag, BatchDone, outer
 // iterations.

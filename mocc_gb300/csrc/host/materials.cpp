@@ -107,6 +107,18 @@ MaterialLib MaterialLib::from_xsl_text(const std::string &text)
             for (int f = 0; f < ml.ng; f++) mat.scat[(size_t)to * ml.ng + f] = v[f];
         }
         mat.finalize();
+        // a solve on a non-finite or non-positive transport cross section
+        // would only end in a NaN eigenvalue: refuse the library instead
+        for (int g = 0; g < ml.ng; g++) {
+            const double vals[5] = {mat.xstr[g], mat.xsab[g], mat.xsnf[g], mat.xsf[g], mat.xsch[g]};
+            for (double v : vals)
+                if (!std::isfinite(v)) MOCGPU_THROW(4, "non-finite cross section in material " + mat.name);
+            if (!(mat.xstr[g] > 0.0))
+                MOCGPU_THROW(4, "non-positive transport cross section in material " + mat.name + ", group " +
+                                    std::to_string(g + 1));
+        }
+        for (double v : mat.scat)
+            if (!std::isfinite(v)) MOCGPU_THROW(4, "non-finite scattering cross section in material " + mat.name);
         ml.by_name[mat.name] = m;
         ml.lib.push_back(std::move(mat));
     }

@@ -61,6 +61,11 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
         else if (p == "mixed" || p == "single" || p == "fp32") o.precision = 1;
         else MOCGPU_THROW(7, "Unrecognized precision option (double|mixed).");
     }
+    if (sweeper->has_attr("bundles_per_unit")) {
+        o.bundles_per_unit = sweeper->attr_int("bundles_per_unit", -1);
+        if (o.bundles_per_unit < 0 || o.bundles_per_unit > 4)
+            MOCGPU_THROW(7, "bundles_per_unit must be 0 (automatic) or 1..4.");
+    }
     if (sweeper->has_attr("kernel")) {
         std::string k = sanitize(sweeper->attr("kernel"));
         if (k == "plain") o.sweep_kernel = 0;

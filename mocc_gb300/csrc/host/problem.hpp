@@ -29,6 +29,7 @@ struct SolverOptions {
     bool gs_boundary = true; // Gauss-Seidel (default) or Jacobi boundary update
     int precision = 0;       // 0: FP64 sweep, 1: FP32 sweep + FP64 reductions/CMFD
     int sweep_kernel = 1;    // 0: one thread per track (plain), 1: bundled work units
+    int bundles_per_unit = 0; // bundled sweep work-unit shape (1..4 bundles of 32 tracks), 0: chosen from the size
 };
 
 // Flat problem description. Angles cover octants 1-4 (2-D); tracks are

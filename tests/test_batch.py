@@ -233,7 +233,8 @@ def test_requests_given_as_input_text_share_one_trace():
     assert st["trace_misses"] == 1 and st["trace_hits"] == 1 and st["geometries"] == 1
     ref = _run(m.BatchEngine(precision=1, capacity=4), [m.Problem(xml, xsl1), m.Problem(xml2, xsl2)])
     for r, q in zip(res, ref):
-        # float reductions of the currents add in any order: rounding only
-        assert r["error"] == 0 and r["iterations"] == q["iterations"]
-        assert abs(r["k"] - q["k"]) < 1e-9
-        assert np.allclose(r["pin_powers"], q["pin_powers"], rtol=1e-7)
+        # float reductions (FP32 side path of the tally, crossing currents)
+        # add in any order: the same tolerance as a solve alone and in a mix
+        assert r["error"] == 0
+        assert abs(r["k"] - q["k"]) < 5e-7 * q["k"]
+        assert np.allclose(r["pin_powers"], q["pin_powers"], rtol=1e-5)
