@@ -71,6 +71,16 @@ typedef struct mocgpu_options {
     int cmfd_max_iter, cmfd_negative_fixup;
     int n_inner, gs_boundary, precision;
     int sweep_kernel; /* 0: one thread per track, 1: bundled work units (default) */
+    int bundles_per_unit; /* bundled sweep: bundles of 32 tracks per work unit, 1..4; 0 chosen from the size */
+    /* boundary angular flux update after each CMFD solve, MoCSweeper::
+     * update_incoming_flux (src/sweepers/moc/moc_sweeper.cpp:255-291):
+     * 0 off (default; MOCC's EigenSolver::do_cmfd has the call commented out,
+     * src/solvers/eigen_solver.cpp:289), 1 as MOCC's code reads the partial
+     * currents (at the index of the track's starting coarse cell), 2 from the
+     * partial currents of the surface each track enters through, vacuum
+     * faces left at zero. XML: <sweeper incoming_update="off|mocc|surface">.
+     * Single solves only; the batch engine refuses it. */
+    int incoming_update;
 } mocgpu_options;
 
 typedef struct mocgpu_result {
@@ -159,6 +169,12 @@ int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in /* [n_
 int mocgpu_pin_powers(mocgpu_sweeper *s, double *out);
 /* CoarseData current and surface flux after the last current sweep, [G][n_surf] */
 int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux);
+/* BoundaryCondition::get_boundary (src/core/boundary_condition.hpp:144-164):
+ * the incoming angular flux entries of one group, every angle of octants
+ * 1-4 in turn, each angle's x-face entries then its y-face entries (MOCC's
+ * layout). Writes min(cap, n) values converted to double and reports n in
+ * *n (out may be NULL with cap 0 to ask for the size). */
+int mocgpu_get_boundary_flux(mocgpu_sweeper *s, int group, double *out, int64_t cap, int64_t *n);
 /* TransportSweeper::get_homogenized_xsmesh (transport_sweeper.hpp:184) with
  * XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363): homogenises
  * the current flux on the device, one region per pin, and copies out the

@@ -43,7 +43,8 @@ class _Options(C.Structure):
                 ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
-                ("precision", C.c_int), ("sweep_kernel", C.c_int)]
+                ("precision", C.c_int), ("sweep_kernel", C.c_int), ("bundles_per_unit", C.c_int),
+                ("incoming_update", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -117,6 +118,7 @@ def load_library(build: bool = True):
         "mocgpu_get_flux": (I, [P, DP]),
         "mocgpu_set_flux": (I, [P, DP]),
         "mocgpu_get_pin_flux_1g": (I, [P, I, DP]),
+        "mocgpu_get_boundary_flux": (I, [P, I, DP, C.c_int64, C.POINTER(C.c_int64)]),
         "mocgpu_set_pin_flux_1g": (I, [P, I, DP, DP]),
         "mocgpu_pin_powers": (I, [P, DP]),
         "mocgpu_get_coarse_currents": (I, [P, DP, DP]),
@@ -349,6 +351,14 @@ class MoCSweeper:
     def set_flux(self, f: np.ndarray):
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.n_reg, self.n_group)
         _check(self._lib.mocgpu_set_flux(self._h, _dp(f)))
+
+    def boundary_flux(self, g: int) -> np.ndarray:
+        """Incoming boundary angular flux of group g (MOCC's per-group layout)."""
+        n = C.c_int64()
+        _check(self._lib.mocgpu_get_boundary_flux(self._h, g, None, 0, C.byref(n)))
+        out = np.empty(n.value)
+        _check(self._lib.mocgpu_get_boundary_flux(self._h, g, _dp(out), n.value, C.byref(n)))
+        return out
 
     def get_pin_flux_1g(self, g: int) -> np.ndarray:
         out = np.empty(self.n_pin)

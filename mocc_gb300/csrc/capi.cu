@@ -1,6 +1,7 @@
 // extern "C" boundary of the library (declarations in include/mocgpu.h).
 #include "../../include/mocgpu.h"
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -125,6 +126,8 @@ void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
     c->gs_boundary = o.gs_boundary;
     c->precision = o.precision;
     c->sweep_kernel = o.sweep_kernel;
+    c->bundles_per_unit = o.bundles_per_unit;
+    c->incoming_update = o.incoming_update;
 }
 void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
 {
@@ -146,6 +149,10 @@ void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
     o.precision = c->precision;
     REQUIRE(c->sweep_kernel == 0 || c->sweep_kernel == 1, "sweep_kernel must be 0 or 1");
     o.sweep_kernel = c->sweep_kernel;
+    REQUIRE(c->bundles_per_unit >= 0 && c->bundles_per_unit <= 4, "bundles_per_unit must be 0..4");
+    o.bundles_per_unit = c->bundles_per_unit;
+    REQUIRE(c->incoming_update >= 0 && c->incoming_update <= 2, "incoming_update must be 0, 1 or 2");
+    o.incoming_update = c->incoming_update;
 }
 } // namespace
 
@@ -427,6 +434,16 @@ int mocgpu_set_flux(mocgpu_sweeper *s, const double *flux)
     return guarded([&] {
         REQUIRE(flux, "null argument");
         sw(s).set_flux(flux);
+    });
+}
+int mocgpu_get_boundary_flux(mocgpu_sweeper *s, int group, double *out, int64_t cap, int64_t *n)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(n && group >= 0 && group < S.flat().ng && cap >= 0 && (out || cap == 0), "bad argument");
+        std::vector<double> v = S.get_boundary(group);
+        *n = (int64_t)v.size();
+        std::copy(v.begin(), v.begin() + std::min<int64_t>(cap, (int64_t)v.size()), out);
     });
 }
 int mocgpu_get_pin_flux_1g(mocgpu_sweeper *s, int group, double *out)

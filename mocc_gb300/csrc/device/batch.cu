@@ -92,6 +92,7 @@ void BatchEngine::check_config(const Problem &P)
 {
     const SolverOptions &o = P.opts;
     if (!o.gs_boundary) MOCGPU_THROW(1, "the batched engine runs the Gauss-Seidel boundary update only");
+    if (o.incoming_update) MOCGPU_THROW(1, "the batched engine does not run the incoming boundary flux update");
     const bool cm = o.cmfd && o.cmfd_enabled;
     if (!configured_) {
         pol_ = P.flat.pol_per_set;

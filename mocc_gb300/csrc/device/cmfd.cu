@@ -1126,3 +1126,116 @@ void launch_cmfd_solve_static(const CmfdView &c, cudaStream_t s)
 }
 
 } // namespace mocgpu
+
+// ---------------------------------------------------------------------------
+// Incoming boundary angular flux from the CMFD solution
+// (MoCSweeper::update_incoming_flux, moc_sweeper.cpp:255-291, reading the
+// partial currents of CMFD::store_currents, cmfd.cpp:555-638). Off unless the
+// solve's options ask for it, as in MOCC, whose call of it is commented out
+// (eigen_solver.cpp:289).
+namespace mocgpu {
+
+namespace {
+
+// CMFD::store_currents: net current and surface flux of every surface from
+// the solved coarse flux, and the two partial currents from them. Of the
+// partial currents the update reads only 2 (J+ + J-); that is stored per
+// [G][n_surf], the previous solve's values moving to part_old first.
+__global__ void k_store_partials(CmfdView c, double *part, double *part_old)
+{
+    const int ns = c.n_surf, n = c.n_cell;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < c.G * ns; idx += gridDim.x * blockDim.x) {
+        const int g = idx / ns, is = idx % ns;
+        int c1, c2, nrm;
+        surf_info(c, is, c1, c2, nrm);
+        const double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
+        const double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
+        const double dt = c.d_tilde[idx], dh = c.d_hat[idx], st = c.s_tilde[idx], sh = c.s_hat[idx];
+        const double j = -dt * (fr - fl) + dh * (fr + fl);
+        const double sf = (c1 >= 0) ? st * fl + (1.0 - st) * fr + sh * (fl + fr) : st * fr + sh * (fl + fr);
+        const double jp = 0.25 * sf + 0.5 * j, jm = 0.25 * sf - 0.5 * j;
+        part_old[idx] = part[idx];
+        part[idx] = 2.0 * (jp + jm);
+    }
+}
+
+// One boundary entry: scaled by the change of 2 (J+ + J-) on its surface
+// since the previous CMFD solve, or (first solve) set to the isotropic
+// angular flux 2 (J+ + J-) / 4pi.
+__device__ __forceinline__ double incoming_value(double in, const double *part, const double *part_old, int idx,
+                                                 int has_old)
+{
+    if (has_old) {
+        const double old = part_old[idx];
+        return old > 0.0 ? in * (part[idx] / old) : in;
+    }
+    return (2.0 / (4.0 * 3.1415926535897932)) * (0.5 * part[idx]);
+}
+
+// Which surface a boundary entry reads, and whether it is left alone:
+// mode 1 reads the partial currents at the index of the track's starting
+// coarse cell as MOCC's update_incoming_generic does (moc_sweeper.hpp:
+// 198-233: ray.cm_cell_fw() passed where a surface index is taken, which
+// lands on the cell's bottom z-face); mode 2 reads the core-boundary surface
+// the track enters through and leaves entries on vacuum faces at zero.
+__device__ __forceinline__ int entry_surface(const CmfdView &c, int cell, int surf, int mode)
+{
+    if (mode == 1) return (cell >= 0 && cell < c.n_surf) ? cell : -1;
+    if (surf < 0 || surf >= c.n_surf) return -1;
+    int c1, c2, nrm;
+    surf_info(c, surf, c1, c2, nrm);
+    int face = (nrm == X_NORM) ? (c1 < 0 ? WEST : EAST) : (nrm == Y_NORM) ? (c1 < 0 ? SOUTH : NORTH) : -1;
+    if (face < 0 || (c1 >= 0 && c2 >= 0)) return -1;
+    return c.bc[face] == (int)BoundaryType::VACUUM ? -1 : surf;
+}
+
+// update_incoming_generic: every (group, track, polar angle) rewrites the two
+// boundary entries its track starts from, forward and backward. Each entry
+// is the start of exactly one track in its direction, so no two threads
+// write the same entry.
+template <typename Real>
+__global__ void k_incoming_update(GeomView gv, CmfdView c, Real *psi_in, const double *part, const double *part_old,
+                                  int mode, int has_old)
+{
+    const int per_g = gv.n_tracks * gv.pol;
+    const int total = gv.G * per_g;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int g = idx / per_g, r = idx % per_g, t = r / gv.pol, p = r % gv.pol;
+        const SetPolar &sp = gv.sp[gv.trk_set[t] * gv.pol + p];
+        const int4 e = gv.trk_entry[t];
+        Real *psi = psi_in + (size_t)g * gv.bc_per_group;
+        const int s1 = entry_surface(c, e.x, e.z, mode), s2 = entry_surface(c, e.y, e.w, mode);
+        const size_t gs = (size_t)g * c.n_surf;
+        if (s1 >= 0) {
+            Real &v = psi[gv.bc_off[sp.ang_fwd] + gv.trk_bc0[t]];
+            v = (Real)incoming_value((double)v, part + gs, part_old + gs, s1, has_old);
+        }
+        if (s2 >= 0) {
+            Real &v = psi[gv.bc_off[sp.ang_bwd] + gv.trk_bc1[t]];
+            v = (Real)incoming_value((double)v, part + gs, part_old + gs, s2, has_old);
+        }
+    }
+}
+
+} // namespace
+
+void launch_incoming_update(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, double *part,
+                            int mode, int has_old, cudaStream_t s)
+{
+    if (mode != 1 && mode != 2) throw Error(1, "incoming update mode must be 1 (MOCC) or 2 (entry surface)");
+    double *part_old = part + (size_t)c.G * c.n_surf;
+    const int n1 = c.G * c.n_surf;
+    note_launch_external();
+    k_store_partials<<<(n1 + 255) / 256, 256, 0, s>>>(c, part, part_old);
+    const int64_t n2 = (int64_t)gv.G * gv.n_tracks * gv.pol;
+    const int blocks = (int)std::min<int64_t>((n2 + 255) / 256, 152 * 16);
+    note_launch_external();
+    if (precision == 0)
+        k_incoming_update<double><<<blocks, 256, 0, s>>>(gv, c, static_cast<double *>(psi_in), part, part_old, mode,
+                                                         has_old);
+    else
+        k_incoming_update<float><<<blocks, 256, 0, s>>>(gv, c, static_cast<float *>(psi_in), part, part_old, mode,
+                                                        has_old);
+}
+
+} // namespace mocgpu

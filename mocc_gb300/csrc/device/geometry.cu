@@ -262,6 +262,12 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     trk_bc0_.upload(f.trk_bc0);
     trk_bc1_.upload(f.trk_bc1);
     trk_set_.upload(f.trk_set);
+    {
+        std::vector<int4> te(f.n_tracks);
+        for (int t = 0; t < f.n_tracks; t++)
+            te[t] = make_int4(f.trk_cm_cell_fw[t], f.trk_cm_cell_bw[t], f.trk_cm_surf_fw[t], f.trk_cm_surf_bw[t]);
+        trk_entry_.upload(te);
+    }
     seg_fsr_.upload(f.seg_fsr);
     if (precision == 0) {
         seg_len_d_.upload(f.seg_len);
@@ -324,6 +330,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     g.trk_bc0 = trk_bc0_.p;
     g.trk_bc1 = trk_bc1_.p;
     g.trk_set = trk_set_.p;
+    g.trk_entry = trk_entry_.p;
     g.seg_len = precision == 0 ? (const void *)seg_len_d_.p : (const void *)seg_len_f_.p;
     g.seg_fsr = seg_fsr_.p;
     g.fsr_mat = fsr_mat_.p;
@@ -353,7 +360,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
              ev_fw_pt_.bytes() * 2 + ev_bw_pt_.bytes() * 2 + ev_fw_begin_.bytes() * 2 + wu_.bytes() +
              ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() + psi_init_dev_.bytes() +
              bundle_row_.bytes() + bundle_nrows_.bytes() + bundle_track_.bytes() + local_fsr_.bytes() +
-             blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes();
+             blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes() + trk_entry_.bytes();
     MOCGPU_CUDA(cudaDeviceSynchronize());
 }
 

@@ -253,8 +253,11 @@ __global__ void __launch_bounds__(128) k_sweep(GeomView g, StateView st, int gro
     };
     auto store_out = [&](int ang, int idx, Real v) {
         if (GS) {
-            int tgt = g.wt_tgt[ang * 2 + (idx < ny_set ? 0 : 1)];
-            if (tgt >= 0) psi_in[tgt + idx] = v;
+            // the reflected angle's entry, zeroed on a vacuum face
+            // (BoundaryCondition::update, boundary_condition.cpp:155-191)
+            const int face = idx < ny_set ? 0 : 1;
+            const int tgt = g.wt_tgt[ang * 2 + face];
+            psi_in[g.wt_tgt[3 * g.n_ang + ang * 2 + face] + idx] = tgt >= 0 ? v : (Real)0;
         } else {
             psi_out[g.bc_off[ang] + idx] = v;
         }

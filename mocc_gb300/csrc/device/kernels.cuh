@@ -36,6 +36,7 @@ struct GeomView {
     double hz;
     const int64_t *seg_begin; // n_tracks + 1
     const int *trk_bc0, *trk_bc1, *trk_set;
+    const int4 *trk_entry; // per track: coarse cell and core-boundary surface where each direction starts (fw cell, bw cell, fw surface, bw surface)
     const void *seg_len; // Real
     const int *seg_fsr;
     const int *fsr_mat;
@@ -212,6 +213,13 @@ void launch_cmfd_solve(const CmfdView &c, cudaStream_t s);
 // overlap in time on one device.
 void launch_cmfd_solve_static(const CmfdView &c, cudaStream_t s);
 int static_cmfd_max_cells();
+// MoCSweeper::update_incoming_flux from the CMFD solution in c: stores the
+// partial currents of every surface (part[G][n_surf], the previous ones to
+// part + G * n_surf), then rewrites every track's starting boundary entries
+// of psi_in (Real of the precision). mode 1: MOCC's surface lookup, mode 2:
+// the track's entry surface; has_old: a previous solve's currents exist.
+void launch_incoming_update(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, double *part,
+                            int mode, int has_old, cudaStream_t s);
 void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev, double *red, cudaStream_t s);
 void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s);
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);

@@ -414,8 +414,9 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
 #pragma unroll
         for (int p = 0; p < NPOL; p++) {
             if (GS) {
-                int tgt = U.s_tgt[dir][p][bc_out < U.ny_set ? 0 : 1];
-                if (tgt >= 0) U.psi_in[tgt + bc_out] = psi[p];
+                // reflected angle's entry, or zero on a vacuum face (-1 - offset)
+                const int tgt = U.s_tgt[dir][p][bc_out < U.ny_set ? 0 : 1];
+                U.psi_in[(tgt >= 0 ? tgt : -1 - tgt) + bc_out] = tgt >= 0 ? psi[p] : (Real)0;
             } else {
                 U.psi_out[U.s_off[dir][p] + bc_out] = psi[p];
             }
@@ -459,6 +460,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
 
     // per unit: boundary-flux offsets of every (direction, polar) angle and
     // the reflected angles' incoming offsets for the Gauss-Seidel write-through
+    // (stored as -1 - offset where the face is vacuum: the entry is zeroed,
+    // as BoundaryCondition::update does, boundary_condition.cpp:155-191)
     __shared__ int s_off[2][kMaxPolar], s_tgt[2][kMaxPolar][2];
     __shared__ unsigned s_mbits; // largest |qbar| or incoming |psi| of the unit (float bits)
     U.s_off = s_off;
@@ -469,8 +472,10 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         const int a = dir == 0 ? sp.ang_fwd : sp.ang_bwd;
         s_off[dir][p] = g.bc_off[a];
         if (GS) {
-            s_tgt[dir][p][0] = g.wt_tgt[a * 2];
-            s_tgt[dir][p][1] = g.wt_tgt[a * 2 + 1];
+            for (int n = 0; n < 2; n++) {
+                const int base = g.wt_tgt[3 * g.n_ang + a * 2 + n];
+                s_tgt[dir][p][n] = g.wt_tgt[a * 2 + n] >= 0 ? base : -1 - base;
+            }
         }
     }
     if (FIXED && threadIdx.x == 0) s_mbits = 0u;

@@ -15,6 +15,7 @@ size_t Sweeper::state_bytes_for(const FlatProblem &f, int precision, int bcpg)
     d += 2 * G * n + 3 * n;                               // phi, phi_old, fs, fs_prev, src1g
     d += 2 * G * ns;                                      // currents, surface flux
     d += G * nc + 5 * nc * G + nc * G * G + 4 * G * ns;   // coarse flux, homogenised data, coupling
+    d += 2 * G * ns;                                      // partial-current sums, this and the previous CMFD solve
     d += G * 6 * nc + 2 * nc + 12 * nc + 8 + nc + 1 + 64; // CMFD operator, sources, vectors, stats, pins, red
     return d * sizeof(double) + rb * (3 * n + (G + 1) * (size_t)bcpg) + 2 * ns * sizeof(float) + sizeof(unsigned);
 }
@@ -85,6 +86,8 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     dhat_.alloc((size_t)G * f.n_surf);
     stil_.alloc((size_t)G * f.n_surf);
     shat_.alloc((size_t)G * f.n_surf);
+    part_.alloc((size_t)2 * G * f.n_surf);
+    part_.zero(stream_);
     cmat_.alloc((size_t)G * 6 * nc);
     cfs_.alloc(nc);
     cfs_old_.alloc(nc);
@@ -252,9 +255,22 @@ void Sweeper::initialize()
     sflux_.zero(stream_);
     cur32_.zero(stream_);
     status_.zero(stream_);
+    part_.zero(stream_);
+    cmfd_solves_ = 0;
     has_radial_ = false;
     sweeps_done = 0;
     cmfd_iters = 0;
+}
+
+// MoCSweeper::update_incoming_flux after a CMFD solve, when the options ask
+// for it (MOCC's EigenSolver::do_cmfd has the call commented out,
+// eigen_solver.cpp:289, so the default leaves the boundary flux alone).
+void Sweeper::after_cmfd()
+{
+    if (opts_.incoming_update)
+        launch_incoming_update(gv_, cv_, psi_in_.p, precision_, part_.p, opts_.incoming_update, cmfd_solves_ > 0 ? 1 : 0,
+                               stream_);
+    cmfd_solves_++;
 }
 
 void Sweeper::calc_fission_source(double k) { launch_fission_source(gv_, sv_, k, stream_); }
@@ -438,6 +454,24 @@ void Sweeper::pin_powers(double *out) const
     for (int i = 0; i < f_.n_pin; i++) out[i] = p[i] * scale;
 }
 
+std::vector<double> Sweeper::get_boundary(int g) const
+{
+    const size_t n = (size_t)geo_->bc_per_group;
+    std::vector<double> out(n);
+    if (precision_ == 0) {
+        MOCGPU_CUDA(copy_async(out.data(), psi_in_.p + (size_t)g * n * sizeof(double), n * sizeof(double),
+                               cudaMemcpyDeviceToHost, stream_));
+        MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+    } else {
+        std::vector<float> f(n);
+        MOCGPU_CUDA(copy_async(f.data(), psi_in_.p + (size_t)g * n * sizeof(float), n * sizeof(float),
+                               cudaMemcpyDeviceToHost, stream_));
+        MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+        std::copy(f.begin(), f.end(), out.begin());
+    }
+    return out;
+}
+
 void Sweeper::get_currents(double *cur, double *sfl) const
 {
     MOCGPU_CUDA(copy_async(cur, cur_.p, cur_.bytes(), cudaMemcpyDeviceToHost, stream_));
@@ -474,6 +508,7 @@ void Sweeper::cmfd_solve(double &k)
     MOCGPU_CUDA(copy_async(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
     launch_cmfd_solve(cv_, stream_);
     launch_set_pin_flux(gv_, phi_.p, cflux_.p, nullptr, status_.p, stream_);
+    after_cmfd();
     MOCGPU_CUDA(copy_async(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(copy_async(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
     check_status();
@@ -498,6 +533,7 @@ void Sweeper::cmfd_solve_static(double &k)
     MOCGPU_CUDA(copy_async(red_.p + RED_K, &k, sizeof(double), cudaMemcpyHostToDevice, stream_));
     launch_cmfd_solve_static(cv_, stream_);
     launch_set_pin_flux(gv_, phi_.p, cflux_.p, nullptr, status_.p, stream_);
+    after_cmfd();
     MOCGPU_CUDA(copy_async(&k, red_.p + RED_K, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     MOCGPU_CUDA(copy_async(cmfd_stats, cstats_.p, sizeof(double) * 5, cudaMemcpyDeviceToHost, stream_));
     check_status();

@@ -67,6 +67,7 @@ class Sweeper {
     double set_pin_flux(int g, const double *in);
     void pin_powers(double *out) const; // [ny][nx], normalised to n_fuel
     void get_currents(double *cur, double *sflux) const;
+    std::vector<double> get_boundary(int g) const; // incoming boundary psi of group g, as double
     // pin-homogenised cross sections of the current flux, [n_pin][G] and [n_pin][G][G]
     void homogenized_xs(double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm, double *scat);
     void set_coarse_enabled(bool on) { coarse_enabled_ = on; }
@@ -111,6 +112,7 @@ class Sweeper {
     void check_status();
     void launch_phase(int g, int phase, bool gs, bool cur);
     void launch_epilogue(int g, bool update_q);
+    void after_cmfd();
 
     FlatProblem f_;
     SolverOptions opts_;
@@ -120,6 +122,7 @@ class Sweeper {
     bool coarse_enabled_ = false;
     bool has_radial_ = false;
     int n_fissile_ = 0;
+    int cmfd_solves_ = 0; // CMFD solves since initialize (the first has no previous partial currents)
     size_t dev_bytes_ = 0;
 
     // cross sections of this solve
@@ -131,6 +134,7 @@ class Sweeper {
     DevBuf<unsigned> status_;
     // CMFD
     DevBuf<double> cflux_, hxs_, hscat_, dtil_, dhat_, stil_, shat_, cmat_, cfs_, cfs_old_, cvec_, cstats_;
+    DevBuf<double> part_; // [2][G][n_surf]: 2 (J+ + J-) of the last CMFD solve, then of the one before
     DevBuf<double> pinbuf_;
 
     GeomView gv_{};

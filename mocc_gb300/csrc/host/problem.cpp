@@ -66,6 +66,13 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
         if (o.bundles_per_unit < 0 || o.bundles_per_unit > 4)
             MOCGPU_THROW(7, "bundles_per_unit must be 0 (automatic) or 1..4.");
     }
+    if (sweeper->has_attr("incoming_update")) {
+        std::string u = sanitize(sweeper->attr("incoming_update"));
+        if (u == "off") o.incoming_update = 0;
+        else if (u == "mocc") o.incoming_update = 1;
+        else if (u == "surface") o.incoming_update = 2;
+        else MOCGPU_THROW(7, "Unrecognized incoming_update option (off|mocc|surface).");
+    }
     if (sweeper->has_attr("kernel")) {
         std::string k = sanitize(sweeper->attr("kernel"));
         if (k == "plain") o.sweep_kernel = 0;

@@ -47,7 +47,7 @@ class _O(C.Structure):
                 ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("incoming_update", C.c_int)]
 
 
 class _R(C.Structure):
@@ -90,6 +90,7 @@ def load():
             ("orc_flux_residual", I, [V, DP]), ("orc_get_flux", I, [V, DP]), ("orc_set_flux", I, [V, DP]),
             ("orc_get_pin_flux_1g", I, [V, I, DP]), ("orc_set_pin_flux_1g", I, [V, I, DP, DP]),
             ("orc_pin_powers", I, [V, DP]), ("orc_get_coarse_currents", I, [V, DP, DP]),
+            ("orc_get_boundary", I, [V, I, DP, C.POINTER(C.c_int64)]),
             ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
             ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_table_exp", D, [D]),
@@ -263,6 +264,14 @@ class OracleSolver:
         sfl = np.empty((self.n_group, self.n_surf))
         _chk(self._lib.orc_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
         return cur, sfl
+
+    def boundary_flux(self, g):
+        """Incoming boundary angular flux of group g (MOCC's per-group layout)."""
+        n = C.c_int64()
+        _chk(self._lib.orc_get_boundary(self._h, g, None, C.byref(n)))
+        out = np.empty(n.value)
+        _chk(self._lib.orc_get_boundary(self._h, g, _dp(out), C.byref(n)))
+        return out
 
     def homogenized_nu_fission(self):
         """Pin-homogenised nu-Sigma_f of the current flux, [n_pin (FSR order)][G]."""

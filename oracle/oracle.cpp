@@ -70,6 +70,10 @@ struct orc_solver {
     // CMFD state ([n_cell][G])
     std::vector<double> cflux, hxstr, hxsnf, hxsf, hxsch, hxsrm, hscat;
     std::vector<double> d_tilde, d_hat, s_tilde, s_hat; // [n_surf][G]
+    // CoarseData::partial_current and partial_current_old, [n_surf][G] pairs
+    std::vector<std::array<double, 2>> partial, partial_old;
+    bool has_old_partial = false;
+    int n_cmfd_solve = 0;
     std::vector<double> mdiag, mW, mE, mS, mN;          // [G][n_cell]
     int64_t sweeps = 0, cmfd_its = 0;
     int n_fissile = 0;
@@ -207,6 +211,8 @@ struct orc_solver {
         hscat.assign((size_t)ncell * G * G, 0.0);
         d_tilde.assign((size_t)nsurf * G, 0.0);
         d_hat = s_tilde = s_hat = d_tilde;
+        partial.assign((size_t)nsurf * G, {0.0, 0.0});
+        partial_old = partial;
         mdiag.assign((size_t)G * ncell, 0.0);
         mW = mE = mS = mN = mdiag;
         for (int r = 0; r < nreg; r++) {
@@ -240,6 +246,10 @@ struct orc_solver {
         has_radial = false;
         sweeps = 0;
         cmfd_its = 0;
+        std::fill(partial.begin(), partial.end(), std::array<double, 2>{0.0, 0.0});
+        partial_old = partial;
+        has_old_partial = false;
+        n_cmfd_solve = 0;
     }
 
     // BoundaryCondition::update(group, angle, out) (boundary_condition.cpp:155-191)
@@ -758,7 +768,75 @@ struct orc_solver {
         }
         for (double &v : cflux)
             if (v < 0.0) v = -v;
+        if (o.incoming_update) store_currents();
+        n_cmfd_solve++;
         cmfd_its += iter;
+    }
+    // CMFD::store_currents (cmfd.cpp:555-638), the partial currents only
+    // (the net currents it also writes back are not read again in 2-D)
+    void store_currents()
+    {
+        for (int g = 0; g < G; g++) {
+            for (int is = 0; is < nsurf; is++) partial_old[(size_t)is * G + g] = partial[(size_t)is * G + g];
+            has_old_partial = n_cmfd_solve > 0;
+            for (int is = 0; is < nsurf; is++) {
+                int c1, c2;
+                neigh_cells(is, c1, c2);
+                double fr = c2 >= 0 ? cflux[(size_t)c2 * G + g] : 0.0;
+                double fl = c1 >= 0 ? cflux[(size_t)c1 * G + g] : 0.0;
+                double dh = d_hat[(size_t)is * G + g], dt = d_tilde[(size_t)is * G + g];
+                double cur = -dt * (fr - fl) + dh * (fr + fl);
+                double sh = s_hat[(size_t)is * G + g], st = s_tilde[(size_t)is * G + g];
+                double sf = (c1 >= 0) ? st * fl + (1.0 - st) * fr + sh * (fl + fr) : st * fr + sh * (fl + fr);
+                partial[(size_t)is * G + g] = {0.25 * sf + 0.5 * cur, 0.25 * sf - 0.5 * cur};
+            }
+        }
+    }
+    // MoCSweeper::update_incoming_flux (moc_sweeper.cpp:255-291) through
+    // update_incoming_generic (moc_sweeper.hpp:198-233). Mode 1 keeps MOCC's
+    // lookup, which passes the ray's starting coarse cell (cm_cell_fw/bw)
+    // where partial_current takes a surface index, so it reads the cell's
+    // bottom z-face. Mode 2 reads the surface the ray enters through
+    // (cm_surf_fw/bw) and leaves vacuum faces at zero.
+    void update_incoming_flux()
+    {
+        auto f = [&](double in, int is, int g) {
+            const auto &pc = partial[(size_t)is * G + g];
+            if (has_old_partial) {
+                const auto &po = partial_old[(size_t)is * G + g];
+                double part = 2.0 * (pc[0] + pc[1]);
+                double part_old = 2.0 * (po[0] + po[1]);
+                if (part_old > 0.0) {
+                    double r = part / part_old;
+                    return in * r;
+                }
+                return in;
+            }
+            return 2.0 * (1.0 / FPI) * (pc[0] + pc[1]);
+        };
+        auto surface = [&](int cell, int surf) {
+            if (o.incoming_update == 1) return cell;
+            int c1, c2;
+            neigh_cells(surf, c1, c2);
+            int nrm = surface_normal(surf);
+            int face = nrm == X_NORM ? (c1 < 0 ? WEST : EAST) : (c1 < 0 ? SOUTH : NORTH);
+            return p.bc[face] == VACUUM ? -1 : surf;
+        };
+        for (int g = 0; g < G; g++) {
+            for (int iang = 0; iang < 2 * ndo(); iang++) {
+                int iang1 = iang, iang2 = reverse(iang);
+                double *bc_fw = &bc_in[(size_t)g * bcpg + bc_off[iang1]];
+                double *bc_bw = &bc_in[(size_t)g * bcpg + bc_off[iang2]];
+                int set = set_of(iang);
+                for (int t = p.set_first_track[set]; t < p.set_first_track[set + 1]; t++) {
+                    int is1 = surface(p.trk_cm_cell_fw[t], p.trk_cm_surf_fw[t]);
+                    int is2 = surface(p.trk_cm_cell_bw[t], p.trk_cm_surf_bw[t]);
+                    int bc1 = p.trk_bc0[t], bc2 = p.trk_bc1[t];
+                    if (is1 >= 0) bc_fw[bc1] = f(bc_fw[bc1], is1, g);
+                    if (is2 >= 0) bc_bw[bc2] = f(bc_bw[bc2], is2, g);
+                }
+            }
+        }
     }
     // EigenSolver::do_cmfd (eigen_solver.cpp:263-291)
     void do_cmfd(double &k)
@@ -773,6 +851,8 @@ struct orc_solver {
             for (int i = 0; i < ncell; i++) pf[i] = cflux[(size_t)i * G + g];
             set_pin_flux_1g(g, pf.data());
         }
+        // the call MOCC leaves commented out, when the options ask for it
+        if (o.incoming_update) update_incoming_flux();
     }
     // Normalize() (util/utils.hpp:29-51)
     static void normalize(std::vector<double> &v)
@@ -959,6 +1039,14 @@ int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux)
                 cur[(size_t)g * s->nsurf + is] = s->current[(size_t)is * s->G + g];
                 sflux[(size_t)g * s->nsurf + is] = s->surface_flux[(size_t)is * s->G + g];
             }
+    });
+}
+int orc_get_boundary(orc_solver *s, int g, double *out, int64_t *n)
+{
+    return guard([&] {
+        if (g < 0 || g >= s->G) throw std::runtime_error("bad group");
+        *n = s->bcpg;
+        if (out) std::copy(s->bc_in.begin() + (size_t)g * s->bcpg, s->bc_in.begin() + (size_t)(g + 1) * s->bcpg, out);
     });
 }
 int orc_homogenized_nu_fission(orc_solver *s, double *out)

@@ -64,6 +64,7 @@ typedef struct orc_options {
     double cmfd_k_tol, cmfd_psi_tol, cmfd_resid_reduction;
     int cmfd_max_iter, cmfd_negative_fixup;
     int n_inner, gs_boundary, precision;
+    int incoming_update; /* 0 off, 1 MoCSweeper::update_incoming_flux as written, 2 entry-surface variant */
 } orc_options;
 
 typedef struct orc_result {
@@ -98,6 +99,9 @@ int orc_get_pin_flux_1g(orc_solver *s, int g, double *out);
 int orc_set_pin_flux_1g(orc_solver *s, int g, const double *in, double *resid);
 int orc_pin_powers(orc_solver *s, double *out);
 int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux);
+/* incoming boundary flux of group g (bc_per_group entries; the count alone
+ * when out is NULL) */
+int orc_get_boundary(orc_solver *s, int g, double *out, int64_t *n);
 /* XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363) of the current
  * flux; writes the pins' nu-Sigma_f, [n_pin, in FSR order][G] */
 int orc_homogenized_nu_fission(orc_solver *s, double *out);

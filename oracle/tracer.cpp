@@ -1364,6 +1364,15 @@ void read_options(const Node &doc, orc_options &o, const Node *&sweeper)
         o.gs_boundary = (b == "jacobi" || b == "j") ? 0 : 1;
     }
     o.precision = 0;
+    // not a MOCC attribute: enables MoCSweeper::update_incoming_flux, whose
+    // call MOCC leaves commented out (eigen_solver.cpp:289)
+    o.incoming_update = 0;
+    if (sweeper->has("incoming_update")) {
+        std::string u = lower(sweeper->attr("incoming_update"));
+        if (u == "mocc") o.incoming_update = 1;
+        else if (u == "surface") o.incoming_update = 2;
+        else if (u != "off") throw Fail("Unrecognized incoming_update option (off|mocc|surface).");
+    }
 }
 
 Quad read_quad(const Node &q)
