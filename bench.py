@@ -88,6 +88,7 @@ def parse():
                          "named mocgpu_timed (branch256: one batch of --cases solves in one engine; assembly17 / "
                          "minicore: one solve); prints a JSON summary, no benchmark line")
     ap.add_argument("--bundles-per-unit", type=int, default=1, help="work-unit shape for --profile-once")
+    ap.add_argument("--sweep-ring", type=int, default=0, help="segment-ring shape index for --profile-once")
     return ap.parse_args()
 
 
@@ -287,8 +288,8 @@ def run_branch(args, rank, world):
 
     import mocc_gb300 as m
     from mocc_gb300 import workloads as W
-    from mocc_gb300.serve import Request, poisson_arrivals, run_batch, serve
-    from mocc_gb300.tune import tune_bundles_per_unit
+    from mocc_gb300.serve import PHASES, Request, poisson_arrivals, run_batch, serve
+    from mocc_gb300.tune import tune_sweep
     m.load_library()
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
@@ -296,10 +297,14 @@ def run_branch(args, rank, world):
     n = len(reqs)
     n_pin_max = max(P.sizes["npin"] for P, _ in bases.values())
 
-    # work-unit shape: autotuned on a 64-case sample
-    tune = tune_bundles_per_unit(lambda b: m.BatchEngine(precision=1, capacity=64, bundles_per_unit=b),
-                                 reqs[:64])
-    bpu = tune["best"]
+    # work-unit shape x segment-ring shape: autotuned on a 64-case sample
+    tune = tune_sweep(lambda b: m.BatchEngine(precision=1, capacity=64, bundles_per_unit=b), reqs[:64])
+    bpu, ring = tune["best"]["bundles_per_unit"], tune["best"]["shape"]
+
+    def engine(**kw):
+        e = m.BatchEngine(precision=1, bundles_per_unit=bpu, **kw)
+        e.set_sweep_shape(ring)
+        return e
 
     sizes = [size for size, ng, xml, xsl in cases]
 
@@ -321,7 +326,7 @@ def run_branch(args, rank, world):
     def make_lanes(plan):
         keys = sorted({lane_of(plan, i) for i in range(n)})
         cap = {k: sum(1 for i in range(n) if lane_of(plan, i) == k) for k in keys}
-        return {k: m.BatchEngine(precision=1, capacity=cap[k], bundles_per_unit=bpu) for k in keys}
+        return {k: engine(capacity=cap[k]) for k in keys}
 
     def timed_batch(lanes, plan):
         """One batch of all cases over the lanes; device span of the run from
@@ -388,7 +393,7 @@ def run_branch(args, rank, world):
     # sweeps with each other's CMFD, which would stretch each launch's
     # events); replays stepped one at a time, so the launches made while all
     # 256 solves are active are reported on their own.
-    RE = m.BatchEngine(precision=1, capacity=n, bundles_per_unit=bpu)
+    RE = engine(capacity=n)
     RE.set_pipeline_depth(1)
     for P, x in reqs:
         RE.submit(P, x)
@@ -437,8 +442,9 @@ def run_branch(args, rank, world):
             "warmup": args.warmup, "ms_per_step": span_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": CONFIG,
-            "setup": {"cases": n, "bundles_per_unit": bpu, "lanes": plan_name(plan), "replicas": world,
-                      "pipeline_depth": 2},
+            "setup": {"cases": n, "bundles_per_unit": bpu,
+                      "sweep_ring": {"rows": tune["best"]["rows"], "stages": tune["best"]["stages"]},
+                      "lanes": plan_name(plan), "replicas": world, "pipeline_depth": 2},
             "lanes_ms_per_batch": {plan_name(k): v for k, v in lane_ms.items()},
             "sgu_per_s": tot["sweep_sgu"] / (tot["sweep_ms"] / 1e3),
             "sgu_per_s_whole_run": world * args.steps * sum(
@@ -480,8 +486,13 @@ def run_branch(args, rank, world):
 
         keys = [(ng, c) for ng in (7, 23) for c in ("small", "large")]
         free_b = torch.cuda.mem_get_info()[0]
-        SE = {k: m.BatchEngine(precision=1, capacity=256, mem_budget=0.8 * free_b / len(keys), bundles_per_unit=bpu)
-              for k in keys}
+        SE = {k: engine(capacity=256, mem_budget=0.8 * free_b / len(keys)) for k in keys}
+        # one outer iteration in flight per lane: a lane admits arriving
+        # requests only between its replays, and with a second replay queued
+        # behind the first an arrival waits for both (measured: at 400 req/s
+        # p50 33 ms at depth 1 against 196 ms at depth 2, the same solves/s)
+        for e in SE.values():
+            e.set_pipeline_depth(1)
         warm = [Request(xml, xsl, 0.0, lane_of_s(size, ng)) for size, ng, xml, xsl in scases[:96]]
         serve(SE, warm, n_pin_max)  # traces the lattices, captures the graphs
         st0 = {k: e.stats() for k, e in SE.items()}
@@ -492,13 +503,24 @@ def run_branch(args, rank, world):
                   for (size, ng, xml, xsl), a in zip(scases[:nreq], arr)]
             rep = serve(SE, rq, n_pin_max)
             per_class = {}
-            for (size, ng, _, _), lat, r in zip(scases[:nreq], rep.latencies_s, rep.results):
-                per_class.setdefault(f"{size}x{size} {ng}g", []).append(lat)
+            for (size, ng, _, _), lat, ph in zip(scases[:nreq], rep.latencies_s, rep.phases_s):
+                per_class.setdefault(f"{size}x{size} {ng}g", []).append((lat, ph))
+
+            def pct(v, q):
+                return 1e3 * float(np.percentile(v, q))
+
+            def phase_ms(rows):
+                return {p: 1e3 * float(np.mean([ph[p] for _, ph in rows])) for p in PHASES}
+
+            slow = sorted(zip(rep.latencies_s, rep.phases_s), key=lambda x: x[0])[-max(1, nreq // 100):]
             runs.append({"rate_req_per_s": rate, "requests": nreq, "solves_per_s": rep.solves_per_s,
                          "p50_ms": rep.percentile_ms(50), "p99_ms": rep.percentile_ms(99),
-                         "per_class_ms": {c: {"n": len(v), "p50": 1e3 * float(np.percentile(v, 50)),
-                                              "p99": 1e3 * float(np.percentile(v, 99))}
+                         "per_class_ms": {c: {"n": len(v), "p50": pct([x[0] for x in v], 50),
+                                              "p99": pct([x[0] for x in v], 99),
+                                              "queue_p50": pct([x[1]["queue"] for x in v], 50),
+                                              "run_p50": pct([x[1]["run"] for x in v], 50)}
                                           for c, v in sorted(per_class.items())},
+                         "slowest_1pct_phases_ms": phase_ms(slow),
                          "all_ok": all(r is not None and r["error"] == 0 for r in rep.results)})
             if rate == 400.0:
                 serve_cases = [(c, r) for c, r in zip(scases[:nreq], rep.results)]
@@ -507,8 +529,10 @@ def run_branch(args, rank, world):
         line["serving"] = {"runs": runs, "mix": "sizes 1/3/7/17 weighted 0.4/0.3/0.2/0.1, groups 7 or 23",
                            "budget": "80% of free device memory, split between the lanes", "capacity": 256,
                            "lanes": "one engine per (group count, lattice class 1-3 / 7-17 pins), pipelined on "
-                                    "four streams",
-                           "latency": "request arrival to result read on the host",
+                                    "four streams, one outer iteration in flight per lane",
+                           "latency": "request arrival to result read on the host; phases: host (arrival to "
+                                      "submit), queue (submit to admission into a slot), run (admission to the "
+                                      "replay that retired it), collect (to the host read)",
                            "setup_ms_per_request": {
                                "trace": sum(st1[k]["trace_ms"] - st0[k]["trace_ms"] for k in SE) / req,
                                "cross_sections": sum(st1[k]["xs_ms"] - st0[k]["xs_ms"] for k in SE) / req,
@@ -692,6 +716,7 @@ def profile_once(args):
         return 0 if r["converged"] else 1
     cases, bases, reqs = branch_workload(args.cases)
     E = m.BatchEngine(precision=1, capacity=max(1, args.cases), bundles_per_unit=args.bundles_per_unit)
+    E.set_sweep_shape(args.sweep_ring)
 
     def batch():
         ids = [E.submit(P, x) for P, x in reqs]

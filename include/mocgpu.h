@@ -184,8 +184,21 @@ int mocgpu_get_boundary_flux(mocgpu_sweeper *s, int group, double *out, int64_t 
 int mocgpu_homogenized_xs(mocgpu_sweeper *s, double *xstr, double *xsnf, double *xsf, double *xsch, double *xsrm,
                           double *scat);
 /* EigenSolver::do_cmfd (eigen_solver.cpp:263-291) incl. CMFD::solve
- * (cmfd.cpp:171-279); k is read and updated */
+ * (cmfd.cpp:171-279); k is read and updated. With the incoming_update
+ * option on, MoCSweeper::update_incoming_flux (moc_sweeper.cpp:255-291)
+ * follows, from the partial currents of CMFD::store_currents
+ * (cmfd.cpp:555-638). */
 int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
+/* MoCSweeper::update_incoming_flux (moc_sweeper.cpp:255-291) from partial
+ * currents that MOCC's own CMFD stored (CMFD::store_currents,
+ * cmfd.cpp:555-638): part and part_old hold 2 (J+ + J-) of every coarse
+ * surface, [G][n_surf], for the last and (has_old != 0) the previous CMFD
+ * solve; part_old may be NULL when has_old is 0. mode 1 reads them as MOCC's
+ * update_incoming_generic does (at the index of each ray's starting coarse
+ * cell), mode 2 at the surface each ray enters through, leaving vacuum
+ * faces at zero. For a MOCC build that keeps its CPU CMFD and calls the
+ * sweeper's update_incoming_flux. */
+int mocgpu_update_incoming_flux(mocgpu_sweeper *s, const double *part, const double *part_old, int has_old, int mode);
 /* mocgpu_cmfd_solve without allocation (no MOCC counterpart). The CMFD work
  * vectors live in a fixed array inside the library (10 x 8192 doubles, 640
  * KiB per device) instead of a buffer of the handle, so no call allocates
@@ -302,6 +315,14 @@ int mocgpu_batch_launch(mocgpu_batch *b, int *n_active);
 int mocgpu_batch_finish(mocgpu_batch *b, int *n_active);
 /* replays launch may have in flight, 1..4 (set with none in flight) */
 int mocgpu_batch_set_pipeline_depth(mocgpu_batch *b, int depth);
+/* Streaming shape of the batched sweep kernel, 0..MOCGPU_SWEEP_SHAPES-1
+ * (set with none in flight; the next replay re-captures its graph): each
+ * shape is a (rows per chunk, chunks in flight) pair of the warps' segment
+ * rings, reported by mocgpu_sweep_shape_info. The FP64 engine has shape 0
+ * only. Chosen per engine by the autotuner (mocc_gb300.tune). */
+#define MOCGPU_SWEEP_SHAPES 5
+int mocgpu_batch_set_sweep_shape(mocgpu_batch *b, int shape);
+int mocgpu_sweep_shape_info(int shape, int *rows, int *stages);
 /* replays launched and not yet finished */
 int mocgpu_batch_in_flight(mocgpu_batch *b, int *n);
 /* *done = 1 when nothing is in flight or the oldest replay in flight has

@@ -119,6 +119,7 @@ def load_library(build: bool = True):
         "mocgpu_set_flux": (I, [P, DP]),
         "mocgpu_get_pin_flux_1g": (I, [P, I, DP]),
         "mocgpu_get_boundary_flux": (I, [P, I, DP, C.c_int64, C.POINTER(C.c_int64)]),
+        "mocgpu_update_incoming_flux": (I, [P, DP, DP, I, I]),
         "mocgpu_set_pin_flux_1g": (I, [P, I, DP, DP]),
         "mocgpu_pin_powers": (I, [P, DP]),
         "mocgpu_get_coarse_currents": (I, [P, DP, DP]),
@@ -140,6 +141,8 @@ def load_library(build: bool = True):
         "mocgpu_batch_finish": (I, [P, IP]),
         "mocgpu_batch_poll": (I, [P, IP]),
         "mocgpu_batch_set_pipeline_depth": (I, [P, I]),
+        "mocgpu_batch_set_sweep_shape": (I, [P, I]),
+        "mocgpu_sweep_shape_info": (I, [I, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "mocgpu_batch_cancel": (I, [P, C.c_int64, IP]),
         "mocgpu_debug_fail_allocations": (I, [C.c_int64]),
         "mocgpu_batch_in_flight": (I, [P, IP]),
@@ -352,6 +355,14 @@ class MoCSweeper:
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(self.n_reg, self.n_group)
         _check(self._lib.mocgpu_set_flux(self._h, _dp(f)))
 
+    def update_incoming_flux(self, part: np.ndarray, part_old: np.ndarray | None = None, mode: int = 1):
+        """MoCSweeper::update_incoming_flux from given 2 (J+ + J-) per [G][n_surf]
+        (part_old: the previous CMFD solve's, None on the first)."""
+        part = np.ascontiguousarray(part, dtype=np.float64)
+        old = None if part_old is None else np.ascontiguousarray(part_old, dtype=np.float64)
+        _check(self._lib.mocgpu_update_incoming_flux(self._h, _dp(part), None if old is None else _dp(old),
+                                                     0 if old is None else 1, mode))
+
     def boundary_flux(self, g: int) -> np.ndarray:
         """Incoming boundary angular flux of group g (MOCC's per-group layout)."""
         n = C.c_int64()
@@ -428,6 +439,17 @@ def fail_allocations_after(n: int):
     _check(load_library().mocgpu_debug_fail_allocations(n))
 
 
+def sweep_shapes() -> list:
+    """(rows per chunk, chunks in flight) of every built batched-sweep shape."""
+    lib, out = load_library(), []
+    r, s = C.c_int(), C.c_int()
+    i = 0
+    while lib.mocgpu_sweep_shape_info(i, C.byref(r), C.byref(s)) == 0:
+        out.append((r.value, s.value))
+        i += 1
+    return out
+
+
 def launch_count() -> int:
     n = C.c_int64()
     _check(load_library().mocgpu_launch_count(C.byref(n)))
@@ -470,6 +492,7 @@ class BatchEngine:
         self._h = h
         self._keep = {}
         self.depth = 2
+        self.sweep_shape = 0
 
     def close(self):
         if getattr(self, "_h", None):
@@ -504,6 +527,11 @@ class BatchEngine:
         """Outer iterations launch() may have in flight (1..4, default 2)."""
         _check(self._lib.mocgpu_batch_set_pipeline_depth(self._h, depth))
         self.depth = depth
+
+    def set_sweep_shape(self, shape: int):
+        """Streaming shape of the batched sweep (index into sweep_shapes())."""
+        _check(self._lib.mocgpu_batch_set_sweep_shape(self._h, shape))
+        self.sweep_shape = shape
 
     def in_flight(self) -> int:
         n = C.c_int()

@@ -489,6 +489,14 @@ int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k)
         sw(s).cmfd_solve(*k);
     });
 }
+int mocgpu_update_incoming_flux(mocgpu_sweeper *s, const double *part, const double *part_old, int has_old, int mode)
+{
+    return guarded([&] {
+        REQUIRE(part && (part_old || !has_old), "null argument");
+        REQUIRE(mode == 1 || mode == 2, "mode must be 1 (MOCC's lookup) or 2 (entry surface)");
+        sw(s).update_incoming_flux(part, part_old, has_old, mode);
+    });
+}
 int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k)
 {
     return guarded([&] {
@@ -692,6 +700,18 @@ int mocgpu_batch_finish(mocgpu_batch *b, int *n_active)
 int mocgpu_batch_set_pipeline_depth(mocgpu_batch *b, int depth)
 {
     return guarded([&] { eng(b).set_pipeline_depth(depth); });
+}
+int mocgpu_batch_set_sweep_shape(mocgpu_batch *b, int shape)
+{
+    return guarded([&] { eng(b).set_sweep_shape(shape); });
+}
+int mocgpu_sweep_shape_info(int shape, int *rows, int *stages)
+{
+    return guarded([&] {
+        REQUIRE(rows && stages, "null argument");
+        static_assert(MOCGPU_SWEEP_SHAPES == mocgpu::kSweepShapeCount, "shape count");
+        mocgpu::sweep_shape_info(shape, rows, stages);
+    });
 }
 int mocgpu_batch_in_flight(mocgpu_batch *b, int *n)
 {

@@ -60,6 +60,17 @@ void BatchEngine::set_pipeline_depth(int d)
     depth_ = d;
 }
 
+void BatchEngine::set_sweep_shape(int shape)
+{
+    int rows = 0, stages = 0;
+    sweep_shape_info(shape, &rows, &stages); // throws for a shape that is not built
+    if (precision_ == 0 && shape != 0) MOCGPU_THROW(1, "the FP64 batched sweep is built in shape 0 only");
+    if (!flights_.empty()) MOCGPU_THROW(1, "change the sweep shape with no replay in flight");
+    if (shape == sweep_shape_) return;
+    sweep_shape_ = shape;
+    for (Shape &c : captured_) c = Shape{}; // force new captures
+}
+
 void BatchEngine::set_timing(bool on)
 {
     if (on == timing_) return;
@@ -425,8 +436,8 @@ void BatchEngine::capture(int r)
     b.max_surf = shape_.max_surf;
     b.max_cell = shape_.max_cell;
     b.max_g = shape_.max_g;
-    if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local);
-    else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local);
+    if (precision_ == 0) prepare_b_sweep<double>(pol_, bpu_, shape_.max_local, sweep_shape_);
+    else prepare_b_sweep<float>(pol_, bpu_, shape_.max_local, sweep_shape_);
     // pin powers of every active solve, read back with the summary
     if (shape_.max_pin + 1 > pins_stride_ || (size_t)cap_ * (shape_.max_pin + 1) > d_pins_.n) {
         drain();
@@ -474,11 +485,11 @@ void BatchEngine::capture(int r)
                     if (timing_)
                         MOCGPU_CUDA(cudaEventRecordWithFlags(R.tev[2 * R.tev_used], stream_, cudaEventRecordExternal));
                     if (precision_ == 0)
-                        launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
-                                               shape_.max_local, ctr, stream_);
+                        launch_b_sweep<double>(b, items, nit, shape_.items_cap, g, cur, pol_, bpu_,
+                                               shape_.max_local, sweep_shape_, ctr, stream_);
                     else
-                        launch_b_sweep<float>(b, items, nit, shape_.items_cap, g, true, cur, pol_, bpu_,
-                                              shape_.max_local, ctr, stream_);
+                        launch_b_sweep<float>(b, items, nit, shape_.items_cap, g, cur, pol_, bpu_, shape_.max_local,
+                                              sweep_shape_, ctr, stream_);
                     if (timing_) {
                         MOCGPU_CUDA(
                             cudaEventRecordWithFlags(R.tev[2 * R.tev_used + 1], stream_, cudaEventRecordExternal));

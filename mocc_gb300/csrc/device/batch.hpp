@@ -88,6 +88,10 @@ class BatchEngine {
     int in_flight() const { return (int)flights_.size(); }
     // replays that launch() may have in flight (1..4, default 2)
     void set_pipeline_depth(int d);
+    // streaming shape of the batched sweep (see kSweepShapeCount); the next
+    // replay re-captures the graphs
+    void set_sweep_shape(int shape);
+    int sweep_shape() const { return sweep_shape_; }
     int pipeline_depth() const { return depth_; }
     // Runs with the pipeline full until nothing is queued or active.
     void run();
@@ -160,6 +164,7 @@ class BatchEngine {
     void check_config(const Problem &P);
 
     int precision_, cap_, bpu_;
+    int sweep_shape_ = 0;
     size_t budget_ = 0, in_use_ = 0;
     cudaStream_t stream_;
     double t0_;

@@ -1223,10 +1223,17 @@ void launch_incoming_update(const GeomView &gv, const CmfdView &c, void *psi_in,
                             int mode, int has_old, cudaStream_t s)
 {
     if (mode != 1 && mode != 2) throw Error(1, "incoming update mode must be 1 (MOCC) or 2 (entry surface)");
-    double *part_old = part + (size_t)c.G * c.n_surf;
     const int n1 = c.G * c.n_surf;
     note_launch_external();
-    k_store_partials<<<(n1 + 255) / 256, 256, 0, s>>>(c, part, part_old);
+    k_store_partials<<<(n1 + 255) / 256, 256, 0, s>>>(c, part, part + (size_t)n1);
+    launch_apply_incoming(gv, c, psi_in, precision, part, mode, has_old, s);
+}
+
+void launch_apply_incoming(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, const double *part,
+                           int mode, int has_old, cudaStream_t s)
+{
+    if (mode != 1 && mode != 2) throw Error(1, "incoming update mode must be 1 (MOCC) or 2 (entry surface)");
+    const double *part_old = part + (size_t)c.G * c.n_surf;
     const int64_t n2 = (int64_t)gv.G * gv.n_tracks * gv.pol;
     const int blocks = (int)std::min<int64_t>((n2 + 255) / 256, 152 * 16);
     note_launch_external();

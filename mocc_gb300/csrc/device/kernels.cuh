@@ -177,11 +177,16 @@ void launch_b_retire(const BatchViews &b, double *out, cudaStream_t s);
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
 // pin powers of every active solve: out[slot * stride + cell], total at n_pin
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
+// Batched sweep (Gauss-Seidel boundary update) in streaming shape `shape`:
+// rows per chunk and chunks in flight of each warp's segment ring, one of
+// kSweepShapeCount built shapes (FP64: shape 0 only).
 template <typename Real>
-void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool gs,
-                    bool cur, int pol, int bundles_per_unit, int max_local, int *counter, cudaStream_t s);
+void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool cur,
+                    int pol, int bundles_per_unit, int max_local, int shape, int *counter, cudaStream_t s);
 // Sets the shared-memory limit of the batched sweep ahead of graph capture.
-template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local);
+template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local, int shape);
+constexpr int kSweepShapeCount = 5;
+void sweep_shape_info(int shape, int *rows, int *stages); // throws for a shape that is not built
 void note_launches(int64_t n); // adds replayed launches to launch_count()
 
 // ---- launchers (stream-ordered) ----
@@ -220,6 +225,9 @@ int static_cmfd_max_cells();
 // the track's entry surface; has_old: a previous solve's currents exist.
 void launch_incoming_update(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, double *part,
                             int mode, int has_old, cudaStream_t s);
+// The second half alone: psi_in rescaled from given partial-current sums.
+void launch_apply_incoming(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, const double *part,
+                           int mode, int has_old, cudaStream_t s);
 void launch_psi_error(const GeomView &g, const double *fs, const double *fs_prev, double *red, cudaStream_t s);
 void launch_flux_residual(const GeomView &g, const StateView &st, double *out, cudaStream_t s);
 void launch_pin_power(const GeomView &g, const double *phi, double *pow, cudaStream_t s);

@@ -265,6 +265,15 @@ void Sweeper::initialize()
 // MoCSweeper::update_incoming_flux after a CMFD solve, when the options ask
 // for it (MOCC's EigenSolver::do_cmfd has the call commented out,
 // eigen_solver.cpp:289, so the default leaves the boundary flux alone).
+void Sweeper::update_incoming_flux(const double *part, const double *part_old, int has_old, int mode)
+{
+    const size_t n = (size_t)f_.ng * f_.n_surf;
+    MOCGPU_CUDA(copy_async(part_.p, part, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    if (has_old) MOCGPU_CUDA(copy_async(part_.p + n, part_old, n * sizeof(double), cudaMemcpyHostToDevice, stream_));
+    launch_apply_incoming(gv_, cv_, psi_in_.p, precision_, part_.p, mode, has_old ? 1 : 0, stream_);
+    MOCGPU_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void Sweeper::after_cmfd()
 {
     if (opts_.incoming_update)

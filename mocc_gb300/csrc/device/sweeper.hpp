@@ -80,6 +80,9 @@ class Sweeper {
     // cmfd_solve with the CMFD work vectors in the library's fixed scratch
     // array instead of this handle's buffer
     void cmfd_solve_static(double &k);
+    // MoCSweeper::update_incoming_flux from partial-current sums computed
+    // elsewhere (2 (J+ + J-) per [G][n_surf], this and the previous CMFD solve)
+    void update_incoming_flux(const double *part, const double *part_old, int has_old, int mode);
     EigenResult eigen_solve(int max_outer = -1);
     void eigen_step(double &k, double &k_prev);
     double psi_error();

@@ -13,7 +13,11 @@ GPU: solves with few energy groups need not wait for the replays of
 23-group solves, and one lane's latency-bound CMFD phase runs beside
 another lane's sweeps. Latency is
 measured from a request's arrival time to the moment its result is read on
-the host, so queueing is included.
+the host, so queueing is included. Each latency is split into its phases: the
+host loop's delay in submitting the request after it arrived, the wait in the
+engine's queue for a slot (admission), the solve's outer iterations on the
+GPU up to the replay that retired it, and the delay until the host read the
+result.
 """
 from __future__ import annotations
 
@@ -32,12 +36,16 @@ class Request:
     lane: object = 0         # key of the engine that runs it
 
 
+PHASES = ("host", "queue", "run", "collect")
+
+
 @dataclass
 class ServeReport:
     n: int
     wall_s: float
     latencies_s: list = field(default_factory=list)
     results: list = field(default_factory=list)
+    phases_s: list = field(default_factory=list)  # per request: {phase: seconds} (PHASES)
 
     @property
     def solves_per_s(self) -> float:
@@ -66,7 +74,10 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
     outstanding = {k: {} for k in engines}  # lane -> {solve id: request index}
     lat = [0.0] * len(requests)
     res = [None] * len(requests)
+    phases = [None] * len(requests)
     done = 0
+    # engine clock -> this loop's clock
+    off = {k: (time.perf_counter() - t0) - eng.stats()["now"] for k, eng in engines.items()}
 
     def admit_arrivals():
         nonlocal nxt
@@ -86,8 +97,12 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
                 continue
             r = eng.take(sid, max_pins)
             i = outstanding[k].pop(sid)
-            lat[i] = time.perf_counter() - t0 - requests[i].arrival
+            now = time.perf_counter() - t0
+            lat[i] = now - requests[i].arrival
             res[i] = r
+            phases[i] = {"host": r["t_submit"] + off[k] - requests[i].arrival,
+                         "queue": r["t_admit"] - r["t_submit"], "run": r["t_done"] - r["t_admit"],
+                         "collect": now - (r["t_done"] + off[k])}
             done += 1
 
     while done < len(requests):
@@ -119,7 +134,7 @@ def serve(engines, requests: list[Request], max_pins: int = 1 << 12) -> ServeRep
             if wait > 0:
                 time.sleep(min(wait, 1e-3))
     wall = time.perf_counter() - t0
-    return ServeReport(n=len(requests), wall_s=wall, latencies_s=lat, results=res)
+    return ServeReport(n=len(requests), wall_s=wall, latencies_s=lat, results=res, phases_s=phases)
 
 
 def run_batch(engines, jobs, max_pins: int = 1 << 12) -> list:

@@ -91,6 +91,7 @@ def load():
             ("orc_get_pin_flux_1g", I, [V, I, DP]), ("orc_set_pin_flux_1g", I, [V, I, DP, DP]),
             ("orc_pin_powers", I, [V, DP]), ("orc_get_coarse_currents", I, [V, DP, DP]),
             ("orc_get_boundary", I, [V, I, DP, C.POINTER(C.c_int64)]),
+            ("orc_update_incoming", I, [V, DP, DP, I, I]),
             ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
             ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_table_exp", D, [D]),
@@ -264,6 +265,13 @@ class OracleSolver:
         sfl = np.empty((self.n_group, self.n_surf))
         _chk(self._lib.orc_get_coarse_currents(self._h, _dp(cur), _dp(sfl)))
         return cur, sfl
+
+    def update_incoming_flux(self, part, part_old=None, mode=1):
+        """update_incoming_flux from given 2 (J+ + J-) per [G][n_surf]."""
+        part = np.ascontiguousarray(part, dtype=np.float64)
+        old = None if part_old is None else np.ascontiguousarray(part_old, dtype=np.float64)
+        _chk(self._lib.orc_update_incoming(self._h, _dp(part), None if old is None else _dp(old),
+                                           0 if old is None else 1, mode))
 
     def boundary_flux(self, g):
         """Incoming boundary angular flux of group g (MOCC's per-group layout)."""

@@ -1049,6 +1049,23 @@ int orc_get_boundary(orc_solver *s, int g, double *out, int64_t *n)
         if (out) std::copy(s->bc_in.begin() + (size_t)g * s->bcpg, s->bc_in.begin() + (size_t)(g + 1) * s->bcpg, out);
     });
 }
+int orc_update_incoming(orc_solver *s, const double *part, const double *part_old, int has_old, int mode)
+{
+    return guard([&] {
+        if (mode != 1 && mode != 2) throw std::runtime_error("bad mode");
+        for (int g = 0; g < s->G; g++)
+            for (int is = 0; is < s->nsurf; is++) {
+                // a pair whose 2 (J+ + J-) is the given sum exactly
+                s->partial[(size_t)is * s->G + g] = {0.5 * part[(size_t)g * s->nsurf + is], 0.0};
+                if (has_old) s->partial_old[(size_t)is * s->G + g] = {0.5 * part_old[(size_t)g * s->nsurf + is], 0.0};
+            }
+        s->has_old_partial = has_old != 0;
+        const int keep = s->o.incoming_update;
+        s->o.incoming_update = mode;
+        s->update_incoming_flux();
+        s->o.incoming_update = keep;
+    });
+}
 int orc_homogenized_nu_fission(orc_solver *s, double *out)
 {
     return guard([&] {

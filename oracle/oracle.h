@@ -102,6 +102,9 @@ int orc_get_coarse_currents(orc_solver *s, double *cur, double *sflux);
 /* incoming boundary flux of group g (bc_per_group entries; the count alone
  * when out is NULL) */
 int orc_get_boundary(orc_solver *s, int g, double *out, int64_t *n);
+/* update_incoming_flux from given 2 (J+ + J-) sums, [G][n_surf] (part_old
+ * read when has_old), mode 1 (MOCC's lookup) or 2 (entry surface) */
+int orc_update_incoming(orc_solver *s, const double *part, const double *part_old, int has_old, int mode);
 /* XSMeshHomogenized::update (xs_mesh_homogenized.cpp:176-363) of the current
  * flux; writes the pins' nu-Sigma_f, [n_pin, in FSR order][G] */
 int orc_homogenized_nu_fission(orc_solver *s, double *out);

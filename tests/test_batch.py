@@ -238,3 +238,20 @@ def test_requests_given_as_input_text_share_one_trace():
         assert r["error"] == 0
         assert abs(r["k"] - q["k"]) < 5e-7 * q["k"]
         assert np.allclose(r["pin_powers"], q["pin_powers"], rtol=1e-5)
+
+
+def test_every_sweep_ring_shape_gives_the_same_results():
+    # the streaming shape only changes how segment rows reach shared memory
+    cases = _cases(6, seed=21, sizes=(1, 3, 7), precision="mixed")
+    probs = [m.Problem(x, s) for x, s in cases]
+    ref = _run(m.BatchEngine(precision=1, capacity=8), probs)
+    for sh in range(1, len(m.sweep_shapes())):
+        E = m.BatchEngine(precision=1, capacity=8)
+        E.set_sweep_shape(sh)
+        for a, b in zip(_run(E, probs), ref):
+            assert a["error"] == 0 and a["converged"] == 1
+            assert abs(a["k"] - b["k"]) < 5e-7 * b["k"], sh
+            assert max_pin_err(a["pin_powers"], b["pin_powers"]) < 1e-5, sh
+    with pytest.raises(m.MocgpuError) as e:
+        m.BatchEngine(precision=0, capacity=2).set_sweep_shape(1)
+    assert e.value.code == 1

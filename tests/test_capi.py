@@ -83,3 +83,10 @@ def test_batch_engine_requires_a_gpu():
     with pytest.raises(m.MocgpuError) as e:
         m.BatchEngine(precision=1, capacity=4)
     assert e.value.code == 20
+
+
+def test_sweep_ring_shapes_are_listed():
+    shapes = m.sweep_shapes()
+    assert len(shapes) == 5 and shapes[0] == (8, 2)
+    assert len(set(shapes)) == len(shapes)
+    assert all(r % 4 == 0 and s >= 2 for r, s in shapes)

@@ -147,3 +147,25 @@ def test_batch_engine_refuses_the_update():
     with pytest.raises(m.MocgpuError) as e:
         E.submit_xml(_with(xml, "surface"), xsl)
     assert e.value.code == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 2])
+def test_update_from_given_partial_currents_matches_oracle(mode):
+    # the entry point a MOCC build with its own CPU CMFD would call: the
+    # partial-current sums come from the caller
+    xml, xsl = CASES["core_vacuum"]()
+    P = m.Problem(xml, xsl)
+    S, O = m.MoCSweeper(P, 0), oracle.OracleSolver.from_xml(xml, xsl)
+    G, ns = P.sizes["ngroup"], P.sizes["nsurf"]
+    rng = np.random.default_rng(7)
+    part, old = rng.uniform(0.5, 2.0, size=(G, ns)), rng.uniform(0.5, 2.0, size=(G, ns))
+    old[:, ::7] = 0.0  # surfaces without a previous value keep their entries
+    for X in (S, O):
+        X.initialize()
+        X.update_incoming_flux(part, None, mode)   # first solve: set from the sums
+        X.update_incoming_flux(part, old, mode)    # later ones: rescaled by the change
+    for g in range(G):
+        a, b = S.boundary_flux(g), O.boundary_flux(g)
+        assert np.array_equal(a == 0.0, b == 0.0)
+        assert np.allclose(a, b, rtol=1e-15, atol=0.0)

@@ -15,7 +15,8 @@ class FakeEngine:
     iterations; up to `depth` iterations may be launched before the oldest
     is finished, and each completes after `poll_delay` polls (a blocking
     finish() waits for it). As on the device, a solve that ended in one
-    iteration is skipped by the ones launched after it."""
+    iteration is skipped by the ones launched after it. Its clock starts at
+    t0; results carry their submit, admission and retirement times on it."""
 
     def __init__(self, outers=3, poll_delay=2, t0=None, replay_ms=1.0, depth=2):
         self.outers, self.poll_delay, self.replay_ms, self.depth = outers, poll_delay, replay_ms, depth
@@ -23,13 +24,18 @@ class FakeEngine:
         self.next_id, self.active, self.done, self.taken = 0, {}, {}, set()
         self.submits, self.flights, self.replays, self.closed = [], [], 0, False
         self.max_in_flight = 0
+        self.times = {}
 
     def submit(self, problem, xsl=None):
         i = self.next_id
         self.next_id += 1
         self.active[i] = [problem, xsl, 0]
         self.submits.append((problem, time.perf_counter() - self.t0))
+        self.times[i] = [self.now(), None, None]
         return i
+
+    def now(self):
+        return time.perf_counter() - self.t0
 
     def in_flight(self):
         return len(self.flights)
@@ -39,6 +45,9 @@ class FakeEngine:
         if not self.active:
             return 0
         self.flights.append({"solves": list(self.active), "polls": 0})
+        for i in self.active:
+            if self.times[i][1] is None:
+                self.times[i][1] = self.now()
         self.max_in_flight = max(self.max_in_flight, len(self.flights))
         return len(self.active)
 
@@ -60,6 +69,7 @@ class FakeEngine:
             if self.active[i][2] >= self.outers:
                 p, x, _ = self.active.pop(i)
                 self.done[i] = (p, x)
+                self.times[i][2] = self.now()
         return len(self.active)
 
     def step(self):
@@ -78,10 +88,12 @@ class FakeEngine:
             return None
         self.taken.add(i)
         p, x = self.done[i]
-        return {"id": i, "error": 0, "problem": p, "xsl": x, "converged": 1}
+        ts, ta, td = self.times[i]
+        return {"id": i, "error": 0, "problem": p, "xsl": x, "converged": 1, "t_submit": ts, "t_admit": ta,
+                "t_done": td}
 
     def stats(self):
-        return {"replay_ms": self.replays * self.replay_ms}
+        return {"replay_ms": self.replays * self.replay_ms, "now": self.now()}
 
     def close(self):
         self.closed = True
@@ -104,6 +116,10 @@ def test_requests_wait_for_arrival_and_results_match_requests():
         for prob, t in eng.submits:
             assert t >= arrival[prob] - 1e-6
     assert sorted(len(e.submits) for e in lanes.values()) == [14, 26]
+    # each latency splits into host delay, queue, run and collection
+    for lat, ph in zip(rep.latencies_s, rep.phases_s):
+        assert all(v >= -1e-6 for v in ph.values()), ph
+        assert abs(sum(ph.values()) - lat) < 1e-6
 
 
 def test_busy_lane_does_not_block_the_other():
