@@ -36,19 +36,68 @@ __device__ __forceinline__ void warp_sum2(double &a, double &b)
     b = odd ? keep : other;
 }
 
+// Shared doubles a CTA of nw warps needs for gathered block sums: every
+// lane's two partials and the two totals.
+__host__ __device__ constexpr int gather_scratch(int nw) { return 64 * nw + 8; }
+
 struct Blk {
     int nw; // warps in the CTA
     double *scratch;
     int buf = 0;
+    // Gathered sums (scratch of gather_scratch(nw) doubles): every lane
+    // stores its partial, one warp adds them up and publishes the total, at
+    // two barriers per sum instead of one. The FP64 pipe of an SM takes 16
+    // cycles per warp instruction, and a shuffle tree in every warp spends
+    // nw times the FP64 instructions of one warp summing the lanes' column
+    // sums: with four warps that was about 40 % of a BiCGSTAB iteration's
+    // FP64 work.
+    bool gather = false;
     __device__ void sync() const
     {
         if (nw == 1) __syncwarp();
         else __syncthreads();
     }
+    __device__ void gathered2(double &a, double &b)
+    {
+        double *pa = scratch, *pb = scratch + 32 * nw, *res = scratch + 64 * nw;
+        pa[threadIdx.x] = a;
+        pb[threadIdx.x] = b;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double x = pa[threadIdx.x], y = pb[threadIdx.x];
+            for (int w = 1; w < nw; w++) {
+                x += pa[threadIdx.x + 32 * w];
+                y += pb[threadIdx.x + 32 * w];
+            }
+            warp_sum2(x, y);
+            if (threadIdx.x == 0) {
+                res[0] = x;
+                res[1] = y;
+            }
+        }
+        __syncthreads();
+        a = res[0];
+        b = res[1];
+    }
+    __device__ double gathered(double a)
+    {
+        double *pa = scratch, *res = scratch + 64 * nw;
+        pa[threadIdx.x] = a;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double x = pa[threadIdx.x];
+            for (int w = 1; w < nw; w++) x += pa[threadIdx.x + 32 * w];
+            x = warp_sum(x);
+            if (threadIdx.x == 0) res[0] = x;
+        }
+        __syncthreads();
+        return res[0];
+    }
     // Two block sums with a single barrier (double-buffered scratch); the
     // per-warp partials are combined pairwise so the adds form a tree.
     __device__ void sum2(double &a, double &b)
     {
+        if (gather && nw > 1) return gathered2(a, b);
         warp_sum2(a, b);
         if (nw == 1) return;
         int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -65,6 +114,7 @@ struct Blk {
     // One block sum (five FP64 adds per lane in the warp stage).
     __device__ double sum(double a)
     {
+        if (gather && nw > 1) return gathered(a);
         a = warp_sum(a);
         if (nw == 1) return a;
         int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -338,13 +388,15 @@ __device__ void cmfd_body(CmfdView c, int vec_in_smem)
     extern __shared__ __align__(16) double sm[];
     Blk B;
     B.nw = blockDim.x >> 5;
-    B.scratch = sm; // 128 doubles
+    B.scratch = sm; // gather_scratch(nw) doubles
+    B.gather = true;
+    const int sc = gather_scratch(B.nw);
     const int n = c.n_cell, G = c.G, ns = c.n_surf;
     // work vectors: b, x (group flux copy), 8 BiCGSTAB vectors
-    double *vec = vec_in_smem ? sm + 128 : c.vec;
+    double *vec = vec_in_smem ? sm + sc : c.vec;
     // mode 2: the current group's operator is also staged in shared memory;
     // mode 3: every group's operator, staged once after it is built
-    double *ms = (vec_in_smem >= 2) ? sm + 128 + 10 * n : nullptr;
+    double *ms = (vec_in_smem >= 2) ? sm + sc + 10 * n : nullptr;
     double *b = vec, *x = vec + n, *w = vec + 2 * n;
     double k = *c.k;
     if (c.fixup)
@@ -937,11 +989,23 @@ void note_launch_external();
 // Warps per CMFD CTA. One warp reaches only about a quarter of an SM's FP64
 // rate (one of four schedulers issues), so meshes with work for more than
 // one warp get at least four; tiny meshes stay on one warp, where every
-// reduction is a shuffle tree.
+// reduction is a shuffle tree. With gathered sums a CTA of about two rows
+// per lane does best on the 289-cell assembly (measured per solve: 4 warps
+// 180 ms, 5 warps 167 ms, 10 warps 215 ms).
+#ifndef MOCGPU_CMFD_CELLS_PER_WARP
+#define MOCGPU_CMFD_CELLS_PER_WARP 64
+#endif
 static int cmfd_warps(int n_cell)
 {
     if (n_cell <= 64) return 1;
-    int nw = (n_cell + 255) / 256;
+    int nw = (n_cell + MOCGPU_CMFD_CELLS_PER_WARP - 1) / MOCGPU_CMFD_CELLS_PER_WARP;
+    return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
+}
+// Warps per CTA of the cluster solve (its sums stay shuffle trees, whose cost
+// grows with the warps): one per 256 cells of the CTA's slice, at least four.
+static int cluster_warps(int slice)
+{
+    int nw = (slice + 255) / 256;
     return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
 
@@ -955,7 +1019,7 @@ static int cmfd_warps(int n_cell)
 // operator, 1 = work vectors only, 0 = nothing (vectors in global memory).
 static int cmfd_smem_mode(int n_cell, size_t *bytes, int all_groups = 0)
 {
-    const size_t base = 128 * sizeof(double), lim = 200 * 1024;
+    const size_t base = gather_scratch(cmfd_warps(n_cell)) * sizeof(double), lim = 200 * 1024;
     const size_t vec = (size_t)10 * n_cell * sizeof(double), op = (size_t)6 * n_cell * sizeof(double);
     if (all_groups > 0 && base + vec + op * all_groups <= lim) {
         *bytes = base + vec + op * all_groups;
@@ -1014,7 +1078,7 @@ static ClusterShape cluster_shape(const CmfdView &c, int max_cl)
     ClusterShape sh;
     sh.cl = std::max(2, std::min(max_cl, (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
     const int slice = (c.n_cell + sh.cl - 1) / sh.cl;
-    sh.nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cmfd_warps(slice);
+    sh.nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cluster_warps(slice);
     const size_t lim = 200 * 1024, all = (size_t)(192 + 8 * slice + 6 * c.G * slice) * sizeof(double);
     sh.all_groups = all <= lim ? 1 : 0;
     sh.smem = sh.all_groups ? all : (size_t)(192 + 14 * slice) * sizeof(double);
@@ -1122,7 +1186,7 @@ void launch_cmfd_solve_static(const CmfdView &c, cudaStream_t s)
     v.vec = static_scratch_address();
     const int nw = cmfd_warps(c.n_cell);
     note_launch_external();
-    k_cmfd_solve_static<<<1, 32 * nw, 128 * sizeof(double), s>>>(v);
+    k_cmfd_solve_static<<<1, 32 * nw, gather_scratch(nw) * sizeof(double), s>>>(v);
 }
 
 } // namespace mocgpu

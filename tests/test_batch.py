@@ -241,7 +241,10 @@ def test_requests_given_as_input_text_share_one_trace():
 
 
 def test_every_sweep_ring_shape_gives_the_same_results():
-    # the streaming shape only changes how segment rows reach shared memory
+    # the streaming shape only changes how segment rows reach shared memory,
+    # and with it the order of the FP32 tally's float reductions: the solves
+    # may stop one outer iteration apart, so k agrees to a few k_tol (1e-6)
+    # and pin powers to the fission-source tolerance
     cases = _cases(6, seed=21, sizes=(1, 3, 7), precision="mixed")
     probs = [m.Problem(x, s) for x, s in cases]
     ref = _run(m.BatchEngine(precision=1, capacity=8), probs)
@@ -250,8 +253,8 @@ def test_every_sweep_ring_shape_gives_the_same_results():
         E.set_sweep_shape(sh)
         for a, b in zip(_run(E, probs), ref):
             assert a["error"] == 0 and a["converged"] == 1
-            assert abs(a["k"] - b["k"]) < 5e-7 * b["k"], sh
-            assert max_pin_err(a["pin_powers"], b["pin_powers"]) < 1e-5, sh
+            assert abs(a["k"] - b["k"]) < 3e-6, sh
+            assert max_pin_err(a["pin_powers"], b["pin_powers"]) < 1e-4, sh
     with pytest.raises(m.MocgpuError) as e:
         m.BatchEngine(precision=0, capacity=2).set_sweep_shape(1)
     assert e.value.code == 1

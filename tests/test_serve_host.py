@@ -7,7 +7,7 @@ the least device time per solve."""
 import time
 
 from mocc_gb300.serve import Request, poisson_arrivals, run_batch, serve
-from mocc_gb300.tune import tune_bundles_per_unit
+from mocc_gb300.tune import tune_bundles_per_unit, tune_sweep
 
 
 class FakeEngine:
@@ -153,3 +153,27 @@ def test_autotuner_keeps_the_fastest_shape():
     assert out["best"] == 2
     assert set(out["ms_per_solve"]) == {1, 2, 4}
     assert all(e.closed for e in made.values())
+
+
+def test_grid_autotuner_searches_both_dimensions():
+    # replay time per iteration as a function of (bundles per unit, ring shape)
+    cost = {(b, s): 2.0 + abs(b - 2) + 0.5 * abs(s - 3) for b in (1, 2, 4) for s in range(5)}
+    made = []
+
+    class Shaped(FakeEngine):
+        def __init__(self, bpu):
+            super().__init__(outers=2)
+            self.bpu = bpu
+
+        def set_sweep_shape(self, s):
+            self.replay_ms = cost[(self.bpu, s)]
+
+    def make(bpu):
+        made.append(Shaped(bpu))
+        return made[-1]
+
+    out = tune_sweep(make, [(("s", i), None) for i in range(3)])
+    assert out["points"] == 15 and len(made) == 15 and all(e.closed for e in made)
+    assert out["best"]["bundles_per_unit"] == 2 and out["best"]["shape"] == 3
+    import mocc_gb300 as m
+    assert (out["best"]["rows"], out["best"]["stages"]) == m.sweep_shapes()[3]
