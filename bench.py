@@ -9,7 +9,7 @@ angles, 0.05 cm spacing, CMFD on the pin mesh, k_tol 1e-6, psi_tol 1e-5,
 n_inner 5, reflective boundaries. FP32 sweep, FP64 k/fission source/CMFD.
 One step = all 256 solves from flat-flux start to convergence through the
 batch engine (continuous batching, one captured CUDA graph per outer
-iteration, work-unit shape chosen by the autotuner).
+iteration, work-unit and segment-ring shapes chosen by the autotuner).
 
 Printed JSON (one line, rank 0):
   value          solves/s: solves / device time of the graph replays (CUDA
@@ -22,7 +22,8 @@ Printed JSON (one line, rank 0):
   serving        a Poisson request stream at 50-2000 requests/s (lattice
                  sizes weighted 0.4/0.3/0.2/0.1, 7 or 23 groups, given as
                  MOCC input text): solves/s, p50/p99 latency overall and per
-                 class, host setup time per request
+                 class with each request's phases (host, queue, run,
+                 collect), host setup time per request
   accuracy       k error (pcm) and max fuel-pin power error of every one of
                  the 256 batched solves against the FP64 CPU oracle (which
                  traces each input itself); served results likewise, one per
@@ -38,9 +39,9 @@ L2 is flushed (256 MB write) before every timed step; within a step the four
 shared traced geometries (~35 MB of segment streams) stay in the 129 MB L2 by
 design, while the per-solve state (~0.2 GB for 256 solves) does not fit.
 
---workload assembly17 / minicore: one solve of that single lattice per step
-(the 17x17 assembly at 0.03 cm, or the 68x68-pin mini-core with vacuum
-reflector faces), mixed precision timed, with the plain FP64 path's time and
+--workload pin3x3 / assembly17 / minicore: one solve of that single lattice
+per step (the 3x3 pin lattice, the 17x17 assembly at 0.03 cm, or the
+68x68-pin mini-core with vacuum reflector faces), mixed precision timed, with the plain FP64 path's time and
 its k / pin-power difference, the sweep kernel's roofline, and a full FP64
 solve of the oracle with the accuracy of both paths.
 
@@ -79,7 +80,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="branch256", choices=["branch256", "assembly17", "minicore"])
+    ap.add_argument("--workload", default="branch256", choices=["branch256", "pin3x3", "assembly17", "minicore"])
     ap.add_argument("--cases", type=int, default=N_CASES)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle legs")
     ap.add_argument("--no-serve", action="store_true", help="skip the served request stream")
@@ -602,6 +603,7 @@ def run_branch(args, rank, world):
 
 
 SINGLE = {
+    "pin3x3": "pin3x3: 3x3 pins (24 FSRs each), 8 azimuths/octant, 3 polar, 0.05 cm",
     "assembly17": "assembly17: 17x17 assembly, 16 azimuths/octant, 3 polar, 0.03 cm",
     "minicore": "minicore: 3x3 assemblies of 17x17 pins (3 fuel compositions) + a 21.42 cm reflector row on "
                 "two sides (68x68 pins), vacuum on the reflector sides, 16 azimuths/octant, 3 polar, 0.03 cm",
