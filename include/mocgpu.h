@@ -72,6 +72,8 @@ typedef struct mocgpu_options {
     int n_inner, gs_boundary, precision;
     int sweep_kernel; /* 0: one thread per track, 1: bundled work units (default) */
     int bundles_per_unit; /* bundled sweep: bundles of 32 tracks per work unit, 1..4; 0 chosen from the size */
+    int window_rows;      /* bundled sweep: rows of a unit staged at a time (multiple of 16); 0 whole units; -1
+                           * automatic (windows where they shrink a unit's shared memory well) */
     /* boundary angular flux update after each CMFD solve, MoCSweeper::
      * update_incoming_flux (src/sweepers/moc/moc_sweeper.cpp:255-291):
      * 0 off (default; MOCC's EigenSolver::do_cmfd has the call commented out,
@@ -220,15 +222,20 @@ int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
 int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
 
 /* ---- layout inspection (no MOCC counterpart) ---------------------------
- * Builds the bundled work-unit layout of the GPU sweep on the host and
- * reports: [0] units, [1] bundles, [2] rows, [3] real segment entries,
- * [4] FSR slots of the largest unit (its FSRs + 1 padding slot),
- * [5] phases; stats_d: [0] sum of real segment lengths, [1] padding
- * fraction. */
-int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int64_t *stats,
-                        double *stats_d);
+ * Builds the bundled work-unit layout of the GPU sweep on the host (rows
+ * staged window_rows at a time, a multiple of 16; 0: whole units), checks
+ * that every segment maps back to its FSR and length, and reports:
+ * [0] units, [1] bundles, [2] rows, [3] real segment entries, [4] FSR slots
+ * of the largest window table (its FSRs + 1 padding slot), [5] phases,
+ * [6] most windows of one unit, [7] windows; stats_d: [0] sum of real
+ * segment lengths, [1] padding fraction. */
+int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int window_rows,
+                        int64_t *stats, double *stats_d);
 
 /* ---- measurement helpers (no MOCC counterpart) ------------------------- */
+/* The bundled sweep layout of the handle's geometry: work units, tracks per
+ * unit, rows per staged window (0: whole units) and FSR slots per table. */
+int mocgpu_sweeper_layout(mocgpu_sweeper *s, int *units, int *tracks_per_unit, int *window_rows, int *table_slots);
 /* The CUDA stream (cudaStream_t) every launch of this handle is ordered on. */
 int mocgpu_sweeper_stream(mocgpu_sweeper *s, void **stream);
 /* Runs reps single-inner sweeps of a group and returns the summed device

@@ -44,7 +44,7 @@ class _Options(C.Structure):
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
                 ("precision", C.c_int), ("sweep_kernel", C.c_int), ("bundles_per_unit", C.c_int),
-                ("incoming_update", C.c_int)]
+                ("window_rows", C.c_int), ("incoming_update", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -120,6 +120,7 @@ def load_library(build: bool = True):
         "mocgpu_get_pin_flux_1g": (I, [P, I, DP]),
         "mocgpu_get_boundary_flux": (I, [P, I, DP, C.c_int64, C.POINTER(C.c_int64)]),
         "mocgpu_update_incoming_flux": (I, [P, DP, DP, I, I]),
+        "mocgpu_sweeper_layout": (I, [P, IP, IP, IP, IP]),
         "mocgpu_set_pin_flux_1g": (I, [P, I, DP, DP]),
         "mocgpu_pin_powers": (I, [P, DP]),
         "mocgpu_get_coarse_currents": (I, [P, DP, DP]),
@@ -130,7 +131,7 @@ def load_library(build: bool = True):
         "mocgpu_sweeper_stream": (I, [P, C.POINTER(C.c_void_p)]),
         "mocgpu_time_sweep": (I, [P, I, I, DP, IP]),
         "mocgpu_launch_count": (I, [I64P]),
-        "mocgpu_layout_stats": (I, [P, I, I, I, I64P, DP]),
+        "mocgpu_layout_stats": (I, [P, I, I, I, I, I64P, DP]),
         "mocgpu_batch_create": (I, [I, I, D, I, C.POINTER(P)]),
         "mocgpu_batch_destroy": (None, [P]),
         "mocgpu_batch_submit": (I, [P, P, CP, I64P]),
@@ -229,12 +230,14 @@ class Problem:
         _check(self._lib.mocgpu_problem_export(self._h, field.encode(), out.ctypes.data_as(C.c_void_p), n.value))
         return out
 
-    def layout_stats(self, gs: bool = True, tracks_per_unit: int = 64, max_local: int = 16384) -> dict:
+    def layout_stats(self, gs: bool = True, tracks_per_unit: int = 64, max_local: int = 16384,
+                     window_rows: int = 0) -> dict:
         """Host-side build of the GPU sweep's bundled layout, with checks."""
-        st = (C.c_int64 * 6)()
+        st = (C.c_int64 * 8)()
         sd = (C.c_double * 2)()
-        _check(self._lib.mocgpu_layout_stats(self._h, 1 if gs else 0, tracks_per_unit, max_local, st, sd))
-        keys = ["units", "bundles", "rows", "real_segments", "max_local", "phases"]
+        _check(self._lib.mocgpu_layout_stats(self._h, 1 if gs else 0, tracks_per_unit, max_local, window_rows, st,
+                                             sd))
+        keys = ["units", "bundles", "rows", "real_segments", "max_local", "phases", "max_windows", "windows"]
         d = dict(zip(keys, list(st)))
         d["len_sum"], d["padding"] = sd[0], sd[1]
         return d
@@ -362,6 +365,12 @@ class MoCSweeper:
         old = None if part_old is None else np.ascontiguousarray(part_old, dtype=np.float64)
         _check(self._lib.mocgpu_update_incoming_flux(self._h, _dp(part), None if old is None else _dp(old),
                                                      0 if old is None else 1, mode))
+
+    def layout(self) -> dict:
+        """Bundled sweep layout of this handle's geometry."""
+        v = [C.c_int() for _ in range(4)]
+        _check(self._lib.mocgpu_sweeper_layout(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(("units", "tracks_per_unit", "window_rows", "table_slots"), (x.value for x in v)))
 
     def boundary_flux(self, g: int) -> np.ndarray:
         """Incoming boundary angular flux of group g (MOCC's per-group layout)."""

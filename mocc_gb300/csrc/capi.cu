@@ -127,6 +127,7 @@ void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
     c->precision = o.precision;
     c->sweep_kernel = o.sweep_kernel;
     c->bundles_per_unit = o.bundles_per_unit;
+    c->window_rows = o.window_rows;
     c->incoming_update = o.incoming_update;
 }
 void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
@@ -151,6 +152,9 @@ void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
     o.sweep_kernel = c->sweep_kernel;
     REQUIRE(c->bundles_per_unit >= 0 && c->bundles_per_unit <= 4, "bundles_per_unit must be 0..4");
     o.bundles_per_unit = c->bundles_per_unit;
+    REQUIRE(c->window_rows >= -1 && (c->window_rows <= 0 || c->window_rows % 16 == 0),
+            "window_rows must be -1, 0 or a positive multiple of 16");
+    o.window_rows = c->window_rows;
     REQUIRE(c->incoming_update >= 0 && c->incoming_update <= 2, "incoming_update must be 0, 1 or 2");
     o.incoming_update = c->incoming_update;
 }
@@ -528,12 +532,13 @@ int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep
     });
 }
 
-int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int64_t *stats,
-                        double *stats_d)
+int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, int max_local, int window_rows,
+                        int64_t *stats, double *stats_d)
 {
     return guarded([&] {
         REQUIRE(p && stats && stats_d, "null argument");
-        mocgpu::SweepLayout L = mocgpu::build_sweep_layout(p->P->flat, gs != 0, tracks_per_unit, max_local);
+        mocgpu::SweepLayout L =
+            mocgpu::build_sweep_layout(p->P->flat, gs != 0, tracks_per_unit, max_local, true, window_rows);
         int64_t real = 0;
         double sum = 0.0;
         std::vector<int> unit_of(L.bundle_row.size(), -1);
@@ -548,15 +553,19 @@ int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, in
                 int n = t < 0 ? 0 : (int)(f.trk_seg_begin[t + 1] - f.trk_seg_begin[t]);
                 for (int r = 0; r < L.bundle_nrows[b]; r++) {
                     size_t i = (size_t)(L.bundle_row[b] + r) * 32 + lane;
+                    // the row's window
+                    const int wr = L.wu[wu].n_win > 1 ? L.window_rows : (1 << 30);
+                    const int w = r / wr;
+                    if (w >= L.wu[wu].n_win) throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "row outside its unit's windows");
+                    const mocgpu::RowWindowHost &W = L.win[L.wu[wu].win_begin + w];
                     if (r < n) {
                         real++;
                         sum += L.len[i];
-                        // the unit-local index must map back to the segment's FSR
-                        if (L.lfsr[i] >= L.wu[wu].n_local ||
-                            L.local_fsr[L.wu[wu].fsr_begin + L.lfsr[i]] != f.seg_fsr[f.trk_seg_begin[t] + r] ||
+                        // the window-local index must map back to the segment's FSR
+                        if (L.lfsr[i] >= W.n_local || L.local_fsr[W.fsr_begin + L.lfsr[i]] != f.seg_fsr[f.trk_seg_begin[t] + r] ||
                             L.len[i] != f.seg_len[f.trk_seg_begin[t] + r])
                             throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "layout maps a segment to the wrong FSR or length");
-                    } else if (L.len[i] != 0.0 || L.lfsr[i] != L.wu[wu].n_local) {
+                    } else if (L.len[i] != 0.0 || L.lfsr[i] != W.n_local) {
                         throw mocgpu::Error(MOCGPU_ERR_INTERNAL, "padding entry not zero-length or not on the padding slot");
                     }
                 }
@@ -568,11 +577,24 @@ int mocgpu_layout_stats(const mocgpu_problem *p, int gs, int tracks_per_unit, in
         stats[3] = real;
         stats[4] = L.max_local;
         stats[5] = L.n_phases;
+        stats[6] = L.max_windows;
+        stats[7] = (int64_t)L.win.size();
         stats_d[0] = sum;
         stats_d[1] = L.padding;
     });
 }
 
+int mocgpu_sweeper_layout(mocgpu_sweeper *s, int *units, int *tracks_per_unit, int *window_rows, int *table_slots)
+{
+    return guarded([&] {
+        REQUIRE(units && tracks_per_unit && window_rows && table_slots, "null argument");
+        const auto &G = *sw(s).geometry();
+        *units = G.layout_units;
+        *tracks_per_unit = G.layout_tracks_per_unit;
+        *window_rows = G.layout_window_rows;
+        *table_slots = G.layout_max_local;
+    });
+}
 int mocgpu_sweeper_stream(mocgpu_sweeper *s, void **stream)
 {
     return guarded([&] {

@@ -229,7 +229,7 @@ bool BatchEngine::try_admit(Pending &p)
         if (in_use_ + need_geo + need_state > budget_) return false;
     }
     if (!geo) {
-        geo = std::make_shared<const DeviceGeometry>(f, precision_, bpu_);
+        geo = std::make_shared<const DeviceGeometry>(f, precision_, bpu_, 0); // whole units: the batched kernel
         GeoEntry e;
         e.P = p.P;
         e.geo = geo;

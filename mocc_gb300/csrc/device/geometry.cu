@@ -8,6 +8,19 @@ namespace mocgpu {
 namespace {
 constexpr double kPiD = 3.1415926535897932;
 
+// Row windows of the bundled sweep: rows per window, and the FSRs of a whole
+// unit above which the unit is staged a window at a time (build-time knobs).
+// Measured on the 68x68 mini-core (one group sweep, 2 bundles per unit):
+// whole units 618 us (3 CTAs per SM), windows of 128 rows 589 us (5 CTAs),
+// 64 rows 635 us and 32 rows 674 us: the restaging and the per-window tally
+// flushes grow as the windows shrink and eat the occupancy they buy.
+#ifndef MOCGPU_WINDOW_ROWS
+#define MOCGPU_WINDOW_ROWS 128
+#endif
+#ifndef MOCGPU_WINDOW_MIN_FSRS
+#define MOCGPU_WINDOW_MIN_FSRS 1024
+#endif
+
 int reflect_angle(int iang, int normal, int ndir_oct)
 {
     static const int table[3][8] = {{1, 0, 3, 2, 5, 4, 7, 6}, {3, 2, 1, 0, 7, 6, 5, 4}, {4, 5, 6, 7, 0, 1, 2, 3}};
@@ -22,7 +35,7 @@ Surface upwind(double ox, double oy, int normal)
 }
 } // namespace
 
-DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_unit) : precision(prec)
+DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_unit, int window_rows) : precision(prec)
 {
     for (int s : {EAST, NORTH, WEST, SOUTH})
         if (f.bc[s] != (int)BoundaryType::VACUUM && f.bc[s] != (int)BoundaryType::REFLECT)
@@ -213,11 +226,29 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         if (bundles_per_unit > 0) tpu = 32 * std::min(bundles_per_unit, 4);
         int max_local = (precision == 0) ? 4096 : 8192;
         SweepLayout L = build_sweep_layout(f, true, tpu, max_local, true);
+        // Units whose FSRs would take more than a few KB of shared memory
+        // are staged a window of rows at a time (two tables: the forward
+        // warps' window and the backward warps'), so that more CTAs fit on
+        // an SM; kept where the two tables come to well under the one.
+        if (window_rows > 0) {
+            L = build_sweep_layout(f, true, tpu, max_local, true, window_rows);
+        } else if (window_rows < 0 && MOCGPU_WINDOW_ROWS > 0 && L.max_local > MOCGPU_WINDOW_MIN_FSRS) {
+            SweepLayout Lw = build_sweep_layout(f, true, tpu, max_local, true, MOCGPU_WINDOW_ROWS);
+            if (10 * 2 * Lw.max_local <= 6 * L.max_local) L = std::move(Lw);
+        }
         std::vector<WorkUnitDev> wud(L.wu.size());
+        for (const WorkUnitHost &w : L.wu)
+            if (w.n_bundles > tpu / 32) // the kernel gives each bundle direction one warp of the CTA
+                MOCGPU_THROW(99, "a work unit has more bundles than its CTA has warp pairs");
         for (size_t i = 0; i < L.wu.size(); i++)
-            wud[i] = WorkUnitDev{L.wu[i].set, L.wu[i].bundle_begin, L.wu[i].n_bundles, L.wu[i].fsr_begin,
-                                 L.wu[i].n_local};
+            wud[i] = WorkUnitDev{L.wu[i].set, L.wu[i].bundle_begin, L.wu[i].n_bundles, L.wu[i].win_begin,
+                                 L.wu[i].n_win};
         wu_.upload(wud);
+        {
+            std::vector<int2> wi(L.win.size());
+            for (size_t i = 0; i < L.win.size(); i++) wi[i] = make_int2(L.win[i].fsr_begin, L.win[i].n_local);
+            win_.upload(wi);
+        }
         bundle_row_.upload(L.bundle_row);
         bundle_nrows_.upload(L.bundle_nrows);
         bundle_track_.upload(L.bundle_track);
@@ -246,14 +277,18 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         fv.len = precision == 0 ? (const void *)blen_d_.p : (const void *)blen_f_.p;
         fv.lfsr = blfsr_.p;
         fv.local_fsr = local_fsr_.p;
+        fv.win = win_.p;
+        fv.window_rows = L.window_rows;
+        fv.table_slots = L.max_local;
         fv.bundles_per_unit = tpu / 32;
-        fv.max_local = L.max_local;
+        fv.max_local = L.max_local * (L.max_windows > 1 ? 2 : 1);
         fv.max_hits = L.max_hits;
         if (precision != 0 && L.max_hits > kMaxTallyHits)
             MOCGPU_THROW(6, "a work unit adds more often to one FSR tally than the fixed-point tally allows");
         layout_padding = L.padding;
         layout_units = (int)L.wu.size();
         layout_max_local = L.max_local;
+        layout_window_rows = L.max_windows > 1 ? L.window_rows : 0;
         layout_tracks_per_unit = tpu;
     }
 
@@ -360,7 +395,8 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
              ev_fw_pt_.bytes() * 2 + ev_bw_pt_.bytes() * 2 + ev_fw_begin_.bytes() * 2 + wu_.bytes() +
              ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() + psi_init_dev_.bytes() +
              bundle_row_.bytes() + bundle_nrows_.bytes() + bundle_track_.bytes() + local_fsr_.bytes() +
-             blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes() + trk_entry_.bytes();
+             blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes() + trk_entry_.bytes() +
+             win_.bytes();
     MOCGPU_CUDA(cudaDeviceSynchronize());
 }
 

@@ -18,7 +18,11 @@ class DeviceGeometry {
   public:
     // bundles_per_unit: bundles of 32 tracks per work unit (CTA); 0 picks it
     // from the number of tracks so that one phase fills the GPU.
-    DeviceGeometry(const FlatProblem &f, int precision, int bundles_per_unit = 0);
+    // window_rows: rows of a unit staged at a time by the single-solve kernel
+    // (a multiple of 16); 0 whole units (the batched kernel takes only
+    // those); -1 automatic: windows of MOCGPU_WINDOW_ROWS rows where they
+    // shrink a unit's shared memory well.
+    DeviceGeometry(const FlatProblem &f, int precision, int bundles_per_unit = 0, int window_rows = -1);
     DeviceGeometry(const DeviceGeometry &) = delete;
     DeviceGeometry &operator=(const DeviceGeometry &) = delete;
 
@@ -33,7 +37,7 @@ class DeviceGeometry {
     std::vector<double> psi_init;
     FastView fv{};
     double layout_padding = 0.0;
-    int layout_units = 0, layout_max_local = 0, layout_tracks_per_unit = 0;
+    int layout_units = 0, layout_max_local = 0, layout_tracks_per_unit = 0, layout_window_rows = 0;
     std::vector<int> set_nx, set_ny;
 
     // view with geometry pointers filled and cross-section pointers null
@@ -65,6 +69,7 @@ class DeviceGeometry {
     DevBuf<WorkUnitDev> wu_;
     DevBuf<int64_t> bundle_row_;
     DevBuf<int> bundle_nrows_, bundle_track_, local_fsr_;
+    DevBuf<int2> win_;
     DevBuf<float> blen_f_;
     DevBuf<double> blen_d_;
     DevBuf<uint16_t> blfsr_;

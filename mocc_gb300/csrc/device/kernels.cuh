@@ -93,7 +93,7 @@ struct CmfdView {
 
 // Bundled work-unit layout of the fast sweep (see host/layout.hpp).
 struct WorkUnitDev {
-    int set, bundle_begin, n_bundles, fsr_begin, n_local;
+    int set, bundle_begin, n_bundles, win_begin, n_win; // row windows [win_begin, win_begin + n_win)
 };
 struct FastView {
     const WorkUnitDev *wu;
@@ -101,10 +101,13 @@ struct FastView {
     const int *bundle_nrows, *bundle_track;
     const int2 *bundle_bc; // [bundle][32]: both boundary indices of each lane's track (0 for padding lanes)
     const void *len; // Real [rows][32]
-    const uint16_t *lfsr;
-    const int *local_fsr;
+    const uint16_t *lfsr;      // window-local FSR id of every row entry
+    const int *local_fsr;      // window tables: window-local -> plane FSR ids
+    const int2 *win;           // per row window: (first entry in local_fsr, FSRs)
+    int window_rows;           // rows per window of units with several windows
+    int table_slots;           // FSR slots of one window table (the largest + its padding slot)
     int bundles_per_unit; // warps per CTA = 2 * bundles_per_unit (forward and backward on separate warps)
-    int max_local;
+    int max_local;             // FSR slots a CTA stages: one table, or two when a unit has several windows
     int max_hits; // most tally adds on one unit FSR in one group sweep (bounds the fixed-point tally)
 };
 

@@ -224,8 +224,8 @@ template <typename Real, int NPOL> struct UnitCtx {
 
 // CUR: 0 no coarse tallies; 1 currents and surface fluxes; 2 currents only
 // (the batched eigen path: MOCC's surface fluxes only feed the partial-current
-// store of CMFD::store_currents, cmfd.cpp:555-666, whose consumer
-// update_incoming_flux is disabled at eigen_solver.cpp:289).
+// store of CMFD::store_currents, cmfd.cpp:555-666, which the batched engine
+// does not run).
 //
 // One warp sweeps bundle b in one direction (FWD: rows ascending). Per
 // segment and polar angle the FP32 path computes psi' = qbar + (psi - qbar)
@@ -234,39 +234,41 @@ template <typename Real, int NPOL> struct UnitCtx {
 // MOCC's psi -= (psi - qbar)(1 - E) and tally += w (psi - qbar)(1 - E)
 // (moc_sweeper_kernel.inc.hpp:100-140) summed over the polar angles. The
 // FP64 path follows MOCC's form with its table exponential.
-template <typename Real, int NPOL, bool GS, int CUR, bool FWD, class SH>
-__device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv, const UnitCtx<Real, NPOL> &U,
-                                           int b, int lane)
-{
+//
+// The walk is resumable: the unit stages the FSRs of one window of rows at a
+// time, and between windows the warp keeps its angular flux, its place in
+// the segment ring and its crossing-event cursor in registers. Chunks are
+// aligned to absolute rows (chunk k holds rows [k CH, (k + 1) CH)), in both
+// directions, so no chunk straddles two windows.
+// One state serves both directions (a warp walks one): the direction is a
+// template argument of the methods, so the state takes registers once.
+template <typename Real, int NPOL, bool GS, int CUR, class SH> struct Walker {
     using R2 = typename Pair<Real>::T;
-    constexpr int CH = SH::rows;
-    constexpr int ST = SH::stages;
-    constexpr bool FIXED = Chunk<Real>::fixed;
-    const int t = fv.bundle_track[(size_t)b * 32 + lane];
-    const int2 bc = fv.bundle_bc[(size_t)b * 32 + lane];
-    const int nrows = fv.bundle_nrows[b];
-    const int64_t row0 = fv.bundle_row[b];
-    const int nch = (nrows + CH - 1) / CH;
-    constexpr int dir = FWD ? 0 : 1;
-    const int bc_in = FWD ? bc.x : bc.y, bc_out = FWD ? bc.y : bc.x;
-    const Real *lenp = (const Real *)fv.len;
+    static constexpr int CH = SH::rows;
+    static constexpr int ST = SH::stages;
+    static constexpr bool FIXED = Chunk<Real>::fixed;
+    int t, nrows, nch, c, bc_out;
+    int64_t row0;
+    Real psi[NPOL];
+    Real S; // FP32: sum_p w_p psi_p with the current window's scaled weights
+    int ev, ev_end;
+    int2 ev0, ev1;
 
-    // chunk c of this direction covers rows [lo, hi)
-    auto chunk_rows = [&](int c, int &lo, int &hi) {
-        if (FWD) {
-            lo = c * CH;
-            hi = min(nrows, lo + CH);
-        } else {
-            hi = nrows - c * CH;
-            lo = max(0, hi - CH);
-        }
-    };
-    auto issue = [&](int c) {
+    // chunk cc (in sweep order) covers rows [lo, hi)
+    template <bool FWD> __device__ __forceinline__ void chunk_rows(int cc, int &lo, int &hi) const
+    {
+        const int k = FWD ? cc : nch - 1 - cc;
+        lo = k * CH;
+        hi = min(nrows, lo + CH);
+    }
+    template <bool FWD>
+    __device__ __forceinline__ void issue(const FastView &fv, const UnitCtx<Real, NPOL> &U, int cc, int lane) const
+    {
         int lo, hi;
-        chunk_rows(c, lo, hi);
+        chunk_rows<FWD>(cc, lo, hi);
         const int nr = hi - lo;
-        const int buf = c % ST;
-        const char *gl = (const char *)(lenp + (row0 + lo) * 32);
+        const int buf = cc % ST;
+        const char *gl = (const char *)((const Real *)fv.len + (row0 + lo) * 32);
         char *sl = (char *)(U.ring_len + (size_t)buf * CH * 32);
         const int nl = nr * 32 * (int)sizeof(Real) / 16;
         for (int i = lane; i < nl; i += 32) cp_async16(sl + 16 * i, gl + 16 * i);
@@ -275,40 +277,56 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
         const int nf = nr * 32 * (int)sizeof(uint16_t) / 16;
         for (int i = lane; i < nf; i += 32) cp_async16(sf + 16 * i, gf + 16 * i);
         cp_async_commit();
-    };
-    // ST-1 chunks ahead: one commit group per chunk (empty groups past the
-    // end keep the count uniform), so waiting until at most ST-1 groups are
-    // pending means chunk c has landed
-    for (int c = 0; c < ST - 1; c++) {
-        if (c < nch) issue(c);
-        else cp_async_commit();
     }
 
-    Real psi[NPOL];
+    template <bool FWD>
+    __device__ void begin(const GeomView &g, const FastView &fv, const UnitCtx<Real, NPOL> &U, int b, int lane)
+    {
+        constexpr int dir = FWD ? 0 : 1;
+        t = fv.bundle_track[(size_t)b * 32 + lane];
+        const int2 bc = fv.bundle_bc[(size_t)b * 32 + lane];
+        nrows = fv.bundle_nrows[b];
+        row0 = fv.bundle_row[b];
+        nch = (nrows + CH - 1) / CH;
+        c = 0;
+        const int bc_in = FWD ? bc.x : bc.y;
+        bc_out = FWD ? bc.y : bc.x;
+        // ST-1 chunks ahead: one commit group per chunk (empty groups past the
+        // end keep the count uniform), so waiting until at most ST-1 groups are
+        // pending means the chunk about to be swept has landed
+        for (int cc = 0; cc < ST - 1; cc++) {
+            if (cc < nch) issue<FWD>(fv, U, cc, lane);
+            else cp_async_commit();
+        }
 #pragma unroll
-    for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? U.psi_in[U.s_off[dir][p] + bc_in] : (Real)0;
-    Real S = 0; // FP32: sum_p w_p psi_p
-    if constexpr (FIXED) {
+        for (int p = 0; p < NPOL; p++) psi[p] = (t >= 0) ? U.psi_in[U.s_off[dir][p] + bc_in] : (Real)0;
+        S = 0;
+        if constexpr (FIXED) {
 #pragma unroll
-        for (int p = 0; p < NPOL; p++) S = fmaf(U.wt[p], psi[p], S); // the same chain as in row()
+            for (int p = 0; p < NPOL; p++) S = fmaf(U.wt[p], psi[p], S); // the same chain as in update()
+        }
+        ev = ev_end = 0;
+        const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
+        if (CUR && t >= 0) {
+            ev = FWD ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
+            ev_end = FWD ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
+        }
+        const int2 none = make_int2(INT_MAX, 0);
+        ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
+        ev1 = (CUR && ev + 1 < ev_end) ? evp[ev + 1] : none;
     }
-    int ev = 0, ev_end = 0;
-    const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
-    if (CUR && t >= 0) {
-        ev = FWD ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
-        ev_end = FWD ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
-    }
-    // the next two crossing events (row, code) live in registers, so a row
-    // without an event costs one compare and the load of the event after
-    // next has rows of time to arrive
-    const int2 none = make_int2(INT_MAX, 0);
-    int2 ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
-    int2 ev1 = (CUR && ev + 1 < ev_end) ? evp[ev + 1] : none;
-    auto events = [&](int k) {
+
+    // the crossing events at row boundary k (the next two live in registers,
+    // so a row without an event costs one compare and the load of the event
+    // after next has rows of time to arrive)
+    template <bool FWD> __device__ __forceinline__ void events(const GeomView &g, const UnitCtx<Real, NPOL> &U, int k)
+    {
+        const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
+        const int2 none = make_int2(INT_MAX, 0);
         while (ev0.x == k) {
-            int c = ev0.y;
-            int surf = c >> 1;
-            bool ynorm = c & 1;
+            int cd = ev0.y;
+            int surf = cd >> 1;
+            bool ynorm = cd & 1;
             if constexpr (FIXED) {
                 // MOCC's current weight of a crossing (moc_current_worker.hpp:
                 // 176-181) is the tally weight w_p with the sign of the
@@ -338,99 +356,116 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
             ev0 = ev1;
             ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
         }
-    };
-    // Per row: the factors E (FP32: E = 2^(-tau log2(e) / sin), the
-    // transmitted fraction; FP64: 1 - e^-tau from MOCC's table) of a segment
-    // in unit FSR l with Sigma_t sq.x and length L. They do not depend on psi,
-    // so a group of rows computes them all before the serial psi updates and
-    // tally adds (shared-memory atomics, which later loads cannot pass).
-    auto factors = [&](Real L, const R2 &sq, Real (&E)[NPOL]) {
-        const Real tau0 = sq.x * L;
-#pragma unroll
-        for (int p = 0; p < NPOL; p++) {
-            if constexpr (FIXED) {
-                float e;
-                asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"((float)(tau0 * U.rsin[p])));
-                E[p] = e;
-            } else {
-                E[p] = atten(tau0, U.rsin[p], g.exp_tab);
-            }
-        }
-    };
-    auto update = [&](const R2 &sq, const Real (&E)[NPOL], int l) {
-        if constexpr (FIXED) {
-            Real S1 = 0;
-#pragma unroll
-            for (int p = 0; p < NPOL; p++) {
-#if MOCGPU_PSI_FMA2
-                psi[p] = fmaf(psi[p], E[p], fmaf(-sq.y, E[p], sq.y));
-#else
-                psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
-#endif
-                S1 = fmaf(U.wt[p], psi[p], S1);
-            }
-            tally_fixed(U.s_hi, U.s_lo, U.tally, U.lf, U.inv_scale, l, S - S1);
-            S = S1;
-        } else {
-            Real acc = 0;
-#pragma unroll
-            for (int p = 0; p < NPOL; p++) {
-                Real d = (psi[p] - sq.y) * E[p];
-                psi[p] -= d;
-                acc += d * U.wt[p];
-            }
-            tally_add(U.s_tal, l, acc);
-        }
-    };
-
-    for (int c = 0; c < nch; c++) {
-        if (c + ST - 1 < nch) issue(c + ST - 1);
-        else cp_async_commit();
-        cp_async_wait<ST - 1>();
-        __syncwarp();
-        int lo, hi;
-        chunk_rows(c, lo, hi);
-        const int nr = hi - lo;
-        // rows of this chunk in sweep order: FWD from the first, else from the last
-        const Real *cl = U.ring_len + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
-        const uint16_t *cf = U.ring_fsr + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
-        constexpr int step = FWD ? 32 : -32;
-        // Four rows per step: the loads and gathers of the four rows issue
-        // back to back; only the psi recurrence that follows is serial.
-        constexpr int UR = SH::unroll;
-        int k = 0;
-        for (; k + UR <= nr; k += UR) {
-            Real L[UR];
-            int l[UR];
-            R2 sq[UR];
-            Real E[UR][NPOL];
-#pragma unroll
-            for (int v = 0; v < UR; v++) {
-                L[v] = cl[(k + v) * step];
-                l[v] = cf[(k + v) * step];
-            }
-#pragma unroll
-            for (int v = 0; v < UR; v++) sq[v] = U.s_sq[l[v]];
-#pragma unroll
-            for (int v = 0; v < UR; v++) factors(L[v], sq[v], E[v]);
-#pragma unroll
-            for (int v = 0; v < UR; v++) {
-                if (CUR && t >= 0) events(FWD ? lo + k + v : hi - (k + v));
-                update(sq[v], E[v], l[v]);
-            }
-        }
-        for (; k < nr; k++) {
-            if (CUR && t >= 0) events(FWD ? lo + k : hi - k);
-            const int l = cf[k * step];
-            const R2 sq = U.s_sq[l];
-            Real E[NPOL];
-            factors(cl[k * step], sq, E);
-            update(sq, E, l);
-        }
-        __syncwarp();
     }
-    if (t >= 0) {
-        if (CUR) events(FWD ? nrows : 0);
+
+    // Sweeps this direction's chunks whose rows lie in [row_lo, row_hi).
+    template <bool FWD>
+    __device__ void run(const GeomView &g, const UnitCtx<Real, NPOL> &U, const FastView &fv, int row_lo, int row_hi,
+                        int lane)
+    {
+        // Per row: the factors E (FP32: E = 2^(-tau log2(e) / sin), the
+        // transmitted fraction; FP64: 1 - e^-tau from MOCC's table) of a
+        // segment in table slot l with Sigma_t sq.x and length L. They do not
+        // depend on psi, so a group of rows computes them all before the
+        // serial psi updates and tally adds (shared-memory atomics, which
+        // later loads cannot pass).
+        auto factors = [&](Real L, const R2 &sq, Real (&E)[NPOL]) {
+            const Real tau0 = sq.x * L;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                if constexpr (FIXED) {
+                    float e;
+                    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"((float)(tau0 * U.rsin[p])));
+                    E[p] = e;
+                } else {
+                    E[p] = atten(tau0, U.rsin[p], g.exp_tab);
+                }
+            }
+        };
+        auto update = [&](const R2 &sq, const Real (&E)[NPOL], int l) {
+            if constexpr (FIXED) {
+                Real S1 = 0;
+#pragma unroll
+                for (int p = 0; p < NPOL; p++) {
+#if MOCGPU_PSI_FMA2
+                    psi[p] = fmaf(psi[p], E[p], fmaf(-sq.y, E[p], sq.y));
+#else
+                    psi[p] = fmaf(psi[p] - sq.y, E[p], sq.y);
+#endif
+                    S1 = fmaf(U.wt[p], psi[p], S1);
+                }
+                tally_fixed(U.s_hi, U.s_lo, U.tally, U.lf, U.inv_scale, l, S - S1);
+                S = S1;
+            } else {
+                Real acc = 0;
+#pragma unroll
+                for (int p = 0; p < NPOL; p++) {
+                    Real d = (psi[p] - sq.y) * E[p];
+                    psi[p] -= d;
+                    acc += d * U.wt[p];
+                }
+                tally_add(U.s_tal, l, acc);
+            }
+        };
+
+        while (c < nch) {
+            int lo, hi;
+            chunk_rows<FWD>(c, lo, hi);
+            if (FWD ? lo >= row_hi : lo < row_lo) break; // the chunk belongs to a later window
+            if (c + ST - 1 < nch) issue<FWD>(fv, U, c + ST - 1, lane);
+            else cp_async_commit();
+            cp_async_wait<ST - 1>();
+            __syncwarp();
+            const int nr = hi - lo;
+            // rows of this chunk in sweep order: FWD from the first, else from the last
+            const Real *cl = U.ring_len + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
+            const uint16_t *cf = U.ring_fsr + (size_t)(c % ST) * CH * 32 + (FWD ? 0 : (nr - 1) * 32) + lane;
+            constexpr int step = FWD ? 32 : -32;
+            // UR rows per step: the loads and gathers of the rows issue back
+            // to back; only the psi recurrence that follows is serial.
+            constexpr int UR = SH::unroll;
+            int k = 0;
+            for (; k + UR <= nr; k += UR) {
+                Real L[UR];
+                int l[UR];
+                R2 sq[UR];
+                Real E[UR][NPOL];
+#pragma unroll
+                for (int v = 0; v < UR; v++) {
+                    L[v] = cl[(k + v) * step];
+                    l[v] = cf[(k + v) * step];
+                }
+#pragma unroll
+                for (int v = 0; v < UR; v++) sq[v] = U.s_sq[l[v]];
+#pragma unroll
+                for (int v = 0; v < UR; v++) factors(L[v], sq[v], E[v]);
+#pragma unroll
+                for (int v = 0; v < UR; v++) {
+                    if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k + v : hi - (k + v));
+                    update(sq[v], E[v], l[v]);
+                }
+            }
+            for (; k < nr; k++) {
+                if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k : hi - k);
+                const int l = cf[k * step];
+                const R2 sq = U.s_sq[l];
+                Real E[NPOL];
+                factors(cl[k * step], sq, E);
+                update(sq, E, l);
+            }
+            __syncwarp();
+            c++;
+        }
+    }
+
+    // After the last row: the crossing at the track's end and the outgoing
+    // angular flux (Gauss-Seidel: straight into the reflected angle's
+    // incoming entry).
+    template <bool FWD> __device__ void finish(const GeomView &g, const UnitCtx<Real, NPOL> &U)
+    {
+        constexpr int dir = FWD ? 0 : 1;
+        if (t < 0) return;
+        if (CUR) events<FWD>(g, U, FWD ? nrows : 0);
 #pragma unroll
         for (int p = 0; p < NPOL; p++) {
             if (GS) {
@@ -442,9 +477,30 @@ __device__ __forceinline__ void sweep_task(const GeomView &g, const FastView &fv
             }
         }
     }
-}
+};
 
-template <typename Real, int NPOL, bool GS, int CUR, class SH>
+// One FSR table in shared memory: the (Sigma_t, qbar) pairs of a window's
+// FSRs and their tally (FP32: fixed-point high and low words; FP64: the
+// tally copies), slot n_local being the padding slot.
+template <typename Real> struct Table {
+    using R2 = typename Pair<Real>::T;
+    R2 *sq;
+    int *hi;       // FP32
+    unsigned *lo;  // FP32
+    Real *tal;     // FP64: [TC][slots]
+    __device__ void place(unsigned char *base, int slots)
+    {
+        sq = reinterpret_cast<R2 *>(base);
+        hi = reinterpret_cast<int *>(sq + slots);
+        lo = reinterpret_cast<unsigned *>(hi + slots);
+        tal = reinterpret_cast<Real *>(sq + slots);
+    }
+};
+
+// WIN: the layout may have units of several row windows (the single-solve
+// kernel); without it (the batched kernel, whose geometries are laid out in
+// whole units) the window loop folds away and takes no registers.
+template <typename Real, int NPOL, bool GS, int CUR, class SH, bool WIN>
 __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv, const StateView &st, int group,
                                            int wu, unsigned char *smem_raw)
 {
@@ -456,26 +512,30 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     const WorkUnitDev u = fv.wu[wu];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    // [warp rings][(sigma_t, qbar) pairs][tally]
+    const int K = WIN ? u.n_win : 1, slots = fv.table_slots;
+    // [warp rings][table A][table B]: A holds the window the forward warps
+    // sweep, B the one the backward warps sweep (A serves both when they are
+    // the same window)
     unsigned char *ring = smem_raw + (size_t)warp * ring_bytes<Real, SH>();
-    R2 *s_sq = reinterpret_cast<R2 *>(smem_raw + (size_t)nwarps * ring_bytes<Real, SH>());
-    Real *s_tal0 = reinterpret_cast<Real *>(s_sq + fv.max_local); // FP64: [TC][max_local]
-    int *s_hi = reinterpret_cast<int *>(s_sq + fv.max_local);      // FP32: [max_local] high words
-    unsigned *s_lo = reinterpret_cast<unsigned *>(s_hi + fv.max_local); // and [max_local] low words
+    unsigned char *tables = smem_raw + (size_t)nwarps * ring_bytes<Real, SH>();
+    // table pointers are recomputed where they are needed (fewer registers
+    // live across the sweep)
+    auto table = [&](int which) {
+        Table<Real> T;
+        T.place(tables + (size_t)which * slots * fsr_slot_bytes<Real>(), slots);
+        return T;
+    };
 
     UnitCtx<Real, NPOL> U;
     U.ring_len = reinterpret_cast<const Real *>(ring);
     U.ring_fsr = reinterpret_cast<const uint16_t *>(ring + ST * CH * 32 * sizeof(Real));
-    U.s_sq = s_sq;
-    U.s_tal = s_tal0 + (size_t)(lane % TC) * fv.max_local;
-    U.s_hi = s_hi;
-    U.s_lo = s_lo;
     U.psi_in = (Real *)st.psi_in + (size_t)group * g.bc_per_group;
     U.psi_out = (Real *)st.psi_out;
     U.cur = st.cur + (size_t)group * g.n_surf;
     U.sfl = st.sflux + (size_t)group * g.n_surf;
     U.cur32 = st.cur32;
     U.sfl32 = st.sfl32;
+    U.tally = (float *)st.tally;
     U.ny_set = g.set_ny[u.set];
 
     // per unit: boundary-flux offsets of every (direction, polar) angle and
@@ -483,7 +543,7 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     // (stored as -1 - offset where the face is vacuum: the entry is zeroed,
     // as BoundaryCondition::update does, boundary_condition.cpp:155-191)
     __shared__ int s_off[2][kMaxPolar], s_tgt[2][kMaxPolar][2];
-    __shared__ unsigned s_mbits; // largest |qbar| or incoming |psi| of the unit (float bits)
+    __shared__ unsigned s_mbits; // largest |qbar| or incoming |psi| staged so far (float bits)
     U.s_off = s_off;
     U.s_tgt = s_tgt;
     if (threadIdx.x < 2 * NPOL) {
@@ -499,63 +559,6 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
         }
     }
     if (FIXED && threadIdx.x == 0) s_mbits = 0u;
-    __syncthreads();
-
-    const Real *sigt = (const Real *)st.sigt;
-    const Real *qbar = (const Real *)st.qbar;
-    const int *lf = fv.local_fsr + u.fsr_begin;
-    unsigned mbits = 0u; // float bits of a non-negative value order like the integers
-    // staging: four FSRs per thread in flight, so the dependent loads
-    // (local id, then Sigma_t and qbar) overlap
-    for (int i0 = threadIdx.x; i0 < u.n_local; i0 += 4 * blockDim.x) {
-        int gl[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int i = i0 + j * blockDim.x;
-            gl[j] = (i < u.n_local) ? lf[i] : -1;
-        }
-        Real sg[4], qq[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            sg[j] = gl[j] >= 0 ? sigt[gl[j]] : (Real)0;
-            qq[j] = gl[j] >= 0 ? qbar[gl[j]] : (Real)0;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int i = i0 + j * blockDim.x;
-            if (i >= u.n_local) break;
-            s_sq[i] = R2{sg[j], qq[j]};
-            if constexpr (FIXED) {
-                mbits = max(mbits, __float_as_uint(fabsf((float)qq[j])));
-                s_hi[i] = 0;
-                s_lo[i] = 0u;
-            } else {
-#pragma unroll
-                for (int cc = 0; cc < TC; cc++) s_tal0[(size_t)cc * fv.max_local + i] = (Real)0;
-            }
-        }
-    }
-    // padding entries of the unit's rows point at the slot after its FSRs,
-    // which holds Sigma_t = qbar = 0: a padding row leaves psi unchanged
-    // bit for bit and adds nothing
-    if (threadIdx.x == 0) s_sq[u.n_local] = R2{(Real)0, (Real)0};
-    if constexpr (FIXED) {
-        // incoming angular fluxes of every lane, direction and polar angle
-        for (int i = threadIdx.x; i < u.n_bundles * 64; i += blockDim.x) {
-            const size_t bl = (size_t)(u.bundle_begin + (i >> 6)) * 32 + (i & 31);
-            const int dir = (i >> 5) & 1;
-            if (fv.bundle_track[bl] < 0) continue;
-            const int2 bc = fv.bundle_bc[bl];
-            const int bc_in = dir == 0 ? bc.x : bc.y;
-#pragma unroll
-            for (int p = 0; p < NPOL; p++)
-                mbits = max(mbits, __float_as_uint(fabsf((float)U.psi_in[s_off[dir][p] + bc_in])));
-        }
-        mbits = __reduce_max_sync(0xffffffffu, mbits);
-        if (lane == 0 && mbits) atomicMax(&s_mbits, mbits);
-    }
-    __syncthreads();
-
 #pragma unroll
     for (int p = 0; p < NPOL; p++) {
         const SetPolar sp = g.sp[u.set * NPOL + p];
@@ -568,46 +571,152 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
             U.fwt[p][1] = (Real)sp.fw[1];
         }
     }
-    float inv_scale = 1.f;
-    if constexpr (FIXED) {
-        float sum_w = 0.f;
-#pragma unroll
-        for (int p = 0; p < NPOL; p++) sum_w += fabsf((float)U.wt[p]);
-        const unsigned mb = s_mbits;
-        if (mb >= 0x7F800000u && threadIdx.x == 0) atomicOr(st.status, (unsigned)DEV_NAN); // inf or NaN
-        float scale;
-        fixed_scale(__uint_as_float(mb), sum_w, fv.max_hits, scale, inv_scale);
-#pragma unroll
-        for (int p = 0; p < NPOL; p++) U.wt[p] *= scale;
-        U.tally = (float *)st.tally;
-        U.lf = lf;
-        U.inv_scale = inv_scale;
-        if (CUR) {
-            const SetPolar sp0 = g.sp[u.set * NPOL];
-            U.csgn[0] = copysignf(inv_scale, (float)sp0.cw[0]);
-            U.csgn[1] = copysignf(inv_scale, (float)sp0.cw[1]);
-        }
-    }
-
-    const int ntasks = 2 * u.n_bundles;
-    for (int task = warp; task < ntasks; task += nwarps) {
-        const int b = u.bundle_begin + (task >> 1);
-        if ((task & 1) == 0) sweep_task<Real, NPOL, GS, CUR, true, SH>(g, fv, U, b, lane);
-        else sweep_task<Real, NPOL, GS, CUR, false, SH>(g, fv, U, b, lane);
-    }
     __syncthreads();
-    Real *tally = (Real *)st.tally;
-    for (int i = threadIdx.x; i < u.n_local; i += blockDim.x) {
-        Real v;
-        if constexpr (FIXED) {
-            const long long x = (long long)s_hi[i] * (1ll << 20) + (long long)s_lo[i];
-            v = (Real)(__ll2float_rn(x) * inv_scale);
-        } else {
-            v = s_tal0[i];
+
+    const Real *sigt = (const Real *)st.sigt;
+    const Real *qbar = (const Real *)st.qbar;
+    // stages window w into table T: (Sigma_t, qbar) of its FSRs, zero
+    // tallies, the zero padding slot; returns the largest |qbar| (float bits)
+    auto stage = [&](Table<Real> T, int w) -> unsigned {
+        const int2 wi = fv.win[w]; // (first entry in local_fsr, FSRs)
+        const int *lf = fv.local_fsr + wi.x;
+        unsigned mb = 0u; // float bits of a non-negative value order like the integers
+        // four FSRs per thread in flight, so the dependent loads (local id,
+        // then Sigma_t and qbar) overlap
+        for (int i0 = threadIdx.x; i0 < wi.y; i0 += 4 * blockDim.x) {
+            int gl[4];
 #pragma unroll
-            for (int cc = 1; cc < TC; cc++) v += s_tal0[(size_t)cc * fv.max_local + i];
+            for (int j = 0; j < 4; j++) {
+                const int i = i0 + j * blockDim.x;
+                gl[j] = (i < wi.y) ? lf[i] : -1;
+            }
+            Real sg[4], qq[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                sg[j] = gl[j] >= 0 ? sigt[gl[j]] : (Real)0;
+                qq[j] = gl[j] >= 0 ? qbar[gl[j]] : (Real)0;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int i = i0 + j * blockDim.x;
+                if (i >= wi.y) break;
+                T.sq[i] = R2{sg[j], qq[j]};
+                if constexpr (FIXED) {
+                    mb = max(mb, __float_as_uint(fabsf((float)qq[j])));
+                    T.hi[i] = 0;
+                    T.lo[i] = 0u;
+                } else {
+#pragma unroll
+                    for (int cc = 0; cc < TC; cc++) T.tal[(size_t)cc * slots + i] = (Real)0;
+                }
+            }
         }
-        if (v != (Real)0) atomicAdd(tally + lf[i], v);
+        // padding entries point at the slot after the window's FSRs, which
+        // holds Sigma_t = qbar = 0: a padding row leaves psi unchanged bit
+        // for bit and adds nothing
+        if (threadIdx.x == 0) T.sq[wi.y] = R2{(Real)0, (Real)0};
+        return mb;
+    };
+    // adds table T's tally (window w) to the solve's FSR tally
+    auto flush = [&](Table<Real> T, int w, float inv) {
+        const int2 wi = fv.win[w];
+        const int *lf = fv.local_fsr + wi.x;
+        Real *tally = (Real *)st.tally;
+        for (int i = threadIdx.x; i < wi.y; i += blockDim.x) {
+            Real v;
+            if constexpr (FIXED) {
+                const long long x = (long long)T.hi[i] * (1ll << 20) + (long long)T.lo[i];
+                v = (Real)(__ll2float_rn(x) * inv);
+            } else {
+                v = T.tal[i];
+#pragma unroll
+                for (int cc = 1; cc < TC; cc++) v += T.tal[(size_t)cc * slots + i];
+            }
+            if (v != (Real)0) atomicAdd(tally + lf[i], v);
+        }
+    };
+
+    // this warp's task: bundle b, forward (even warps) or backward (odd);
+    // a unit has at most as many bundles as a CTA has warp pairs
+    const bool has_task = warp < 2 * u.n_bundles;
+    const bool fwd = (warp & 1) == 0;
+    const int b = u.bundle_begin + (warp >> 1);
+    Walker<Real, NPOL, GS, CUR, SH> w;
+    float scale = 1.f, inv_scale = 1.f;
+    for (int j = 0; j < K; j++) {
+        const int wa = u.win_begin + j, wbk = u.win_begin + K - 1 - j;
+        const bool same = !WIN || wa == wbk;
+        unsigned mb = stage(table(0), wa);
+        if (!same) mb = max(mb, stage(table(1), wbk));
+        if constexpr (FIXED) {
+            if (j == 0) {
+                // incoming angular fluxes of every lane, direction and polar angle
+                for (int i = threadIdx.x; i < u.n_bundles * 64; i += blockDim.x) {
+                    const size_t bl = (size_t)(u.bundle_begin + (i >> 6)) * 32 + (i & 31);
+                    const int dir = (i >> 5) & 1;
+                    if (fv.bundle_track[bl] < 0) continue;
+                    const int2 bc = fv.bundle_bc[bl];
+                    const int bc_in = dir == 0 ? bc.x : bc.y;
+#pragma unroll
+                    for (int p = 0; p < NPOL; p++)
+                        mb = max(mb, __float_as_uint(fabsf((float)U.psi_in[s_off[dir][p] + bc_in])));
+                }
+            }
+            mb = __reduce_max_sync(0xffffffffu, mb);
+            if (lane == 0 && mb) atomicMax(&s_mbits, mb);
+        }
+        __syncthreads();
+        if constexpr (FIXED) {
+            // Power-of-two scale of this window's fixed-point tally from the
+            // largest qbar or incoming psi staged so far, which bounds psi in
+            // the rows swept up to here; the running sums S change scale
+            // exactly with it.
+            const unsigned mbits = s_mbits;
+            if (mbits >= 0x7F800000u && threadIdx.x == 0) atomicOr(st.status, (unsigned)DEV_NAN); // inf or NaN
+            float sum_w = 0.f, w0[NPOL];
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) {
+                w0[p] = (float)g.sp[u.set * NPOL + p].wt;
+                sum_w += fabsf(w0[p]);
+            }
+            float sc, inv;
+            fixed_scale(__uint_as_float(mbits), sum_w, fv.max_hits, sc, inv);
+            const float ratio = sc * inv_scale;
+            scale = sc;
+            inv_scale = inv;
+#pragma unroll
+            for (int p = 0; p < NPOL; p++) U.wt[p] = w0[p] * scale;
+            U.inv_scale = inv_scale;
+            if (CUR) {
+                const SetPolar sp0 = g.sp[u.set * NPOL];
+                U.csgn[0] = copysignf(inv_scale, (float)sp0.cw[0]);
+                U.csgn[1] = copysignf(inv_scale, (float)sp0.cw[1]);
+            }
+            if (j > 0 && has_task) w.S *= ratio;
+        }
+        if (has_task) {
+            const Table<Real> T = table((fwd || same) ? 0 : 1);
+            const int2 wi = fv.win[fwd ? wa : wbk];
+            U.s_sq = T.sq;
+            U.s_hi = T.hi;
+            U.s_lo = T.lo;
+            U.s_tal = T.tal + (size_t)(lane % TC) * slots;
+            U.lf = fv.local_fsr + wi.x;
+            const int wr = (WIN && K > 1) ? fv.window_rows : INT_MAX / 2;
+            if (fwd) {
+                if (j == 0) w.template begin<true>(g, fv, U, b, lane);
+                w.template run<true>(g, U, fv, j * wr, (j + 1) * wr, lane);
+                if (j == K - 1) w.template finish<true>(g, U);
+            } else {
+                if (j == 0) w.template begin<false>(g, fv, U, b, lane);
+                w.template run<false>(g, U, fv, (K - 1 - j) * wr, (K - j) * wr, lane);
+                if (j == K - 1) w.template finish<false>(g, U);
+            }
+        }
+        __syncthreads();
+        flush(table(0), wa, inv_scale);
+        if (!same) flush(table(1), wbk, inv_scale);
+        if (j + 1 < K) __syncthreads(); // the next window's staging overwrites the tables
     }
 }
 
@@ -617,7 +726,7 @@ template <typename Real, int NPOL, bool GS, int CUR>
 __global__ void k_sweep_fast(GeomView g, FastView fv, StateView st, int group, int wu0)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    sweep_unit<Real, NPOL, GS, CUR, DefaultShape>(g, fv, st, group, wu0 + blockIdx.x, smem_raw);
+    sweep_unit<Real, NPOL, GS, CUR, DefaultShape, true>(g, fv, st, group, wu0 + blockIdx.x, smem_raw);
 }
 
 // Persistent batched sweep: a fixed grid walks the (solve slot, work unit)
@@ -637,7 +746,8 @@ __global__ void MOCGPU_SWEEP_BOUNDS kb_sweep_fast(BatchViews b, const int2 *item
         const int2 item = items[it];
         // solves that ended in an earlier replay are frozen (uniform per CTA)
         if (b.sv[item.x].red[RED_DONE] == 0.0)
-            sweep_unit<Real, NPOL, true, CUR, SH>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y, smem_raw);
+            sweep_unit<Real, NPOL, true, CUR, SH, false>(b.gv[item.x], b.fv[item.x], b.sv[item.x], group, item.y,
+                                                         smem_raw);
         if (threadIdx.x == 0) s_next = (int)gridDim.x + atomicAdd(counter, 1);
         __syncthreads(); // also: the next unit may overwrite this one's shared data
         it = s_next;

@@ -35,7 +35,8 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
         f_.scat = xs->scat;
     }
     const FlatProblem &f = f_;
-    if (!geo_) geo_ = std::make_shared<const DeviceGeometry>(P.flat, precision_, P.opts.bundles_per_unit);
+    if (!geo_)
+        geo_ = std::make_shared<const DeviceGeometry>(P.flat, precision_, P.opts.bundles_per_unit, P.opts.window_rows);
     if (geo_->precision != precision_) MOCGPU_THROW(1, "shared geometry has a different precision");
     if (geo_->n_fsr != f.n_fsr || geo_->n_tracks != f.n_tracks || geo_->G != f.ng)
         MOCGPU_THROW(1, "shared geometry does not match this problem");

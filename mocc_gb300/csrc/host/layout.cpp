@@ -6,10 +6,13 @@
 
 namespace mocgpu {
 
-SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local, bool interleave)
+SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_unit, int max_local, bool interleave,
+                               int window_rows)
 {
     SweepLayout L;
     const int W = SweepLayout::kLanes;
+    if (window_rows < 0 || window_rows % 16 != 0) MOCGPU_THROW(1, "window rows must be a multiple of 16");
+    L.window_rows = window_rows;
     if (tracks_per_unit < W) tracks_per_unit = W;
     tracks_per_unit = (tracks_per_unit / W) * W;
     if (max_local > 65535) max_local = 65535;
@@ -50,17 +53,10 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                     tracks.push_back(t);
                     t++;
                 }
-                std::sort(fsrs.begin(), fsrs.end());
-                std::unordered_map<int, int> loc;
-                loc.reserve(fsrs.size() * 2);
-                for (size_t i = 0; i < fsrs.size(); i++) loc[fsrs[i]] = (int)i;
                 WorkUnitHost u;
                 u.set = s;
                 u.bundle_begin = (int)L.bundle_row.size();
-                u.fsr_begin = (int)L.local_fsr.size();
                 u.n_local = (int)fsrs.size();
-                L.local_fsr.insert(L.local_fsr.end(), fsrs.begin(), fsrs.end());
-                L.max_local = std::max(L.max_local, u.n_local + 1); // + the padding slot
                 // longest first, bundles of W
                 std::stable_sort(tracks.begin(), tracks.end(), [&](int a, int b) {
                     return (f.trk_seg_begin[a + 1] - f.trk_seg_begin[a]) > (f.trk_seg_begin[b + 1] - f.trk_seg_begin[b]);
@@ -69,17 +65,43 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                 // lanes of a bundle have similar lengths (little padding) but
                 // are not spatial neighbours, which cross the same FSR in the
                 // same row and contend for its tally
-                {
-                    std::vector<int> hits(fsrs.size(), 0);
-                    for (int tr : tracks)
-                        for (int64_t k = f.trk_seg_begin[tr]; k < f.trk_seg_begin[tr + 1]; k++)
-                            hits[loc[f.seg_fsr[k]]] += 2; // swept forward and backward
-                    for (int h : hits) L.max_hits = std::max(L.max_hits, h);
-                }
                 const size_t nb = (tracks.size() + W - 1) / W;
                 std::vector<std::vector<int>> groups(nb);
                 for (size_t j = 0; j < tracks.size(); j++)
                     groups[interleave ? j % nb : j / W].push_back(tracks[j]);
+                int maxrows = 0;
+                for (const std::vector<int> &grp : groups)
+                    for (int tr : grp)
+                        maxrows = std::max<int>(maxrows, (int)(f.trk_seg_begin[tr + 1] - f.trk_seg_begin[tr]));
+                // row windows: one table of FSRs per window, local ids per window
+                const int wr = (window_rows > 0 && maxrows > window_rows) ? window_rows : std::max(maxrows, 1);
+                const int nwin = (maxrows + wr - 1) / wr > 0 ? (maxrows + wr - 1) / wr : 1;
+                u.win_begin = (int)L.win.size();
+                u.n_win = nwin;
+                L.max_windows = std::max(L.max_windows, nwin);
+                std::vector<std::unordered_map<int, int>> loc(nwin);
+                for (int w = 0; w < nwin; w++) {
+                    std::vector<int> wf;
+                    std::unordered_map<int, int> count;
+                    for (int tr : tracks) {
+                        const int64_t a = f.trk_seg_begin[tr];
+                        const int n = (int)(f.trk_seg_begin[tr + 1] - a);
+                        for (int r = w * wr; r < std::min(n, (w + 1) * wr); r++) count[f.seg_fsr[a + r]]++;
+                    }
+                    wf.reserve(count.size());
+                    for (const auto &kv : count) {
+                        wf.push_back(kv.first);
+                        // a window's table may take both directions' adds (when
+                        // forward and backward warps stage the same window)
+                        L.max_hits = std::max(L.max_hits, 2 * kv.second);
+                    }
+                    std::sort(wf.begin(), wf.end());
+                    loc[w].reserve(wf.size() * 2);
+                    for (size_t i = 0; i < wf.size(); i++) loc[w][wf[i]] = (int)i;
+                    L.win.push_back(RowWindowHost{(int)L.local_fsr.size(), (int)wf.size()});
+                    L.local_fsr.insert(L.local_fsr.end(), wf.begin(), wf.end());
+                    L.max_local = std::max(L.max_local, (int)wf.size() + 1); // + the padding slot
+                }
                 for (const std::vector<int> &grp : groups) {
                     int nrows = 0;
                     for (int tr : grp) nrows = std::max<int>(nrows, (int)(f.trk_seg_begin[tr + 1] - f.trk_seg_begin[tr]));
@@ -87,7 +109,12 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                     L.bundle_nrows.push_back(nrows);
                     size_t base = L.len.size();
                     L.len.resize(base + (size_t)nrows * W, 0.0);
-                    L.lfsr.resize(base + (size_t)nrows * W, (uint16_t)fsrs.size());
+                    L.lfsr.resize(base + (size_t)nrows * W, 0);
+                    // padding entries keep length 0 and point at their window's
+                    // padding slot (local id n_local, after its FSRs)
+                    for (int r = 0; r < nrows; r++)
+                        for (int lane = 0; lane < W; lane++)
+                            L.lfsr[base + (size_t)r * W + lane] = (uint16_t)L.win[u.win_begin + r / wr].n_local;
                     for (int lane = 0; lane < W; lane++) {
                         if (lane >= (int)grp.size()) {
                             L.bundle_track.push_back(-1);
@@ -99,10 +126,8 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                         int n = (int)(f.trk_seg_begin[tr + 1] - a);
                         for (int r = 0; r < n; r++) {
                             L.len[base + (size_t)r * W + lane] = f.seg_len[a + r];
-                            L.lfsr[base + (size_t)r * W + lane] = (uint16_t)loc[f.seg_fsr[a + r]];
+                            L.lfsr[base + (size_t)r * W + lane] = (uint16_t)loc[r / wr].at(f.seg_fsr[a + r]);
                         }
-                        // padding rows keep length 0 and point at the padding slot
-                        // (local id n_local, after the unit's FSRs)
                         real += n;
                     }
                     padded += (int64_t)nrows * W;

@@ -66,6 +66,11 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
         if (o.bundles_per_unit < 0 || o.bundles_per_unit > 4)
             MOCGPU_THROW(7, "bundles_per_unit must be 0 (automatic) or 1..4.");
     }
+    if (sweeper->has_attr("window_rows")) {
+        o.window_rows = sweeper->attr_int("window_rows", -2);
+        if (o.window_rows < -1 || (o.window_rows > 0 && o.window_rows % 16 != 0))
+            MOCGPU_THROW(7, "window_rows must be -1 (automatic), 0 or a positive multiple of 16.");
+    }
     if (sweeper->has_attr("incoming_update")) {
         std::string u = sanitize(sweeper->attr("incoming_update"));
         if (u == "off") o.incoming_update = 0;

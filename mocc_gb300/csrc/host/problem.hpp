@@ -30,6 +30,7 @@ struct SolverOptions {
     int precision = 0;       // 0: FP64 sweep, 1: FP32 sweep + FP64 reductions/CMFD
     int sweep_kernel = 1;    // 0: one thread per track (plain), 1: bundled work units
     int bundles_per_unit = 0; // bundled sweep work-unit shape (1..4 bundles of 32 tracks), 0: chosen from the size
+    int window_rows = -1;     // bundled sweep: rows staged per window (a multiple of 16), 0 whole units, -1 automatic
     // boundary angular flux update after each CMFD solve
     // (MoCSweeper::update_incoming_flux): 0 off (MOCC's behaviour, its call
     // is disabled), 1 as MOCC's code reads the partial currents, 2 from the

@@ -299,3 +299,28 @@ def test_mixed_wide_flux_range_matches_fp64():
     assert (flux[1] > 0).all()
     assert pcm(res[1]["k"], res[0]["k"]) < PCM_TOL
     assert max_pin_err(pins[1], pins[0]) < PIN_TOL
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_row_windows_match_whole_units(precision):
+    # units staged 16 rows at a time (two tables, the fixed-point scale
+    # renewed per window) against the oracle, on a core with vacuum faces
+    xml, xsl = W.minicore(n_lat=3, n_azi=4, spacing=0.05, precision="double")
+    P, S, O = _pair(xml, xsl, precision, window_rows=16)
+    lay = S.layout()
+    assert lay["window_rows"] == 16
+    ra = m.EigenSolver(P, sweeper=S).solve()
+    rb = O.solve()
+    assert ra["converged"] and rb["converged"]
+    if precision == 0:
+        assert ra["iterations"] == rb["iterations"]
+        assert abs(ra["k"] - rb["k"]) / rb["k"] < 1e-9
+        assert max_pin_err(S.pin_powers(), O.pin_powers()) < 1e-8
+    else:
+        assert pcm(ra["k"], rb["k"]) < PCM_TOL
+        assert max_pin_err(S.pin_powers(), O.pin_powers()) < PIN_TOL
+    # the same solve in whole units
+    P0, S0, _ = _pair(xml, xsl, precision, window_rows=0)
+    assert S0.layout()["window_rows"] == 0
+    r0 = m.EigenSolver(P0, sweeper=S0).solve()
+    assert abs(r0["k"] - ra["k"]) < (1e-12 if precision == 0 else 3e-6)
