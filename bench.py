@@ -192,12 +192,12 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(name="kb_sweep_fast_dram_branch256.md"):
-    """DRAM bytes per sweep launch from the committed ncu summary (None if absent)."""
+def profiled_traffic(name="kb_sweep_fast_dram_branch256.md", key="traffic_bytes_per_launch"):
+    """DRAM bytes of the sweep from a committed ncu summary (None if absent)."""
     p = ROOT / "profiles" / name
     if p.exists():
         for line in p.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     return None
 
@@ -665,7 +665,13 @@ def run_single(args, rank, world):
             "plain_fp64": {"ms_per_solve": ms64[0], "k": r64["k"],
                            "mixed_vs_fp64_pcm": pcm(r["k"], r64["k"]), "mixed_vs_fp64_pin": max_pin_err(pins, pins64)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None, "traffic": None, "kernel": "k_sweep_fast",
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": profiled_traffic("k_sweep_fast_minicore.md", "traffic_bytes_per_group_sweep")
+                         if args.workload == "minicore" else None,
+                         "traffic_note": "DRAM bytes of one group sweep (two launches, the unit of `achieved` "
+                                         "here) from profiles/k_sweep_fast_minicore.md"
+                         if args.workload == "minicore" else "not captured for this workload",
+                         "kernel": "k_sweep_fast",
                          "peak_source": peak_kind,
                          "secondary": secondary_ceilings(achieved, P.sizes["nseg"] / (ms / 20 / 1e3) if nl else None,
                                                          clk)},
