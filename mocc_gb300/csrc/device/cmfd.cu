@@ -616,15 +616,21 @@ struct Team {
     double *xch; // [2][2][16] exchange slots (double-buffered, two values)
     int xb = 0;
     __device__ void sync() const { cl_sync(); }
-    // cluster sums; every CTA adds the same per-CTA totals in rank order
+    // Cluster sums: each CTA's total goes into every CTA's exchange slots,
+    // and after the cluster barrier every warp adds the (at most 16) totals
+    // with one shuffle tree: the same values in the same order in every warp
+    // of every CTA, so all hold bit-identical sums and every loop test
+    // agrees. (A sequential add of the totals in every lane cost each warp
+    // 16 FP64 instructions per sum.)
     __device__ double sum(double a)
     {
         a = B.sum(a);
         double *s = xch + xb * 32;
         if (threadIdx.x < size) st_peer(s + rank, threadIdx.x, a);
         cl_sync();
-        double t = 0.0;
-        for (unsigned r = 0; r < size; r++) t += s[r];
+        const unsigned lane = threadIdx.x & 31;
+        double t = lane < size ? s[lane] : 0.0;
+        t = warp_sum(t);
         xb ^= 1;
         return t;
     }
@@ -637,11 +643,9 @@ struct Team {
             st_peer(s + 16 + rank, threadIdx.x, b);
         }
         cl_sync();
-        double ta = 0.0, tb = 0.0;
-        for (unsigned r = 0; r < size; r++) {
-            ta += s[r];
-            tb += s[16 + r];
-        }
+        const unsigned lane = threadIdx.x & 31;
+        double ta = lane < size ? s[lane] : 0.0, tb = lane < size ? s[16 + lane] : 0.0;
+        warp_sum2(ta, tb);
         a = ta;
         b = tb;
         xb ^= 1;
@@ -775,8 +779,10 @@ __device__ void cmfd_body_cluster(CmfdView c, int all_groups)
     const int n = c.n_cell, G = c.G, ns = c.n_surf;
     Team T;
     T.B.nw = blockDim.x >> 5;
-    T.B.scratch = sm; // 128 doubles
-    T.xch = sm + 128; // 64 doubles
+    T.B.scratch = sm; // gather_scratch(nw) doubles: the CTA's gathered sums
+    T.B.gather = true;
+    const int sc = gather_scratch(T.B.nw);
+    T.xch = sm + sc; // 64 doubles
     T.rank = cl_rank();
     T.size = cl_nrank();
     T.slice = (n + (int)T.size - 1) / (int)T.size;
@@ -785,7 +791,7 @@ __device__ void cmfd_body_cluster(CmfdView c, int all_groups)
     const int s = T.slice, lo = T.lo, hi = T.hi, bd = blockDim.x, tid = threadIdx.x;
     // slice vectors: b, x, 6 BiCGSTAB vectors; the current group's operator rows
     // ms: the current group's rows, or with all_groups every group's rows [G][6][slice]
-    double *b = sm + 192, *x = b + s, *w = x + s, *ms = w + 6 * s;
+    double *b = sm + sc + 64, *x = b + s, *w = x + s, *ms = w + 6 * s;
     double k = *c.k;
     if (c.fixup)
         for (int g = 0; g < G; g++)
@@ -1001,11 +1007,14 @@ static int cmfd_warps(int n_cell)
     int nw = (n_cell + MOCGPU_CMFD_CELLS_PER_WARP - 1) / MOCGPU_CMFD_CELLS_PER_WARP;
     return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
-// Warps per CTA of the cluster solve (its sums stay shuffle trees, whose cost
-// grows with the warps): one per 256 cells of the CTA's slice, at least four.
+// Warps per CTA of the cluster solve: as for one CTA, about two rows per
+// lane (MOCGPU_CMFD_CLUSTER_CELLS_PER_WARP), at least four.
+#ifndef MOCGPU_CMFD_CLUSTER_CELLS_PER_WARP
+#define MOCGPU_CMFD_CLUSTER_CELLS_PER_WARP 64
+#endif
 static int cluster_warps(int slice)
 {
-    int nw = (slice + 255) / 256;
+    int nw = (slice + MOCGPU_CMFD_CLUSTER_CELLS_PER_WARP - 1) / MOCGPU_CMFD_CLUSTER_CELLS_PER_WARP;
     return nw < 4 ? 4 : (nw > 16 ? 16 : nw);
 }
 
@@ -1079,9 +1088,10 @@ static ClusterShape cluster_shape(const CmfdView &c, int max_cl)
     sh.cl = std::max(2, std::min(max_cl, (c.n_cell + MOCGPU_CMFD_CLUSTER_CELLS - 1) / MOCGPU_CMFD_CLUSTER_CELLS));
     const int slice = (c.n_cell + sh.cl - 1) / sh.cl;
     sh.nw = MOCGPU_CMFD_CLUSTER_WARPS > 0 ? MOCGPU_CMFD_CLUSTER_WARPS : cluster_warps(slice);
-    const size_t lim = 200 * 1024, all = (size_t)(192 + 8 * slice + 6 * c.G * slice) * sizeof(double);
+    const size_t head = (size_t)gather_scratch(sh.nw) + 64; // gathered sums + the cluster exchange slots
+    const size_t lim = 200 * 1024, all = (head + 8 * slice + 6 * c.G * slice) * sizeof(double);
     sh.all_groups = all <= lim ? 1 : 0;
-    sh.smem = sh.all_groups ? all : (size_t)(192 + 14 * slice) * sizeof(double);
+    sh.smem = sh.all_groups ? all : (head + 14 * slice) * sizeof(double);
     return sh;
 }
 
