@@ -254,9 +254,19 @@ def run_reference(args, rank, world):
         return
     import oracle
     from mocc_gb300 import workloads as W
-    cases = W.branch_cases(args.cases, seed=7)
-    sample = oracle_sample(cases)
-    solvers = [oracle.OracleSolver.from_xml(xml, xsl) for _, xml, xsl in sample]
+    config = CONFIG
+    what = ("each step: one full FP64 solve of one case of each lattice size (1x1, 3x3, 7x7, 17x17) of the 256, "
+            "each traced by the oracle from its MOCC input text before the timed steps")
+    if args.workload in SINGLE:
+        # one full solve of the single lattice per step, as the GPU arm times
+        xml, xsl = getattr(W, args.workload)(precision="mixed")
+        solvers = [oracle.OracleSolver.from_xml(xml, xsl)]
+        config = {"workload": SINGLE[args.workload], "segments": solvers[0].n_seg,
+                  "l2": "flushed (256 MB write) before each timed solve"}
+        what = "each step: one full FP64 solve, traced by the oracle from the MOCC input text before the timed steps"
+    else:
+        cases = W.branch_cases(args.cases, seed=7)
+        solvers = [oracle.OracleSolver.from_xml(xml, xsl) for _, xml, xsl in oracle_sample(cases)]
 
     def step():
         for O in solvers:
@@ -274,11 +284,9 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": "solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": CONFIG,
+            "config": config,
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": solvers[0].threads, "kind": "port",
-                             "sample": "each step: one full FP64 solve of one case of each lattice size "
-                                       "(1x1, 3x3, 7x7, 17x17) of the 256, each traced by the oracle from its "
-                                       "MOCC input text before the timed steps"},
+                             "sample": what},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
