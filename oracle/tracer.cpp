@@ -23,8 +23,11 @@
  *   core and plane lookup      src/core/pin.cpp, lattice.cpp, assembly.cpp,
  *                              core.cpp, plane.cpp, core_mesh.cpp
  *   mesh trace and surfaces    src/core/mesh.cpp:88-600
- *   ray laydown, trace,
- *   flat volume correction     src/sweepers/moc/ray_data.cpp:67-527,
+ *   ray laydown (core or pin
+ *   modularity, rational or
+ *   trig modularisation),
+ *   trace, volume correction
+ *   (flat, angle, none)        src/sweepers/moc/ray_data.cpp:67-527,
  *                              src/sweepers/moc/ray.cpp:52-175
  *   solver options             src/solvers/eigen_solver.cpp, src/core/cmfd.cpp,
  *                              src/sweepers/moc/moc_sweeper.cpp
@@ -1411,33 +1414,68 @@ std::unique_ptr<orc_traced> trace_problem(const std::string &xml, const std::str
     if (!rn) throw Fail("No input privided for ray spacing.");
     const double spacing = rn->dbl("spacing", -1.0);
     if (spacing <= 0.0) throw Fail("Failed to read valid ray spacing.");
-    if (rn->has("volume_correction") && lower(rn->attr("volume_correction")) != "flat")
-        throw Fail("the oracle restates the flat volume correction only");
-    if (rn->has("modularity") && lower(rn->attr("modularity")) != "core")
-        throw Fail("the oracle restates core modularity only");
-    if (rn->has("modularization") && lower(rn->attr("modularization")) != "rational_fraction")
-        throw Fail("the oracle restates rational-fraction modularisation only");
+    // ray_data.cpp:67-134: volume correction, modularity, modularisation method
+    const std::string corr = rn->has("volume_correction") ? lower(rn->attr("volume_correction")) : "flat";
+    if (corr != "flat" && corr != "angle" && corr != "none")
+        throw Fail("Unrecognized volume correction option in <rays>");
+    bool core_modular = true;
+    if (rn->has("modularity")) {
+        const std::string mo = lower(rn->attr("modularity"));
+        if (mo == "pin") core_modular = false;
+        else if (mo != "core") throw Fail("Unrecognized modularity option.");
+    }
+    bool rational_mod = true;
+    if (rn->has("modularization")) {
+        const std::string mm = lower(rn->attr("modularization"));
+        if (mm == "trig") rational_mod = false;
+        else if (mm != "rational_fraction") throw Fail("Unrecognized modularization method specified.");
+    }
     const Node *aq = sweeper->child("ang_quad");
     if (!aq && doc->child("solver")) aq = doc->child("solver")->child("ang_quad");
     if (!aq) aq = doc->child("ang_quad");
     if (!aq) throw Fail("No angular quadrature (<ang_quad>) found.");
     Quad Q = read_quad(*aq);
 
-    // ray_data.cpp:136-206: modularise every octant-1 angle
+    // ray_data.cpp:136-206: modularise every octant-1 angle, over the core or
+    // (pin modularity) over one pin cell, all of which must be alike
+    double hx_mod = C.hx, hy_mod = C.hy;
+    if (!core_modular) {
+        hx_mod = C.pins.front()->mesh->px;
+        hy_mod = C.pins.front()->mesh->py;
+        for (const Pin *pn : C.pins)
+            if (pn->mesh->px != hx_mod || pn->mesh->py != hy_mod)
+                throw Fail("Core Mesh does not support pin modular ray tracing.");
+    }
     const int nd = Q.ndir;
     std::vector<int> Nx1(nd), Ny1(nd);
     std::vector<double> sp1(nd);
     for (int ia = 0; ia < nd; ia++) {
         Ang a = Q.ang[ia];
-        double m = (a.alpha < PI / 4.0) ? std::tan(a.alpha) : std::tan(PI / 2.0 - a.alpha);
-        auto f = rational(m, 0.002);
-        int Nx = f.first, Ny = f.second;
-        if (Nx == 0) throw Fail("azimuthal angle too shallow for rational modularisation");
-        double al = std::atan((Nx * C.hy) / (Ny * C.hx));
-        int scale = (int)std::ceil((C.hx / Nx * std::fabs(std::sin(al))) / spacing);
-        Nx *= scale;
-        Ny *= scale;
-        if (a.alpha > PI / 4.0) std::swap(Nx, Ny);
+        int Nx = 0, Ny = 0;
+        if (rational_mod) {
+            // RayData::modularize_angle, RATIONAL (ray_data.cpp:495-516)
+            double m = (a.alpha < PI / 4.0) ? std::tan(a.alpha) : std::tan(PI / 2.0 - a.alpha);
+            auto f = rational(m, 0.002);
+            Nx = f.first;
+            Ny = f.second;
+            if (Nx == 0) throw Fail("azimuthal angle too shallow for rational modularisation");
+            double al = std::atan((Nx * hy_mod) / (Ny * hx_mod));
+            int scale = (int)std::ceil((hx_mod / Nx * std::fabs(std::sin(al))) / spacing);
+            Nx *= scale;
+            Ny *= scale;
+            if (a.alpha > PI / 4.0) std::swap(Nx, Ny);
+        } else {
+            // TRIG (ray_data.cpp:517-523): ray counts from the nominal
+            // spacing, rounded up to even
+            Nx = (int)std::ceil(hx_mod / spacing * std::fabs(std::sin(a.alpha)));
+            Ny = (int)std::ceil(hy_mod / spacing * std::fabs(std::cos(a.alpha)));
+            Nx += Nx % 2;
+            Ny += Ny % 2;
+        }
+        if (!core_modular) {
+            Nx *= C.nx;
+            Ny *= C.ny;
+        }
         Ang b = ang_from_at(std::atan(C.hy * Nx / (C.hx * Ny)), a.theta, a.w);
         Q.modify(ia, b);
         Nx1[ia] = Nx;
@@ -1480,17 +1518,38 @@ std::unique_ptr<orc_traced> trace_problem(const std::string &xml, const std::str
             sets[s].push_back(trace_ray(C, p1, p2, k + Ny, exit_bc(p2), literal));
         }
     }
-    // ray_data.cpp:345-387: flat volume correction, per angle
     std::vector<double> area;
     for (const Pin *p : C.pins) area.insert(area.end(), p->mesh->areas.begin(), p->mesh->areas.end());
-    for (int s = 0; s < n_sets; s++) {
+    if (corr == "flat") {
+        // ray_data.cpp:348-411: each angle's lengths scaled so that its
+        // segments' volumes equal every FSR's area (the polar angles of a
+        // set share its tracks and get the same factor)
+        for (int s = 0; s < n_sets; s++) {
+            std::vector<double> vol(C.n_reg, 0.0);
+            for (const Track &t : sets[s])
+                for (size_t k = 0; k < t.len.size(); k++) vol[t.reg[k]] += t.len[k] * ssp[s];
+            std::vector<double> cf(C.n_reg);
+            for (int r = 0; r < C.n_reg; r++) cf[r] = area[r] / vol[r];
+            for (Track &t : sets[s])
+                for (size_t k = 0; k < t.len.size(); k++) t.len[k] = t.len[k] * cf[t.reg[k]];
+        }
+    } else if (corr == "angle") {
+        // ray_data.cpp:414-474: one factor per FSR from the weighted volume
+        // integral over every angle of octants 1 and 2 (weight / 2 each),
+        // applied to every angle's lengths
         std::vector<double> vol(C.n_reg, 0.0);
-        for (const Track &t : sets[s])
-            for (size_t k = 0; k < t.len.size(); k++) vol[t.reg[k]] += t.len[k] * ssp[s];
-        std::vector<double> cf(C.n_reg);
-        for (int r = 0; r < C.n_reg; r++) cf[r] = area[r] / vol[r];
-        for (Track &t : sets[s])
-            for (size_t k = 0; k < t.len.size(); k++) t.len[k] = t.len[k] * cf[t.reg[k]];
+        for (int s = 0; s < n_sets; s++) {
+            const int ia0 = (s / sets_oct) * nd + (s % sets_oct) * pps;
+            for (int p = 0; p < pps; p++) {
+                const double wgt = Q.ang[ia0 + p].w * 0.5;
+                for (const Track &t : sets[s])
+                    for (size_t k = 0; k < t.len.size(); k++) vol[t.reg[k]] += t.len[k] * ssp[s] * wgt;
+            }
+        }
+        for (int r = 0; r < C.n_reg; r++) vol[r] = area[r] / vol[r];
+        for (int s = 0; s < n_sets; s++)
+            for (Track &t : sets[s])
+                for (size_t k = 0; k < t.len.size(); k++) t.len[k] = t.len[k] * vol[t.reg[k]];
     }
 
     // ---- flatten ----

@@ -2,7 +2,10 @@
 (oracle/tracer.cpp, a restatement of MOCC's) against the library's tracer on
 the same input text: every array of the flat problem must agree, integers
 exactly and volumes and angles to rounding (the Gauss polar angles come from
-Newton iterations whose last bits may differ), segment lengths to 1e-10 cm.
+Newton iterations whose last bits may differ), segment lengths to 1e-10 cm;
+also under MOCC's other <rays> options (angle and no volume correction, pin
+modularity, trigonometric modularisation) and the Chebyshev-Gauss
+quadrature.
 
 The library follows MOCC's coarse walk except at pin-cell corners (pin-line
 crossings within 1e-10 cm of a ray end dropped, crossings shorter than
@@ -75,6 +78,48 @@ def test_oracle_tracer_matches_library(name):
     for k, v in P.options.items():
         if k in o and k != "precision":
             assert o[k] == pytest.approx(v), k
+
+
+RAY_OPTIONS = {
+    "angle_correction": ('<rays spacing="0.05"', '<rays spacing="0.05" volume_correction="angle"'),
+    "no_correction": ('<rays spacing="0.05"', '<rays spacing="0.05" volume_correction="none"'),
+    "pin_modular": ('<rays spacing="0.05"', '<rays spacing="0.05" modularity="pin"'),
+    "trig_modularisation": ('<rays spacing="0.05"', '<rays spacing="0.05" modularization="trig"'),
+    "pin_trig": ('<rays spacing="0.05"', '<rays spacing="0.05" modularity="pin" modularization="trig"'),
+    "chebyshev_gauss": ('type="cy"', 'type="cg"'),
+}
+
+
+@pytest.mark.parametrize("option", sorted(RAY_OPTIONS))
+def test_oracle_tracer_matches_library_ray_options(option):
+    # the <rays> and <ang_quad> options of ray_data.cpp:67-134 and
+    # angular_quadrature.cpp on a 3x3 lattice: MOCC's other volume
+    # corrections, pin modularity, trigonometric modularisation and the
+    # Chebyshev-Gauss product quadrature
+    xml, xsl = W.lattice_case(3, 8, 0.05, "double", seed=1000)
+    old, new = RAY_OPTIONS[option]
+    assert old in xml
+    xml = xml.replace(old, new, 1)
+    P = m.Problem(xml, xsl)
+    T = oracle.Traced(xml, xsl)
+    assert T.problem.n_seg == P.sizes["nseg"] and T.problem.n_tracks == P.sizes["ntracks"]
+    for f in FIELDS:
+        a, b = np.asarray(P.export(f)), T.array(f)
+        assert a.shape == b.shape, f
+        if a.dtype.kind == "f":
+            tol = 1e-10 if f == "seg_len" else 1e-13
+            assert np.max(np.abs(a - b) / np.maximum(np.abs(a), 1.0), initial=0.0) < tol, f
+        else:
+            assert np.array_equal(a, b), f
+    if option == "no_correction":
+        # uncorrected lengths: each set's segment volumes differ from the areas
+        v = np.zeros(P.sizes["nfsr"])
+        sb, ln, fs = T.array("trk_seg_begin"), T.array("seg_len"), T.array("seg_fsr")
+        s0 = T.array("set_first_track")
+        sp = T.array("set_spacing")
+        for t in range(s0[0], s0[1]):
+            np.add.at(v, fs[sb[t]:sb[t + 1]], ln[sb[t]:sb[t + 1]] * sp[0])
+        assert not np.allclose(v, T.array("fsr_area"), rtol=1e-9)
 
 
 def _coarse(T, t):
