@@ -324,3 +324,19 @@ def test_row_windows_match_whole_units(precision):
     assert S0.layout()["window_rows"] == 0
     r0 = m.EigenSolver(P0, sweeper=S0).solve()
     assert abs(r0["k"] - ra["k"]) < (1e-12 if precision == 0 else 3e-6)
+
+
+@pytest.mark.parametrize("option", ["angle_correction", "no_correction", "pin_trig", "chebyshev_gauss"])
+def test_eigen_fp64_under_ray_options(option):
+    # MOCC's other <rays> and quadrature options: the oracle traces the same
+    # input itself (its tracer equals the library's, test_oracle_tracer.py)
+    from test_oracle_tracer import RAY_OPTIONS
+    xml, xsl = W.lattice_case(3, 8, 0.05, "double", seed=1000)
+    old, new = RAY_OPTIONS[option]
+    xml = xml.replace(old, new, 1)
+    P, S, O = _pair(xml, xsl, 0)
+    ra, rb = m.EigenSolver(P, sweeper=S).solve(), O.solve()
+    assert ra["converged"] and rb["converged"]
+    assert ra["iterations"] == rb["iterations"]
+    assert abs(ra["k"] - rb["k"]) / rb["k"] < 1e-9
+    assert max_pin_err(S.pin_powers(), O.pin_powers()) < 1e-8
