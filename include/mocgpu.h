@@ -81,7 +81,7 @@ typedef struct mocgpu_options {
      * currents (at the index of the track's starting coarse cell), 2 from the
      * partial currents of the surface each track enters through, vacuum
      * faces left at zero. XML: <sweeper incoming_update="off|mocc|surface">.
-     * Single solves only; the batch engine refuses it. */
+     * Every solve of one batch engine must ask for the same value. */
     int incoming_update;
 } mocgpu_options;
 

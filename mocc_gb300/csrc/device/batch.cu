@@ -103,18 +103,19 @@ void BatchEngine::check_config(const Problem &P)
 {
     const SolverOptions &o = P.opts;
     if (!o.gs_boundary) MOCGPU_THROW(1, "the batched engine runs the Gauss-Seidel boundary update only");
-    if (o.incoming_update) MOCGPU_THROW(1, "the batched engine does not run the incoming boundary flux update");
     const bool cm = o.cmfd && o.cmfd_enabled;
+    const int inc = cm ? o.incoming_update : 0; // the update follows a CMFD solve
     if (!configured_) {
         pol_ = P.flat.pol_per_set;
         n_inner_ = o.n_inner;
         cmfd_ = cm;
+        incoming_mode_ = inc;
         configured_ = true;
         return;
     }
-    if (P.flat.pol_per_set != pol_ || o.n_inner != n_inner_ || cm != cmfd_)
+    if (P.flat.pol_per_set != pol_ || o.n_inner != n_inner_ || cm != cmfd_ || inc != incoming_mode_)
         MOCGPU_THROW(1, "solve does not share the batch's sweep configuration (polar angles per set, inner "
-                        "iterations, CMFD)");
+                        "iterations, CMFD, incoming flux update)");
 }
 
 size_t BatchEngine::geometry_estimate(const FlatProblem &f) const
@@ -270,9 +271,9 @@ bool BatchEngine::try_admit(Pending &p)
     Sweeper &sw = *S.sw;
     sw.set_coarse_enabled(cmfd_);
     sw.initialize();
-    // per-solve scalars RED_K .. RED_MAX_ITER, with the convergence test's
+    // per-solve scalars RED_K .. RED_CMFD_SOLVES, with the convergence test's
     // parameters (<solver k_tol psi_tol min_iter max_iter>) for kb_retire
-    double init[RED_MAX_ITER - RED_K + 1] = {0};
+    double init[RED_CMFD_SOLVES - RED_K + 1] = {0};
     init[RED_K - RED_K] = 1.0;
     init[RED_K_PREV - RED_K] = 1.0;
     init[RED_N_FISSILE - RED_K] = (double)sw.n_fissile();
@@ -468,6 +469,7 @@ void BatchEngine::capture(int r)
             launch_b_homogenize(b, stream_);
             launch_b_cmfd(b, stream_);
             launch_b_set_pin_flux(b, stream_);
+            if (incoming_mode_) launch_b_incoming_update(b, precision_, incoming_mode_, stream_);
         }
         launch_b_fission_source(b, stream_);
         launch_b_copy_old(b, stream_);

@@ -194,6 +194,7 @@ class BatchEngine {
     bool configured_ = false;
     int pol_ = 0, n_inner_ = 1;
     bool cmfd_ = false;
+    int incoming_mode_ = 0; // <solver incoming_update>, shared by every solve of the batch
 
     // device-side views and lists
     DevBuf<GeomView> d_gv_;

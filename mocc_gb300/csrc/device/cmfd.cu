@@ -1215,22 +1215,25 @@ namespace {
 // the solved coarse flux, and the two partial currents from them. Of the
 // partial currents the update reads only 2 (J+ + J-); that is stored per
 // [G][n_surf], the previous solve's values moving to part_old first.
-__global__ void k_store_partials(CmfdView c, double *part, double *part_old)
+__device__ __forceinline__ void store_partial(const CmfdView &c, double *part, double *part_old, int idx)
 {
     const int ns = c.n_surf, n = c.n_cell;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < c.G * ns; idx += gridDim.x * blockDim.x) {
-        const int g = idx / ns, is = idx % ns;
-        int c1, c2, nrm;
-        surf_info(c, is, c1, c2, nrm);
-        const double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
-        const double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
-        const double dt = c.d_tilde[idx], dh = c.d_hat[idx], st = c.s_tilde[idx], sh = c.s_hat[idx];
-        const double j = -dt * (fr - fl) + dh * (fr + fl);
-        const double sf = (c1 >= 0) ? st * fl + (1.0 - st) * fr + sh * (fl + fr) : st * fr + sh * (fl + fr);
-        const double jp = 0.25 * sf + 0.5 * j, jm = 0.25 * sf - 0.5 * j;
-        part_old[idx] = part[idx];
-        part[idx] = 2.0 * (jp + jm);
-    }
+    const int g = idx / ns, is = idx % ns;
+    int c1, c2, nrm;
+    surf_info(c, is, c1, c2, nrm);
+    const double fr = c2 >= 0 ? c.flux[(size_t)g * n + c2] : 0.0;
+    const double fl = c1 >= 0 ? c.flux[(size_t)g * n + c1] : 0.0;
+    const double dt = c.d_tilde[idx], dh = c.d_hat[idx], st = c.s_tilde[idx], sh = c.s_hat[idx];
+    const double j = -dt * (fr - fl) + dh * (fr + fl);
+    const double sf = (c1 >= 0) ? st * fl + (1.0 - st) * fr + sh * (fl + fr) : st * fr + sh * (fl + fr);
+    const double jp = 0.25 * sf + 0.5 * j, jm = 0.25 * sf - 0.5 * j;
+    part_old[idx] = part[idx];
+    part[idx] = 2.0 * (jp + jm);
+}
+__global__ void k_store_partials(CmfdView c, double *part, double *part_old)
+{
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < c.G * c.n_surf; idx += gridDim.x * blockDim.x)
+        store_partial(c, part, part_old, idx);
 }
 
 // One boundary entry: scaled by the change of 2 (J+ + J-) on its surface
@@ -1268,8 +1271,8 @@ __device__ __forceinline__ int entry_surface(const CmfdView &c, int cell, int su
 // is the start of exactly one track in its direction, so no two threads
 // write the same entry.
 template <typename Real>
-__global__ void k_incoming_update(GeomView gv, CmfdView c, Real *psi_in, const double *part, const double *part_old,
-                                  int mode, int has_old)
+__device__ void incoming_update(const GeomView &gv, const CmfdView &c, Real *psi_in, const double *part,
+                                const double *part_old, int mode, int has_old)
 {
     const int per_g = gv.n_tracks * gv.pol;
     const int total = gv.G * per_g;
@@ -1290,8 +1293,60 @@ __global__ void k_incoming_update(GeomView gv, CmfdView c, Real *psi_in, const d
         }
     }
 }
+template <typename Real>
+__global__ void k_incoming_update(GeomView gv, CmfdView c, Real *psi_in, const double *part, const double *part_old,
+                                  int mode, int has_old)
+{
+    incoming_update<Real>(gv, c, psi_in, part, part_old, mode, has_old);
+}
+
+// Batched forms, one solve per blockIdx.y (solves that ended are frozen):
+// the partial currents of each solve's CMFD solution, the boundary-flux
+// update (a previous CMFD solve's currents exist once RED_CMFD_SOLVES > 0),
+// then the count of CMFD solves.
+__global__ void kb_store_partials(BatchViews b)
+{
+    if ((int)blockIdx.y >= *b.n_act) return;
+    const int slot = b.act[blockIdx.y];
+    const StateView &st = b.sv[slot];
+    if (st.red[RED_DONE] != 0.0) return;
+    const CmfdView &c = b.cv[slot];
+    const int n1 = c.G * c.n_surf;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n1; idx += gridDim.x * blockDim.x)
+        store_partial(c, st.part, st.part + n1, idx);
+}
+template <typename Real> __global__ void kb_incoming_update(BatchViews b, int mode)
+{
+    if ((int)blockIdx.y >= *b.n_act) return;
+    const int slot = b.act[blockIdx.y];
+    const StateView &st = b.sv[slot];
+    if (st.red[RED_DONE] != 0.0) return;
+    const CmfdView &c = b.cv[slot];
+    const double *part = st.part;
+    incoming_update<Real>(b.gv[slot], c, (Real *)st.psi_in, part, part + (size_t)c.G * c.n_surf, mode,
+                          st.red[RED_CMFD_SOLVES] > 0.0 ? 1 : 0);
+}
+__global__ void kb_count_cmfd(BatchViews b)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *b.n_act) return;
+    double *red = b.sv[b.act[i]].red;
+    if (red[RED_DONE] == 0.0) red[RED_CMFD_SOLVES] += 1.0;
+}
 
 } // namespace
+
+void launch_b_incoming_update(const BatchViews &b, int precision, int mode, cudaStream_t s)
+{
+    if (mode != 1 && mode != 2) throw Error(1, "incoming update mode must be 1 (MOCC) or 2 (entry surface)");
+    note_launch_external();
+    kb_store_partials<<<dim3((unsigned)((b.max_surf * b.max_g + 255) / 256), (unsigned)b.cap), 256, 0, s>>>(b);
+    note_launch_external();
+    if (precision == 0) kb_incoming_update<double><<<dim3(64, (unsigned)b.cap), 256, 0, s>>>(b, mode);
+    else kb_incoming_update<float><<<dim3(64, (unsigned)b.cap), 256, 0, s>>>(b, mode);
+    note_launch_external();
+    kb_count_cmfd<<<(b.cap + 127) / 128, 128, 0, s>>>(b);
+}
 
 void launch_incoming_update(const GeomView &gv, const CmfdView &c, void *psi_in, int precision, double *part,
                             int mode, int has_old, cudaStream_t s)

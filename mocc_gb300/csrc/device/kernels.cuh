@@ -64,6 +64,7 @@ struct StateView {
     // tallied, [n_surf] each (native float reductions), folded into cur and
     // sflux by the normalisation and cleared
     float *cur32, *sfl32;
+    double *part;              // [2][G][n_surf]: 2 (J+ + J-) of the last CMFD solve and the one before
     double *cflux;             // coarse (pin) flux [G][n_pin]
     double *red;               // per-solve scalars and reduction scratch (64 doubles)
     unsigned *status;
@@ -134,7 +135,8 @@ enum RedSlot {
     RED_K_TOL = 32,      // the solve's <solver k_tol>, psi_tol, min_iter, max_iter
     RED_PSI_TOL = 33,
     RED_MIN_ITER = 34,
-    RED_MAX_ITER = 35
+    RED_MAX_ITER = 35,
+    RED_CMFD_SOLVES = 36 // CMFD solves since admission (the incoming-flux update's "previous currents" test)
 };
 // How a batched solve ended (RED_DONE and the summary row).
 enum BatchDone { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_NONPOSITIVE = 2, DONE_NAN = 3, DONE_MAX_ITER = 4,
@@ -178,6 +180,9 @@ void launch_b_errors(const BatchViews &b, cudaStream_t s);   // error_k, error_p
 // end are frozen: every batched kernel skips them from the next replay on.
 void launch_b_retire(const BatchViews &b, double *out, cudaStream_t s);
 void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
+// MoCSweeper::update_incoming_flux after each solve's CMFD (mode 1 or 2 as
+// for launch_incoming_update); counts the CMFD solves of each solve.
+void launch_b_incoming_update(const BatchViews &b, int precision, int mode, cudaStream_t s);
 // pin powers of every active solve: out[slot * stride + cell], total at n_pin
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
 // Batched sweep (Gauss-Seidel boundary update) in streaming shape `shape`:

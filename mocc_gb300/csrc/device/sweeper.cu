@@ -120,6 +120,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     s.sflux = sflux_.p;
     s.cur32 = cur32_.p;
     s.sfl32 = cur32_.p + f.n_surf;
+    s.part = part_.p;
     s.cflux = cflux_.p;
     s.red = red_.p;
     s.status = status_.p;

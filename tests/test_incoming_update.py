@@ -141,12 +141,54 @@ def test_mixed_precision_update_within_tolerance():
 
 
 @pytest.mark.gpu
-def test_batch_engine_refuses_the_update():
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batched_update_matches_single_solves(mode):
+    # the batch engine runs the update after each solve's CMFD inside its
+    # captured outer iteration; every solve must give its single-solve result
+    # (FP64: same iterations, k to 1e-9, pins to 1e-8), vacuum faces included
+    name = {1: "mocc", 2: "surface"}[mode]
+    cases = [W.lattice_case(n, 8, 0.05, "double", seed=1000 + n) for n in (1, 3)]
+    cases.append(CASES["core_vacuum"]())
+    probs = [m.Problem(_with(x, name), s) for x, s in cases]
+    E = m.BatchEngine(precision=0, capacity=4, bundles_per_unit=1)
+    ids = [E.submit(P) for P in probs]
+    E.run()
+    for P, i in zip(probs, ids):
+        r = E.take(i)
+        assert r is not None and r["error"] == 0, r
+        S = m.EigenSolver(P, 0)
+        ref = S.solve()
+        assert r["converged"] == ref["converged"]
+        assert r["iterations"] == ref["iterations"]
+        assert abs(r["k"] - ref["k"]) < 1e-9
+        p, q = np.ravel(r["pin_powers"]), np.ravel(S.pin_powers())
+        assert np.max(np.abs(p - q)[q > 0] / q[q > 0]) < 1e-8
+
+
+@pytest.mark.gpu
+def test_batch_engine_keeps_one_update_mode():
+    # the update is part of the captured launch sequence, so every solve of
+    # a batch must ask for the same mode
     xml, xsl = W.lattice_case(3, 8, 0.05, "mixed", seed=1000)
     E = m.BatchEngine(precision=1, capacity=2)
-    with pytest.raises(m.MocgpuError) as e:
-        E.submit_xml(_with(xml, "surface"), xsl)
-    assert e.value.code == 1
+    E.submit_xml(_with(xml, "surface"), xsl)
+    for other in ("off", "mocc"):
+        with pytest.raises(m.MocgpuError) as e:
+            E.submit_xml(_with(xml, other), xsl)
+        assert e.value.code == 1
+
+
+@pytest.mark.gpu
+def test_mixed_precision_batched_update_within_tolerance():
+    xml, xsl = W.minicore(n_lat=3, n_azi=4, spacing=0.1, precision="mixed")
+    xml = _with(xml, "surface")
+    E = m.BatchEngine(precision=1, capacity=2)
+    i = E.submit_xml(xml, xsl)
+    E.run()
+    r = E.take(i)
+    assert r["error"] == 0 and r["converged"]
+    ref = oracle.OracleSolver.from_xml(xml, xsl).solve()
+    assert 1e5 * abs(r["k"] - ref["k"]) / ref["k"] < 10.0
 
 
 @pytest.mark.gpu
