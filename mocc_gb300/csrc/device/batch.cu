@@ -478,8 +478,11 @@ void BatchEngine::capture(int r)
             else launch_b_group_source<float>(b, g, stream_);
             for (int inner = 0; inner < n_inner_; inner++) {
                 const bool last = inner == n_inner_ - 1;
-                const bool cur = last && cmfd_;
-                if (cur) launch_b_zero_currents(b, g, stream_);
+                const bool tally = last && cmfd_;
+                // the CMFD operator reads the net currents; the incoming-flux
+                // update's partial currents read the surface fluxes too
+                const int cur = tally ? (incoming_mode_ ? 1 : 2) : 0;
+                if (tally) launch_b_zero_currents(b, g, stream_);
                 for (int ph = 0; ph < 2; ph++) {
                     const int2 *items = d_items_.p + (size_t)ph * shape_.items_cap;
                     const int *nit = d_nitems_.p + (size_t)g * 2 + ph;

@@ -187,9 +187,11 @@ void launch_b_incoming_update(const BatchViews &b, int precision, int mode, cuda
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
 // Batched sweep (Gauss-Seidel boundary update) in streaming shape `shape`:
 // rows per chunk and chunks in flight of each warp's segment ring, one of
-// kSweepShapeCount built shapes (FP64: shape 0 only).
+// kSweepShapeCount built shapes (FP64: shape 0 only). cur: 0 no coarse
+// tallies, 1 net currents and surface fluxes (the incoming-flux update reads
+// the surface fluxes), 2 net currents only.
 template <typename Real>
-void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool cur,
+void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, int cur,
                     int pol, int bundles_per_unit, int max_local, int shape, int *counter, cudaStream_t s);
 // Sets the shared-memory limit of the batched sweep ahead of graph capture.
 template <typename Real> void prepare_b_sweep(int pol, int bundles_per_unit, int max_local, int shape);

@@ -76,7 +76,7 @@ template void prepare_b_sweep<float>(int, int, int, int);
 template void prepare_b_sweep<double>(int, int, int, int);
 
 template <typename Real>
-void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, bool cur,
+void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group, int cur,
                     int pol, int bundles_per_unit, int max_local, int shape, int *counter, cudaStream_t s)
 {
     if (max_items <= 0) return;
@@ -91,9 +91,9 @@ void launch_b_sweep(const BatchViews &b, const int2 *items, const int *n_items, 
                                  counter, s))
         throw Error(1, "no batched sweep shape " + std::to_string(shape));
 }
-template void launch_b_sweep<float>(const BatchViews &, const int2 *, const int *, int, int, bool, int, int, int, int,
+template void launch_b_sweep<float>(const BatchViews &, const int2 *, const int *, int, int, int, int, int, int, int,
                                     int *, cudaStream_t);
-template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int *, int, int, bool, int, int, int, int,
+template void launch_b_sweep<double>(const BatchViews &, const int2 *, const int *, int, int, int, int, int, int, int,
                                      int *, cudaStream_t);
 
 } // namespace mocgpu

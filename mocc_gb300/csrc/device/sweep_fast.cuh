@@ -836,6 +836,7 @@ template <typename Real, class SH> static void prepare_batched_shape(int pol, in
 #define MOCGPU_P(NP)                                                                                                   \
     case NP:                                                                                                           \
         ensure_smem_limit((const void *)kb_sweep_fast<Real, NP, 0, SH>, smem);                                        \
+        ensure_smem_limit((const void *)kb_sweep_fast<Real, NP, 1, SH>, smem);                                        \
         ensure_smem_limit((const void *)kb_sweep_fast<Real, NP, 2, SH>, smem);                                        \
         return;
         MOCGPU_P(1)
@@ -864,15 +865,19 @@ static void launch_batched(const BatchViews &b, const int2 *items, const int *n_
     k<<<grid, 32 * nwarps, smem, s>>>(b, items, n_items, group, counter);
 }
 
+// cur: 0 no coarse tallies, 1 net currents and surface fluxes, 2 net
+// currents only (all the CMFD operator reads)
 template <typename Real, class SH>
 static void launch_batched_shape(const BatchViews &b, const int2 *items, const int *n_items, int max_items, int group,
-                                 bool cur, int pol, int bundles_per_unit, int max_local, int *counter, cudaStream_t s)
+                                 int cur, int pol, int bundles_per_unit, int max_local, int *counter, cudaStream_t s)
 {
     switch (pol) {
 #define MOCGPU_B(NP)                                                                                                   \
     case NP:                                                                                                           \
-        if (cur) launch_batched<Real, NP, 2, SH>(b, items, n_items, max_items, group, bundles_per_unit, max_local,    \
-                                                 counter, s);                                                          \
+        if (cur == 2) launch_batched<Real, NP, 2, SH>(b, items, n_items, max_items, group, bundles_per_unit,          \
+                                                      max_local, counter, s);                                          \
+        else if (cur == 1) launch_batched<Real, NP, 1, SH>(b, items, n_items, max_items, group, bundles_per_unit,     \
+                                                           max_local, counter, s);                                     \
         else launch_batched<Real, NP, 0, SH>(b, items, n_items, max_items, group, bundles_per_unit, max_local,        \
                                              counter, s);                                                              \
         return;
@@ -890,10 +895,10 @@ static void launch_batched_shape(const BatchViews &b, const int2 *items, const i
 bool prepare_b_sweep_shapes_a(int shape, int pol, int bundles_per_unit, int max_local);
 bool prepare_b_sweep_shapes_b(int shape, int pol, int bundles_per_unit, int max_local);
 bool launch_b_sweep_shapes_a(int shape, const BatchViews &b, const int2 *items, const int *n_items, int max_items,
-                             int group, bool cur, int pol, int bundles_per_unit, int max_local, int *counter,
+                             int group, int cur, int pol, int bundles_per_unit, int max_local, int *counter,
                              cudaStream_t s);
 bool launch_b_sweep_shapes_b(int shape, const BatchViews &b, const int2 *items, const int *n_items, int max_items,
-                             int group, bool cur, int pol, int bundles_per_unit, int max_local, int *counter,
+                             int group, int cur, int pol, int bundles_per_unit, int max_local, int *counter,
                              cudaStream_t s);
 
 } // namespace mocgpu

@@ -14,7 +14,7 @@ bool prepare_b_sweep_shapes_a(int shape, int pol, int bundles_per_unit, int max_
 }
 
 bool launch_b_sweep_shapes_a(int shape, const BatchViews &b, const int2 *items, const int *n_items, int max_items,
-                              int group, bool cur, int pol, int bundles_per_unit, int max_local, int *counter,
+                              int group, int cur, int pol, int bundles_per_unit, int max_local, int *counter,
                               cudaStream_t s)
 {
     switch (shape) {
