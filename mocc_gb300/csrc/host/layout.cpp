@@ -137,6 +137,19 @@ SweepLayout build_sweep_layout(const FlatProblem &f, bool gs, int tracks_per_uni
                 L.wu.push_back(u);
             }
         }
+        // longest units first: a single-solve launch has one CTA per unit,
+        // dispatched in index order, so the long units start in the first
+        // wave and the short ones fill the tail
+        auto rows = [&](const WorkUnitHost &u) {
+            int mx = 0, sum = 0;
+            for (int b = 0; b < u.n_bundles; b++) {
+                mx = std::max(mx, L.bundle_nrows[u.bundle_begin + b]);
+                sum += L.bundle_nrows[u.bundle_begin + b];
+            }
+            return std::make_pair(mx, sum);
+        };
+        std::stable_sort(L.wu.begin() + L.phase_wu_begin.back(), L.wu.end(),
+                         [&](const WorkUnitHost &a, const WorkUnitHost &b) { return rows(a) > rows(b); });
     }
     L.phase_wu_begin.push_back((int)L.wu.size());
     L.padding = real ? (double)padded / (double)real - 1.0 : 0.0;
