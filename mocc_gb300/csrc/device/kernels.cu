@@ -409,7 +409,7 @@ void launch_zero_radial_currents(const GeomView &g, const StateView &st, int gro
 {
     MOCGPU_CUDA(cudaMemsetAsync(st.cur + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
     MOCGPU_CUDA(cudaMemsetAsync(st.sflux + (size_t)group * g.n_surf, 0, sizeof(double) * g.n_surf, s));
-    MOCGPU_CUDA(cudaMemsetAsync(st.cur32, 0, sizeof(float) * 2 * g.n_surf, s));
+    MOCGPU_CUDA(cudaMemsetAsync(st.cur32, 0, sizeof(float) * 2 * kCurCopies * g.n_surf, s));
 }
 
 // Currents per unit area on the x/y-normal surfaces (moc_current_worker.hpp:272-318),
@@ -418,10 +418,16 @@ __device__ __forceinline__ void normalize_surface(const GeomView &g, const State
                                                   const double *area)
 {
     const size_t k = (size_t)group * g.n_surf + i;
-    st.cur[k] = (st.cur[k] + (double)st.cur32[i]) / area[i];
-    st.sflux[k] = (st.sflux[k] + (double)st.sfl32[i]) / area[i];
-    st.cur32[i] = 0.f;
-    st.sfl32[i] = 0.f;
+    float c = 0.f, f = 0.f;
+#pragma unroll
+    for (int j = 0; j < kCurCopies; j++) {
+        c += st.cur32[(size_t)j * g.n_surf + i];
+        f += st.sfl32[(size_t)j * g.n_surf + i];
+        st.cur32[(size_t)j * g.n_surf + i] = 0.f;
+        st.sfl32[(size_t)j * g.n_surf + i] = 0.f;
+    }
+    st.cur[k] = (st.cur[k] + (double)c) / area[i];
+    st.sflux[k] = (st.sflux[k] + (double)f) / area[i];
 }
 __global__ void k_normalize_currents(GeomView g, StateView st, int group, const double *area)
 {
@@ -741,8 +747,10 @@ __global__ void kb_zero_currents(BatchViews b, int group)
     if (i >= g.n_surf || group >= g.G) return;
     st.cur[(size_t)group * g.n_surf + i] = 0.0;
     st.sflux[(size_t)group * g.n_surf + i] = 0.0;
-    st.cur32[i] = 0.f;
-    st.sfl32[i] = 0.f;
+    for (int j = 0; j < kCurCopies; j++) {
+        st.cur32[(size_t)j * g.n_surf + i] = 0.f;
+        st.sfl32[(size_t)j * g.n_surf + i] = 0.f;
+    }
 }
 void launch_b_zero_currents(const BatchViews &b, int group, cudaStream_t s)
 {

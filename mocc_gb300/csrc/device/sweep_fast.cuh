@@ -598,8 +598,8 @@ __device__ __forceinline__ void sweep_unit(const GeomView &g, const FastView &fv
     U.psi_out = (Real *)st.psi_out;
     U.cur = st.cur + (size_t)group * g.n_surf;
     U.sfl = st.sflux + (size_t)group * g.n_surf;
-    U.cur32 = st.cur32;
-    U.sfl32 = st.sfl32;
+    U.cur32 = st.cur32 + (size_t)(blockIdx.x % kCurCopies) * g.n_surf;
+    U.sfl32 = st.sfl32 + (size_t)(blockIdx.x % kCurCopies) * g.n_surf;
     U.tally = (float *)st.tally;
     U.ny_set = g.set_ny[u.set];
 

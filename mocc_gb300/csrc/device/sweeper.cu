@@ -73,7 +73,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     sflux_.alloc((size_t)G * f.n_surf);
     cur_.zero(stream_);
     sflux_.zero(stream_);
-    cur32_.alloc((size_t)2 * f.n_surf);
+    cur32_.alloc((size_t)2 * kCurCopies * f.n_surf);
     cur32_.zero(stream_);
     red_.alloc(64);
     red_.zero(stream_);
@@ -119,7 +119,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     s.cur = cur_.p;
     s.sflux = sflux_.p;
     s.cur32 = cur32_.p;
-    s.sfl32 = cur32_.p + f.n_surf;
+    s.sfl32 = cur32_.p + (size_t)kCurCopies * f.n_surf;
     s.part = part_.p;
     s.cflux = cflux_.p;
     s.red = red_.p;

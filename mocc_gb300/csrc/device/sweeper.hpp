@@ -132,7 +132,7 @@ class Sweeper {
     DevBuf<double> xstr_, xsnf_, xsf_, xsch_, scat_;
     // state
     DevBuf<double> phi_, phi_old_, fs_, fs_prev_, src1g_, cur_, sflux_, red_;
-    DevBuf<float> cur32_; // FP32 sweep: [2][n_surf] crossing currents and surface fluxes of one group
+    DevBuf<float> cur32_; // FP32 sweep: [2][kCurCopies][n_surf] crossing currents and surface fluxes of one group
     DevBuf<unsigned char> qbar_, sigt_, tally_, psi_in_, psi_out_;
     DevBuf<unsigned> status_;
     // CMFD
