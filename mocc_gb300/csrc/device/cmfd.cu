@@ -262,10 +262,153 @@ __device__ void build_source(const CmfdView &c, int g, double *b)
 // is x += alpha D^-1 p + omega D^-1 s), which gives the same iterates as
 // applying D^-1 to p and s. x is in/out; w holds 8 work vectors; rr0 returns
 // ||b - A x||^2 of the incoming x.
+// The same iteration with each thread's R rows of every vector in registers
+// (rows i = threadIdx.x + j blockDim.x): only the two vectors the operator
+// is applied to, p and s, go through shared memory (w and w + n), where the
+// neighbours' entries are read. Each row's off-diagonal entries are loaded
+// once per solve; a missing neighbour has a zero entry and reads a slot in
+// range (the index clamped), which adds exactly nothing. The arithmetic of every entry, the
+// block sums and the barriers are those of the shared-memory form below:
+// the shared-memory traffic of an iteration drops from about 35 accesses
+// per row to 10.
+template <int R>
+__device__ int bicgstab_reg(const CmfdView &c, Blk &B, const double *m, const double *b, double *x, double tol,
+                            int max_it, double *w, double &rr0)
+{
+    const int n = c.n_cell, nx = c.nx, bd = blockDim.x;
+    double *P = w, *S = w + n;
+    double xr[R], rr_[R], r0[R], p[R], v[R], bv[R], cw[R], ce[R], cs[R], cn[R];
+    bool ok[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const int i = threadIdx.x + j * bd;
+        ok[j] = i < n;
+        const int ii = ok[j] ? i : 0;
+        const int ix = ii % nx;
+        cw[j] = (ok[j] && ix > 0) ? m[n + ii] : 0.0;
+        ce[j] = (ok[j] && ix < nx - 1) ? m[2 * n + ii] : 0.0;
+        cs[j] = (ok[j] && ii >= nx) ? m[3 * n + ii] : 0.0;
+        cn[j] = (ok[j] && ii + nx < n) ? m[4 * n + ii] : 0.0;
+        bv[j] = ok[j] ? b[ii] : 0.0;
+        xr[j] = ok[j] ? x[ii] * m[ii] : 0.0;
+        p[j] = 0.0;
+        v[j] = 0.0;
+    }
+    // row j of the unit-diagonal operator applied to the vector in V (own entry e)
+    auto apply = [&](const double *V, int j, double e) {
+        const int i = threadIdx.x + j * bd;
+        double a = e;
+        a = fma(cw[j], V[max(i - 1, 0)], a);
+        a = fma(ce[j], V[min(i + 1, n - 1)], a);
+        a = fma(cs[j], V[max(i - nx, 0)], a);
+        a = fma(cn[j], V[min(i + nx, n - 1)], a);
+        return a;
+    };
+    // r = b - A xh, with xh published in x
+    auto residual = [&](double &acc) {
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if (ok[j]) x[threadIdx.x + j * bd] = xr[j];
+        B.sync();
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            const double ri = ok[j] ? bv[j] - apply(x, j, xr[j]) : 0.0;
+            rr_[j] = ri;
+            r0[j] = ri;
+            acc += ri * ri;
+        }
+    };
+    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
+    double rr = 0.0, bb = 0.0;
+    residual(rr);
+#pragma unroll
+    for (int j = 0; j < R; j++) bb += bv[j] * bv[j];
+    B.sum2(rr, bb);
+    rr0 = rr;
+    if (bb == 0.0) {
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if (ok[j]) x[threadIdx.x + j * bd] = 0.0;
+        B.sync();
+        return 0;
+    }
+    double r0_sq = rr, rho = 1.0, alpha = 1.0, om = 1.0;
+    const double tol2 = tol * tol * bb;
+    int it = 0, restarts = 0;
+    double rho_new = rr;
+    while (rr > tol2 && it < max_it) {
+        double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0_sq) {
+            B.sync();
+            double acc = 0.0;
+            residual(acc);
+            acc = B.sum(acc);
+            rho = r0_sq = acc;
+            if (restarts++ == 0) it = 0;
+        }
+        const double beta = (rho / rho_old) * (alpha / om);
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            p[j] = rr_[j] + beta * (p[j] - om * v[j]);
+            if (ok[j]) P[threadIdx.x + j * bd] = p[j];
+        }
+        B.sync();
+        double r0v = 0.0;
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            v[j] = ok[j] ? apply(P, j, p[j]) : 0.0;
+            r0v += r0[j] * v[j];
+        }
+        r0v = B.sum(r0v);
+        alpha = rho / r0v;
+        double sv[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            sv[j] = rr_[j] - alpha * v[j];
+            if (ok[j]) S[threadIdx.x + j * bd] = sv[j];
+        }
+        B.sync();
+        double tt = 0.0, ts = 0.0, tv[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            tv[j] = ok[j] ? apply(S, j, sv[j]) : 0.0;
+            tt += tv[j] * tv[j];
+            ts += tv[j] * sv[j];
+        }
+        B.sum2(tt, ts);
+        om = (tt > 0.0) ? ts / tt : 0.0;
+        double nrr = 0.0, nrho = 0.0;
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            xr[j] += alpha * p[j] + om * sv[j];
+            const double ri = sv[j] - om * tv[j];
+            rr_[j] = ri;
+            nrr += ri * ri;
+            nrho += r0[j] * ri;
+        }
+        B.sum2(nrr, nrho);
+        rr = nrr;
+        rho_new = nrho;
+        it++;
+    }
+    B.sync();
+#pragma unroll
+    for (int j = 0; j < R; j++)
+        if (ok[j]) x[threadIdx.x + j * bd] = xr[j] * m[5 * n + threadIdx.x + j * bd];
+    B.sync();
+    return it;
+}
+
 __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double *b, double *x, double tol, int max_it,
                         double *w, double &rr0)
 {
     const int n = c.n_cell, nx = c.nx;
+    switch ((n + (int)blockDim.x - 1) / (int)blockDim.x) {
+    case 1: return bicgstab_reg<1>(c, B, m, b, x, tol, max_it, w, rr0);
+    case 2: return bicgstab_reg<2>(c, B, m, b, x, tol, max_it, w, rr0);
+    default: break;
+    }
     double *r = w, *r0 = w + n, *p = w + 2 * n, *v = w + 3 * n, *s = w + 6 * n, *t = w + 7 * n;
     const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
     for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] *= m[i];
