@@ -57,23 +57,33 @@ struct Blk {
         if (nw == 1) __syncwarp();
         else __syncthreads();
     }
+    // The FP64 adds of a gathered sum run on the warp that gathers it. Warp
+    // w issues from scheduler w % 4, and with five warps scheduler 0 also
+    // carries warp 4's rows, so the sums are gathered by warps 1-3 (sum2:
+    // one value each on warps 2 and 3, sum: warp 1), spreading their FP64
+    // instructions over the less loaded schedulers' pipes.
+    __device__ int gather_warp(int k) const { return nw > 3 ? 1 + k : (nw > 1 ? k % nw : 0); }
+    __device__ double gather_one(const double *p) const
+    {
+        const int lane = threadIdx.x & 31;
+        double x = p[lane];
+        for (int w = 1; w < nw; w++) x += p[lane + 32 * w];
+        return warp_sum(x);
+    }
     __device__ void gathered2(double &a, double &b)
     {
         double *pa = scratch, *pb = scratch + 32 * nw, *res = scratch + 64 * nw;
         pa[threadIdx.x] = a;
         pb[threadIdx.x] = b;
         __syncthreads();
-        if (threadIdx.x < 32) {
-            double x = pa[threadIdx.x], y = pb[threadIdx.x];
-            for (int w = 1; w < nw; w++) {
-                x += pa[threadIdx.x + 32 * w];
-                y += pb[threadIdx.x + 32 * w];
-            }
-            warp_sum2(x, y);
-            if (threadIdx.x == 0) {
-                res[0] = x;
-                res[1] = y;
-            }
+        const int w = threadIdx.x >> 5;
+        if (w == gather_warp(1)) {
+            const double x = gather_one(pa);
+            if ((threadIdx.x & 31) == 0) res[0] = x;
+        }
+        if (w == gather_warp(2)) {
+            const double y = gather_one(pb);
+            if ((threadIdx.x & 31) == 0) res[1] = y;
         }
         __syncthreads();
         a = res[0];
@@ -84,11 +94,9 @@ struct Blk {
         double *pa = scratch, *res = scratch + 64 * nw;
         pa[threadIdx.x] = a;
         __syncthreads();
-        if (threadIdx.x < 32) {
-            double x = pa[threadIdx.x];
-            for (int w = 1; w < nw; w++) x += pa[threadIdx.x + 32 * w];
-            x = warp_sum(x);
-            if (threadIdx.x == 0) res[0] = x;
+        if ((threadIdx.x >> 5) == gather_warp(0)) {
+            const double x = gather_one(pa);
+            if ((threadIdx.x & 31) == 0) res[0] = x;
         }
         __syncthreads();
         return res[0];
@@ -347,7 +355,8 @@ __device__ int bicgstab_reg(const CmfdView &c, Blk &B, const double *m, const do
             rho = r0_sq = acc;
             if (restarts++ == 0) it = 0;
         }
-        const double beta = (rho / rho_old) * (alpha / om);
+        // Eigen's (rho / rho_old) (alpha / omega) with one division
+        const double beta = (rho * alpha) / (rho_old * om);
 #pragma unroll
         for (int j = 0; j < R; j++) {
             p[j] = rr_[j] + beta * (p[j] - om * v[j]);
