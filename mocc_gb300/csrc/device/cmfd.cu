@@ -459,7 +459,8 @@ __device__ int bicgstab(const CmfdView &c, Blk &B, const double *m, const double
             rho = r0_sq = acc;
             if (restarts++ == 0) it = 0;
         }
-        const double beta = (rho / rho_old) * (alpha / om);
+        // Eigen's (rho / rho_old) (alpha / omega) with one division
+        const double beta = (rho * alpha) / (rho_old * om);
         for (int i = threadIdx.x; i < n; i += blockDim.x) p[i] = r[i] + beta * (p[i] - om * v[i]);
         B.sync();
         double r0v = 0.0;
@@ -825,10 +826,148 @@ __device__ __forceinline__ double spmv_row_team(const Team &T, const double *m, 
     return v;
 }
 
+// bicgstab_reg() on the team's slices: each thread's R rows (cells
+// lo + threadIdx.x + j blockDim.x) of every vector in registers, p and s
+// published in this CTA's shared memory (w, w + slice) for the neighbours,
+// in a peer's slice read through distributed shared memory.
+template <int R>
+__device__ int bicgstab_team_reg(const CmfdView &c, Team &T, const double *m, const double *b, double *x, double tol,
+                                 int max_it, double *w, double &rr0)
+{
+    const int n = c.n_cell, nx = c.nx, s = T.slice, lo = T.lo, hi = T.hi, bd = blockDim.x;
+    double *P = w, *S = w + s;
+    double xr[R], rr_[R], r0[R], p[R], v[R], bv[R], cw[R], ce[R], cs[R], cn[R];
+    bool ok[R];
+#pragma unroll
+    for (int j = 0; j < R; j++) {
+        const int i = lo + (int)threadIdx.x + j * bd, li = i - lo;
+        ok[j] = i < hi;
+        const int ix = i % nx;
+        cw[j] = (ok[j] && ix > 0) ? m[s + li] : 0.0;
+        ce[j] = (ok[j] && ix < nx - 1) ? m[2 * s + li] : 0.0;
+        cs[j] = (ok[j] && i >= nx) ? m[3 * s + li] : 0.0;
+        cn[j] = (ok[j] && i + nx < n) ? m[4 * s + li] : 0.0;
+        bv[j] = ok[j] ? b[li] : 0.0;
+        xr[j] = ok[j] ? x[li] * m[li] : 0.0;
+        p[j] = 0.0;
+        v[j] = 0.0;
+    }
+    // row j applied to the slice vector V (own entry e); absent neighbours
+    // are skipped (their entries would be a peer load)
+    auto apply = [&](const double *V, int j, double e) {
+        const int i = lo + (int)threadIdx.x + j * bd;
+        double a = e;
+        if (cw[j] != 0.0) a = fma(cw[j], T.at(V, i - 1), a);
+        if (ce[j] != 0.0) a = fma(ce[j], T.at(V, i + 1), a);
+        if (cs[j] != 0.0) a = fma(cs[j], T.at(V, i - nx), a);
+        if (cn[j] != 0.0) a = fma(cn[j], T.at(V, i + nx), a);
+        return a;
+    };
+    auto residual = [&](double &acc) {
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if (ok[j]) x[threadIdx.x + j * bd] = xr[j];
+        T.sync();
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            const double ri = ok[j] ? bv[j] - apply(x, j, xr[j]) : 0.0;
+            rr_[j] = ri;
+            r0[j] = ri;
+            acc += ri * ri;
+        }
+    };
+    const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
+    double rr = 0.0, bb = 0.0;
+    residual(rr);
+#pragma unroll
+    for (int j = 0; j < R; j++) bb += bv[j] * bv[j];
+    T.sum2(rr, bb);
+    rr0 = rr;
+    if (bb == 0.0) {
+#pragma unroll
+        for (int j = 0; j < R; j++)
+            if (ok[j]) x[threadIdx.x + j * bd] = 0.0;
+        T.sync();
+        return 0;
+    }
+    double r0_sq = rr, rho = 1.0, alpha = 1.0, om = 1.0;
+    const double tol2 = tol * tol * bb;
+    int it = 0, restarts = 0;
+    double rho_new = rr;
+    while (rr > tol2 && it < max_it) {
+        double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0_sq) {
+            T.sync();
+            double acc = 0.0;
+            residual(acc);
+            acc = T.sum(acc);
+            rho = r0_sq = acc;
+            if (restarts++ == 0) it = 0;
+        }
+        // Eigen's (rho / rho_old) (alpha / omega) with one division
+        const double beta = (rho * alpha) / (rho_old * om);
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            p[j] = rr_[j] + beta * (p[j] - om * v[j]);
+            if (ok[j]) P[threadIdx.x + j * bd] = p[j];
+        }
+        T.sync();
+        double r0v = 0.0;
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            v[j] = ok[j] ? apply(P, j, p[j]) : 0.0;
+            r0v += r0[j] * v[j];
+        }
+        r0v = T.sum(r0v);
+        alpha = rho / r0v;
+        double sv[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            sv[j] = rr_[j] - alpha * v[j];
+            if (ok[j]) S[threadIdx.x + j * bd] = sv[j];
+        }
+        T.sync();
+        double tt = 0.0, ts = 0.0, tv[R];
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            tv[j] = ok[j] ? apply(S, j, sv[j]) : 0.0;
+            tt += tv[j] * tv[j];
+            ts += tv[j] * sv[j];
+        }
+        T.sum2(tt, ts);
+        om = (tt > 0.0) ? ts / tt : 0.0;
+        double nrr = 0.0, nrho = 0.0;
+#pragma unroll
+        for (int j = 0; j < R; j++) {
+            xr[j] += alpha * p[j] + om * sv[j];
+            const double ri = sv[j] - om * tv[j];
+            rr_[j] = ri;
+            nrr += ri * ri;
+            nrho += r0[j] * ri;
+        }
+        T.sum2(nrr, nrho);
+        rr = nrr;
+        rho_new = nrho;
+        it++;
+    }
+    T.sync();
+#pragma unroll
+    for (int j = 0; j < R; j++)
+        if (ok[j]) x[threadIdx.x + j * bd] = xr[j] * m[5 * s + threadIdx.x + j * bd];
+    T.sync();
+    return it;
+}
+
 // bicgstab() on the team's slices: the same iterates and stopping test.
 __device__ int bicgstab_team(const CmfdView &c, Team &T, const double *m, const double *b, double *x, double tol,
                              int max_it, double *w, double &rr0)
 {
+    switch ((T.hi - T.lo + (int)blockDim.x - 1) / (int)blockDim.x) {
+    case 1: return bicgstab_team_reg<1>(c, T, m, b, x, tol, max_it, w, rr0);
+    case 2: return bicgstab_team_reg<2>(c, T, m, b, x, tol, max_it, w, rr0);
+    default: break;
+    }
     const int n = c.n_cell, nx = c.nx, s = T.slice, lo = T.lo, hi = T.hi;
     double *r = w, *r0 = w + s, *p = w + 2 * s, *v = w + 3 * s, *sv = w + 4 * s, *t = w + 5 * s;
     const double eps2 = 2.220446049250313e-16 * 2.220446049250313e-16;
@@ -873,7 +1012,8 @@ __device__ int bicgstab_team(const CmfdView &c, Team &T, const double *m, const 
             rho = r0_sq = acc;
             if (restarts++ == 0) it = 0;
         }
-        const double beta = (rho / rho_old) * (alpha / om);
+        // Eigen's (rho / rho_old) (alpha / omega) with one division
+        const double beta = (rho * alpha) / (rho_old * om);
         for (int i = lo + (int)threadIdx.x; i < hi; i += blockDim.x) {
             const int li = i - lo;
             p[li] = r[li] + beta * (p[li] - om * v[li]);
