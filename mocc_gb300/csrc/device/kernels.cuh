@@ -211,9 +211,11 @@ void sweep_shape_info(int shape, int *rows, int *stages); // throws for a shape 
 void note_launches(int64_t n); // adds replayed launches to launch_count()
 
 // ---- launchers (stream-ordered) ----
+// currents: 0 none, 1 net currents and surface fluxes, 2 net currents only
+// (Gauss-Seidel; a Jacobi sweep tallies both)
 template <typename Real>
 void launch_sweep_fast(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,
-                       bool gs, bool currents, cudaStream_t s);
+                       bool gs, int currents, cudaStream_t s);
 template <typename Real> size_t fast_sweep_smem(const FastView &fv);
 void launch_fill(double *p, double v, int64_t n, cudaStream_t s);
 template <typename Real> void launch_fill_real(Real *p, double v, int64_t n, cudaStream_t s);

@@ -26,9 +26,10 @@ static void launch_one(const GeomView &g, const FastView &fv, const StateView &s
 
 template <typename Real, int NPOL>
 static void launch_np(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1, bool gs,
-                      bool cur, cudaStream_t s)
+                      int cur, cudaStream_t s)
 {
     if (gs && !cur) launch_one<Real, NPOL, true, 0>(g, fv, st, group, wu0, wu1, s);
+    else if (gs && cur == 2) launch_one<Real, NPOL, true, 2>(g, fv, st, group, wu0, wu1, s);
     else if (gs && cur) launch_one<Real, NPOL, true, 1>(g, fv, st, group, wu0, wu1, s);
     else if (!gs && !cur) launch_one<Real, NPOL, false, 0>(g, fv, st, group, wu0, wu1, s);
     else launch_one<Real, NPOL, false, 1>(g, fv, st, group, wu0, wu1, s);
@@ -36,7 +37,7 @@ static void launch_np(const GeomView &g, const FastView &fv, const StateView &st
 
 template <typename Real>
 void launch_sweep_fast(const GeomView &g, const FastView &fv, const StateView &st, int group, int wu0, int wu1,
-                       bool gs, bool cur, cudaStream_t s)
+                       bool gs, int cur, cudaStream_t s)
 {
     if (wu1 <= wu0) return;
     note_launch_external();
@@ -48,10 +49,10 @@ void launch_sweep_fast(const GeomView &g, const FastView &fv, const StateView &s
     default: throw Error(1, "unsupported number of polar angles per track set");
     }
 }
-template void launch_sweep_fast<float>(const GeomView &, const FastView &, const StateView &, int, int, int, bool, bool,
+template void launch_sweep_fast<float>(const GeomView &, const FastView &, const StateView &, int, int, int, bool, int,
                                        cudaStream_t);
 template void launch_sweep_fast<double>(const GeomView &, const FastView &, const StateView &, int, int, int, bool,
-                                        bool, cudaStream_t);
+                                        int, cudaStream_t);
 
 } // namespace mocgpu
 

@@ -396,6 +396,35 @@ template <typename Real, int NPOL, bool GS, int CUR, class SH> struct Walker {
         }
     }
 
+    // FP32 net currents only (CUR == 2): the crossings of a chunk are tallied
+    // after its rows. Each row's S before its update (the value a crossing
+    // at the row's leading boundary carries) is kept in the row's ring slot,
+    // whose length has been read by then; the slots are this lane's own and
+    // are refilled only after the warp's closing __syncwarp of the chunk.
+    // A row then costs one shared store instead of an event test, and the
+    // warp runs the crossing code once per crossing of its busiest lane in
+    // the chunk rather than at nearly every row.
+    static constexpr bool DEFER = FIXED && CUR == 2;
+    template <bool FWD>
+    __device__ __forceinline__ void chunk_events(const GeomView &g, const UnitCtx<Real, NPOL> &U, const Real *cl,
+                                                 int lo, int hi)
+    {
+        constexpr int step = FWD ? 32 : -32;
+        const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
+        const int2 none = make_int2(INT_MAX, 0);
+        // forward: boundaries lo .. hi-1 (row k's leading boundary is k);
+        // backward: hi .. lo+1 (row k's is k+1), in sweep order
+        while (FWD ? ev0.x < hi : (ev0.x > lo && ev0.x != INT_MAX)) {
+            const float Sb = cl[(FWD ? ev0.x - lo : hi - ev0.x) * step];
+            const int cd = ev0.y;
+            const float cs = (cd & 1) ? U.csgn[1] : U.csgn[0];
+            atomicAdd(U.cur32 + (cd >> 1), Sb * (FWD ? cs : -cs));
+            ev++;
+            ev0 = ev1;
+            ev1 = (ev + 1 < ev_end) ? evp[ev + 1] : none;
+        }
+    }
+
     // Sweeps this direction's chunks whose rows lie in [row_lo, row_hi).
     template <bool FWD>
     __device__ void run(const GeomView &g, const UnitCtx<Real, NPOL> &U, const FastView &fv, int row_lo, int row_hi,
@@ -506,18 +535,22 @@ template <typename Real, int NPOL, bool GS, int CUR, class SH> struct Walker {
                 for (int v = 0; v < UR; v++) factors(L[v], sq[v], E[v]);
 #pragma unroll
                 for (int v = 0; v < UR; v++) {
-                    if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k + v : hi - (k + v));
+                    if constexpr (DEFER) const_cast<Real *>(cl)[(k + v) * step] = S;
+                    else if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k + v : hi - (k + v));
                     update(sq[v], E[v], l[v]);
                 }
             }
             for (; k < nr; k++) {
-                if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k : hi - k);
                 const int l = cf[k * step];
                 const R2 sq = U.s_sq[l];
                 Real E[NPOL];
                 factors(cl[k * step], sq, E);
+                if constexpr (DEFER) const_cast<Real *>(cl)[k * step] = S;
+                else if (CUR && t >= 0) events<FWD>(g, U, FWD ? lo + k : hi - k);
                 update(sq, E, l);
             }
+            if constexpr (DEFER)
+                if (t >= 0) chunk_events<FWD>(g, U, cl, lo, hi);
             __syncwarp();
             c++;
         }

@@ -309,13 +309,13 @@ void Sweeper::group_source(int g)
 }
 
 // phase 0: octant-1 track sets, 1: octant-2 track sets, -1: all (Jacobi)
-void Sweeper::launch_phase(int g, int phase, bool gs, bool cur)
+void Sweeper::launch_phase(int g, int phase, bool gs, int cur)
 {
     if (opts_.sweep_kernel == 0) {
         int t0 = (phase == 1) ? geo_->phaseA_end : 0;
         int t1 = (phase == 0) ? geo_->phaseA_end : f_.n_tracks;
-        if (precision_ == 0) launch_sweep<double>(gv_, sv_, g, t0, t1, gs, cur, stream_);
-        else launch_sweep<float>(gv_, sv_, g, t0, t1, gs, cur, stream_);
+        if (precision_ == 0) launch_sweep<double>(gv_, sv_, g, t0, t1, gs, cur != 0, stream_);
+        else launch_sweep<float>(gv_, sv_, g, t0, t1, gs, cur != 0, stream_);
     } else {
         int w0 = (phase == 1) ? geo_->phase_wu[1] : 0;
         int w1 = (phase == 0) ? geo_->phase_wu[1] : geo_->phase_wu[2];
@@ -339,12 +339,13 @@ void Sweeper::sweep(int g)
     for (int inner = 0; inner < opts_.n_inner; inner++) {
         bool last = (inner == opts_.n_inner - 1);
         bool cur = last && coarse_enabled_;
+        const int mode = cur ? (tally_sflux_ ? 1 : 2) : 0;
         if (cur) launch_zero_radial_currents(gv_, sv_, g, stream_);
         if (opts_.gs_boundary) {
-            launch_phase(g, 0, true, cur);
-            launch_phase(g, 1, true, cur);
+            launch_phase(g, 0, true, mode);
+            launch_phase(g, 1, true, mode);
         } else {
-            launch_phase(g, -1, false, cur);
+            launch_phase(g, -1, false, cur ? 1 : 0);
             if (precision_ == 0) launch_jacobi_update<double>(gv_, sv_, g, stream_);
             else launch_jacobi_update<float>(gv_, sv_, g, stream_);
         }
@@ -584,6 +585,13 @@ EigenResult Sweeper::eigen_solve(int max_outer)
     auto t0 = std::chrono::steady_clock::now();
     EigenResult res;
     set_coarse_enabled(opts_.cmfd && opts_.cmfd_enabled);
+    // the CMFD operator reads the net currents only; the surface fluxes feed
+    // the partial currents of the incoming-flux update
+    struct Restore {
+        bool &f, v;
+        ~Restore() { f = v; }
+    } restore{tally_sflux_, tally_sflux_};
+    tally_sflux_ = opts_.incoming_update != 0;
     initialize();
     double k = 1.0, k_prev = 1.0;
     calc_fission_source(k);

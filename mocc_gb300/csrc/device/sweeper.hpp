@@ -113,7 +113,7 @@ class Sweeper {
 
   private:
     void check_status();
-    void launch_phase(int g, int phase, bool gs, bool cur);
+    void launch_phase(int g, int phase, bool gs, int cur); // cur as launch_sweep_fast's currents
     void launch_epilogue(int g, bool update_q);
     void after_cmfd();
 
@@ -123,6 +123,10 @@ class Sweeper {
     cudaStream_t stream_;
     std::shared_ptr<const DeviceGeometry> geo_;
     bool coarse_enabled_ = false;
+    // the last inner sweep tallies surface fluxes with the net currents (as
+    // MOCC's current worker does); the library's own eigenvalue iteration
+    // clears it unless the incoming-flux update reads them
+    bool tally_sflux_ = true;
     bool has_radial_ = false;
     int n_fissile_ = 0;
     int cmfd_solves_ = 0; // CMFD solves since initialize (the first has no previous partial currents)
