@@ -257,6 +257,12 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
             for (size_t i = 0; i < L.bundle_track.size(); i++)
                 if (L.bundle_track[i] >= 0) bbc[i] = make_int2(f.trk_bc0[L.bundle_track[i]], f.trk_bc1[L.bundle_track[i]]);
             bundle_bc_.upload(bbc);
+            std::vector<int4> bev(L.bundle_track.size(), make_int4(0, 0, 0, 0));
+            for (size_t i = 0; i < L.bundle_track.size(); i++) {
+                const int t = L.bundle_track[i];
+                if (t >= 0) bev[i] = make_int4(efb[t], efb[t + 1], ebb[t], ebb[t + 1]);
+            }
+            bundle_ev_.upload(bev);
         }
         local_fsr_.upload(L.local_fsr);
         blfsr_.upload(L.lfsr);
@@ -274,6 +280,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
         fv.bundle_nrows = bundle_nrows_.p;
         fv.bundle_track = bundle_track_.p;
         fv.bundle_bc = bundle_bc_.p;
+        fv.bundle_ev = bundle_ev_.p;
         fv.len = precision == 0 ? (const void *)blen_d_.p : (const void *)blen_f_.p;
         fv.lfsr = blfsr_.p;
         fv.local_fsr = local_fsr_.p;
@@ -393,7 +400,7 @@ DeviceGeometry::DeviceGeometry(const FlatProblem &f, int prec, int bundles_per_u
     bytes_ = seg_begin_.bytes() + trk_bc0_.bytes() * 3 + seg_fsr_.bytes() + seg_len_d_.bytes() + seg_len_f_.bytes() +
              fsr_mat_.bytes() + fsr_vol_.bytes() * 2 + sp_.bytes() + bc_off_.bytes() + wt_tgt_.bytes() +
              ev_fw_pt_.bytes() * 2 + ev_bw_pt_.bytes() * 2 + ev_fw_begin_.bytes() * 2 + wu_.bytes() +
-             ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() + psi_init_dev_.bytes() +
+             ev_fw_.bytes() + ev_bw_.bytes() + bundle_bc_.bytes() + bundle_ev_.bytes() + psi_init_dev_.bytes() +
              bundle_row_.bytes() + bundle_nrows_.bytes() + bundle_track_.bytes() + local_fsr_.bytes() +
              blen_f_.bytes() + blen_d_.bytes() + blfsr_.bytes() + exp_tab_.bytes() + trk_entry_.bytes() +
              win_.bytes();

@@ -62,6 +62,7 @@ class DeviceGeometry {
     DevBuf<SetPolar> sp_;
     DevBuf<int> ev_fw_begin_, ev_fw_pt_, ev_fw_code_, ev_bw_begin_, ev_bw_pt_, ev_bw_code_;
     DevBuf<int2> ev_fw_, ev_bw_, bundle_bc_;
+    DevBuf<int4> bundle_ev_;
     DevBuf<int4> trk_entry_;
     DevBuf<unsigned char> psi_init_dev_;
     DevBuf<int> pin_first_reg_, pin_cell_, pin_fuel_;

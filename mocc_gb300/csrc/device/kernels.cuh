@@ -112,6 +112,10 @@ struct FastView {
     const int64_t *bundle_row;
     const int *bundle_nrows, *bundle_track;
     const int2 *bundle_bc; // [bundle][32]: both boundary indices of each lane's track (0 for padding lanes)
+    // [bundle][32]: each lane's crossing events, forward [x, y) and backward
+    // [z, w) in GeomView::ev_fw / ev_bw (empty for padding lanes), so a warp
+    // starting a bundle reaches its first events in one load less
+    const int4 *bundle_ev;
     const void *len; // Real [rows][32]
     const uint16_t *lfsr;      // window-local FSR id of every row entry
     const int *local_fsr;      // window tables: window-local -> plane FSR ids

@@ -345,9 +345,10 @@ template <typename Real, int NPOL, bool GS, int CUR, class SH> struct Walker {
         }
         ev = ev_end = 0;
         const int2 *evp = FWD ? g.ev_fw : g.ev_bw;
-        if (CUR && t >= 0) {
-            ev = FWD ? g.ev_fw_begin[t] : g.ev_bw_begin[t];
-            ev_end = FWD ? g.ev_fw_begin[t + 1] : g.ev_bw_begin[t + 1];
+        if (CUR) {
+            const int4 e = fv.bundle_ev[(size_t)b * 32 + lane];
+            ev = FWD ? e.x : e.z;
+            ev_end = FWD ? e.y : e.w;
         }
         const int2 none = make_int2(INT_MAX, 0);
         ev0 = (CUR && ev < ev_end) ? evp[ev] : none;
