@@ -169,7 +169,11 @@ int mocgpu_get_pin_flux_1g(mocgpu_sweeper *s, int group, double *out /* [n_pin] 
 int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in /* [n_pin] */, double *resid);
 /* TransportSweeper::pin_powers (transport_sweeper.cpp:140-193), [ny][nx] */
 int mocgpu_pin_powers(mocgpu_sweeper *s, double *out);
-/* CoarseData current and surface flux after the last current sweep, [G][n_surf] */
+/* CoarseData current and surface flux after the last current sweep, [G][n_surf].
+ * mocgpu_sweep tallies both, as MOCC's current worker does; the sweeps inside
+ * mocgpu_eigen_solve tally surface fluxes only when the incoming_update
+ * option reads them (CMFD itself reads the net currents), so after an eigen
+ * solve without it the surface fluxes are those of the last mocgpu_sweep. */
 int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux);
 /* BoundaryCondition::get_boundary (src/core/boundary_condition.hpp:144-164):
  * the incoming angular flux entries of one group, every angle of octants
@@ -216,7 +220,8 @@ int mocgpu_update_incoming_flux(mocgpu_sweeper *s, const double *part, const dou
  * refused call queues no work and leaves the handle unchanged. */
 int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k);
 /* EigenSolver::solve (eigen_solver.cpp:131-223): the whole power iteration.
- * max_outer < 0 uses <solver max_iter>. */
+ * max_outer < 0 uses <solver max_iter>. Its sweeps tally net currents only,
+ * unless the incoming_update option needs the surface fluxes. */
 int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
 /* device bytes held by the handle; algorithmic bytes of one group sweep */
 int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
