@@ -108,6 +108,17 @@ int mocgpu_device_count(int *n);
 int mocgpu_problem_create(const char *xml_text, const char *xsl_text, const char *base_dir, mocgpu_problem **out);
 void mocgpu_problem_destroy(mocgpu_problem *p);
 int mocgpu_problem_sizes(const mocgpu_problem *p, int64_t *sizes /* [MOCGPU_SZ_COUNT] */);
+/* What AngularQuadrature::output writes (src/core/angular_quadrature.cpp:
+ * 213-248) for the traced (modularised) quadrature: polar and azimuthal
+ * angles per octant, and per angle of all 8 octants alpha, theta, omega_x,
+ * omega_y, omega_z, weight (out: [ndir][6]; min(cap, ndir) angles written,
+ * ndir reported). */
+int mocgpu_problem_quadrature(const mocgpu_problem *p, int *n_polar, int *n_azimuthal, double *out, int64_t cap,
+                              int64_t *ndir);
+/* The cross-section library's group upper energy bounds (MaterialLib::
+ * g_bounds, src/core/material_lib.cpp:80-90; written as eubounds by
+ * FixedSourceSolver::output, src/solvers/fixed_source_solver.cpp:119-129). */
+int mocgpu_problem_group_bounds(const mocgpu_problem *p, double *out, int cap, int *n);
 int mocgpu_problem_options(const mocgpu_problem *p, mocgpu_options *out);
 int mocgpu_problem_set_options(mocgpu_problem *p, const mocgpu_options *in);
 /* Copies a named flat array (see FlatProblem: "seg_len", "seg_fsr", ...)
@@ -223,6 +234,11 @@ int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k);
  * max_outer < 0 uses <solver max_iter>. Its sweeps tally net currents only,
  * unless the incoming_update option needs the surface fluxes. */
 int mocgpu_eigen_solve(mocgpu_sweeper *s, int max_outer, mocgpu_result *out);
+/* The last mocgpu_eigen_solve's outer iterations (EigenSolver's
+ * convergence_ and iteration_times_, src/solvers/eigen_solver.cpp:185-190):
+ * out [n][4] = k, error_k, error_psi, seconds since the solve began;
+ * min(cap, n) rows written, n reported. */
+int mocgpu_eigen_history(mocgpu_sweeper *s, double *out, int64_t cap, int64_t *n);
 /* device bytes held by the handle; algorithmic bytes of one group sweep */
 int mocgpu_sweeper_bytes(mocgpu_sweeper *s, int64_t *device_bytes, double *sweep_bytes);
 

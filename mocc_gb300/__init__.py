@@ -96,6 +96,9 @@ def load_library(build: bool = True):
         "mocgpu_problem_create": (I, [CP, CP, CP, C.POINTER(P)]),
         "mocgpu_problem_destroy": (None, [P]),
         "mocgpu_problem_sizes": (I, [P, I64P]),
+        "mocgpu_problem_quadrature": (I, [P, IP, IP, DP, C.c_int64, I64P]),
+        "mocgpu_problem_group_bounds": (I, [P, DP, I, IP]),
+        "mocgpu_eigen_history": (I, [P, DP, C.c_int64, I64P]),
         "mocgpu_problem_options": (I, [P, C.POINTER(_Options)]),
         "mocgpu_problem_set_options": (I, [P, C.POINTER(_Options)]),
         "mocgpu_problem_export": (I, [P, CP, VP, C.c_int64]),
@@ -221,6 +224,28 @@ class Problem:
     @property
     def handle(self):
         return self._h
+
+    def quadrature(self) -> dict:
+        """The traced (modularised) angular quadrature: n_polar and
+        n_azimuthal per octant, and alpha, theta, omega_x/y/z and weight of
+        every angle of all 8 octants (what AngularQuadrature::output writes)."""
+        npol, nazi, nd = C.c_int(), C.c_int(), C.c_int64()
+        _check(self._lib.mocgpu_problem_quadrature(self._h, C.byref(npol), C.byref(nazi), None, 0, C.byref(nd)))
+        a = np.empty((nd.value, 6))
+        _check(self._lib.mocgpu_problem_quadrature(self._h, C.byref(npol), C.byref(nazi), _dp(a), nd.value,
+                                                   C.byref(nd)))
+        out = {"n_polar": npol.value, "n_azimuthal": nazi.value}
+        for j, key in enumerate(("alpha", "theta", "omega_x", "omega_y", "omega_z", "weight")):
+            out[key] = a[:, j].copy()
+        return out
+
+    def group_bounds(self) -> np.ndarray:
+        """Upper energy bounds of the cross-section library's groups."""
+        n = C.c_int()
+        _check(self._lib.mocgpu_problem_group_bounds(self._h, None, 0, C.byref(n)))
+        out = np.empty(n.value)
+        _check(self._lib.mocgpu_problem_group_bounds(self._h, _dp(out), n.value, C.byref(n)))
+        return out
 
     def export(self, field: str) -> np.ndarray:
         n = C.c_int64(0)
@@ -479,6 +504,21 @@ class EigenSolver:
 
     def pin_powers(self) -> np.ndarray:
         return self.sweeper.pin_powers()
+
+    def history(self) -> np.ndarray:
+        """The last solve's outer iterations, [n][4]: k, error_k, error_psi,
+        seconds since the solve began."""
+        lib, h, n = self.sweeper._lib, self.sweeper.handle, C.c_int64()
+        _check(lib.mocgpu_eigen_history(h, None, 0, C.byref(n)))
+        out = np.empty((n.value, 4))
+        _check(lib.mocgpu_eigen_history(h, _dp(out), n.value, C.byref(n)))
+        return out
+
+    def output(self, dump_fsr_flux: bool = False) -> dict:
+        """The datasets MOCC's EigenSolver::output writes after this solve,
+        {HDF5 path: array} (``mocc_gb300.output``)."""
+        from .output import eigen_output
+        return eigen_output(self, dump_fsr_flux=dump_fsr_flux)
 
 
 class BatchEngine:

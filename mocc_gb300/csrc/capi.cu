@@ -187,6 +187,31 @@ int mocgpu_problem_create(const char *xml_text, const char *xsl_text, const char
 
 void mocgpu_problem_destroy(mocgpu_problem *p) { delete p; }
 
+int mocgpu_problem_quadrature(const mocgpu_problem *p, int *n_polar, int *n_azimuthal, double *out, int64_t cap,
+                              int64_t *ndir)
+{
+    return guarded([&] {
+        REQUIRE(p && n_polar && n_azimuthal && ndir && cap >= 0 && (out || cap == 0), "null argument");
+        const mocgpu::AngularQuadrature &q = p->P->rays->quad;
+        *n_polar = q.n_polar;
+        *n_azimuthal = q.n_azimuthal;
+        *ndir = q.ndir();
+        for (int i = 0; i < q.ndir() && i < cap; i++) {
+            const mocgpu::Angle &a = q[i];
+            const double v[6] = {a.alpha, a.theta, a.ox, a.oy, a.oz, a.weight};
+            std::copy(v, v + 6, out + (size_t)6 * i);
+        }
+    });
+}
+int mocgpu_problem_group_bounds(const mocgpu_problem *p, double *out, int cap, int *n)
+{
+    return guarded([&] {
+        REQUIRE(p && n && cap >= 0 && (out || cap == 0), "null argument");
+        const std::vector<double> &b = p->P->mesh->mat_lib.group_bounds;
+        *n = (int)b.size();
+        std::copy(b.begin(), b.begin() + std::min<size_t>((size_t)cap, b.size()), out);
+    });
+}
 int mocgpu_problem_sizes(const mocgpu_problem *p, int64_t *s)
 {
     return guarded([&] {
@@ -438,6 +463,16 @@ int mocgpu_set_flux(mocgpu_sweeper *s, const double *flux)
     return guarded([&] {
         REQUIRE(flux, "null argument");
         sw(s).set_flux(flux);
+    });
+}
+int mocgpu_eigen_history(mocgpu_sweeper *s, double *out, int64_t cap, int64_t *n)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(n && cap >= 0 && (out || cap == 0), "bad argument");
+        const std::vector<double> &h = S.history();
+        *n = (int64_t)h.size() / 4;
+        std::copy(h.begin(), h.begin() + std::min<int64_t>(4 * cap, (int64_t)h.size()), out);
     });
 }
 int mocgpu_get_boundary_flux(mocgpu_sweeper *s, int group, double *out, int64_t cap, int64_t *n)

@@ -593,6 +593,7 @@ EigenResult Sweeper::eigen_solve(int max_outer)
     } restore{tally_sflux_, tally_sflux_};
     tally_sflux_ = opts_.incoming_update != 0;
     initialize();
+    history_.clear();
     double k = 1.0, k_prev = 1.0;
     calc_fission_source(k);
     int max_it = (max_outer >= 0) ? max_outer : opts_.max_iter;
@@ -601,6 +602,9 @@ EigenResult Sweeper::eigen_solve(int max_outer)
         res.error_k = std::fabs(k - k_prev);
         res.error_psi = psi_error();
         res.iterations = it + 1;
+        history_.insert(history_.end(),
+                        {k, res.error_k, res.error_psi,
+                         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count()});
         if (!std::isfinite(k)) MOCGPU_THROW(12, "Eigenvalue is not a number. Giving up.");
         if (res.error_k < opts_.k_tol && res.error_psi < opts_.psi_tol && it >= opts_.min_iter) {
             res.converged = 1;

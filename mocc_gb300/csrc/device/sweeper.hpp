@@ -84,6 +84,10 @@ class Sweeper {
     // elsewhere (2 (J+ + J-) per [G][n_surf], this and the previous CMFD solve)
     void update_incoming_flux(const double *part, const double *part_old, int has_old, int mode);
     EigenResult eigen_solve(int max_outer = -1);
+    // the last eigen_solve's outer iterations, 4 values each: k, error_k,
+    // error_psi, seconds since the solve began (EigenSolver's convergence_
+    // and iteration_times_, eigen_solver.cpp:185-190)
+    const std::vector<double> &history() const { return history_; }
     void eigen_step(double &k, double &k_prev);
     double psi_error();
 
@@ -127,6 +131,7 @@ class Sweeper {
     // MOCC's current worker does); the library's own eigenvalue iteration
     // clears it unless the incoming-flux update reads them
     bool tally_sflux_ = true;
+    std::vector<double> history_;
     bool has_radial_ = false;
     int n_fissile_ = 0;
     int cmfd_solves_ = 0; // CMFD solves since initialize (the first has no previous partial currents)

@@ -94,6 +94,7 @@ def load():
             ("orc_update_incoming", I, [V, DP, DP, I, I]),
             ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
             ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
+            ("orc_history", I, [V, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]),
             ("orc_table_exp", D, [D]),
             ("orc_trace_error", C.c_char_p, []), ("orc_trace", I, [C.c_char_p, C.c_char_p, I, C.POINTER(V)]),
             ("orc_traced_destroy", None, [V]), ("orc_traced_problem", C.POINTER(_P), [V]),
@@ -307,3 +308,58 @@ class OracleSolver:
         r = _R()
         _chk(self._lib.orc_eigen_solve(self._h, max_outer, C.byref(r)))
         return {f: getattr(r, f) for f, _ in _R._fields_}
+
+    def history(self) -> np.ndarray:
+        """The last solve's outer iterations, [n][4]: k, error_k, error_psi,
+        seconds since the solve began."""
+        d, n = C.POINTER(C.c_double)(), C.c_int64()
+        _chk(self._lib.orc_history(self._h, C.byref(d), C.byref(n)))
+        if n.value == 0:
+            return np.zeros((0, 4))
+        return np.ctypeslib.as_array(d, shape=(n.value, 4)).copy()
+
+    def output(self) -> dict:
+        """The datasets MOCC's EigenSolver::output writes after a solve (see
+        mocc_output), from this solver's own trace."""
+        if not hasattr(self, "_traced"):
+            raise ValueError("output needs a solver built from input text (from_xml)")
+        return mocc_output(self._traced, self)
+
+
+def mocc_output(traced: Traced, solver: OracleSolver) -> dict:
+    """Restatement of what MOCC writes to its HDF5 output after an eigenvalue
+    solve, as {dataset path: array}:
+
+    * ``EigenSolver::output`` (eigen_solver.cpp:293-322): convergence/k,
+      error_k, error_psi per outer iteration, iteration_time and abscissae
+      (both the iteration times);
+    * ``FixedSourceSolver::output`` (fixed_source_solver.cpp:119-129): ng and
+      eubounds (the library's group bounds);
+    * ``MoCSweeper::output`` (moc_sweeper.cpp:533-585): flux/001.. of the pin
+      flux (``get_pin_flux``), the whole [pin][group] array scaled by
+      ``Normalize`` (utils.hpp:29-52: to sum to its count of positive
+      entries), each group shaped (nz, ny, nx); pin_powers (nz, ny, nx);
+    * ``AngularQuadrature::output`` (angular_quadrature.cpp:213-248):
+      ang_quad/n_polar, n_azimuthal and every angle's alpha, theta,
+      omega_x/y/z and weight."""
+    h = solver.history()
+    G, ny, nx = solver.n_group, solver.ny, solver.nx
+    flux = np.stack([solver.get_pin_flux_1g(g) for g in range(G)], axis=1)  # [pin][g]
+    n_pos = int(np.count_nonzero(flux > 0.0))
+    flux = flux * (n_pos / flux.sum())
+    out = {
+        "convergence/k": h[:, 0].copy(), "convergence/error_k": h[:, 1].copy(),
+        "convergence/error_psi": h[:, 2].copy(), "convergence/iteration_time": h[:, 3].copy(),
+        "convergence/abscissae": h[:, 3].copy(),
+        "ng": np.array(G, dtype=np.int32), "eubounds": traced.array("group_bounds"),
+    }
+    for g in range(G):
+        out[f"flux/{g + 1:03d}"] = flux[:, g].reshape(1, ny, nx).copy()
+    out["pin_powers"] = solver.pin_powers().reshape(1, ny, nx)
+    npol, nazi = (int(v) for v in traced.array("quad_n"))
+    out["ang_quad/n_polar"] = np.array(npol, dtype=np.int32)
+    out["ang_quad/n_azimuthal"] = np.array(nazi, dtype=np.int32)
+    for key, name in (("alpha", "quad_alpha"), ("theta", "quad_theta"), ("omega_x", "quad_ox"),
+                      ("omega_y", "quad_oy"), ("omega_z", "quad_oz"), ("weight", "quad_weight")):
+        out["ang_quad/" + key] = traced.array(name)
+    return out

@@ -76,6 +76,7 @@ struct orc_solver {
     int n_cmfd_solve = 0;
     std::vector<double> mdiag, mW, mE, mS, mN;          // [G][n_cell]
     int64_t sweeps = 0, cmfd_its = 0;
+    std::vector<double> history; // per outer iteration of eigen_solve: k, error_k, error_psi, seconds
     int n_fissile = 0;
 
     // ---- indexing helpers (mesh.hpp / mesh.cpp) ----
@@ -873,6 +874,7 @@ struct orc_solver {
         orc_result res{};
         coarse = o.cmfd && o.cmfd_enabled;
         initialize();
+        history.clear();
         double k = 1.0, k_prev = 1.0;
         calc_fission_source(k);
         int max_it = max_outer >= 0 ? max_outer : o.max_iter;
@@ -898,6 +900,10 @@ struct orc_solver {
             for (int r = 0; r < nreg; r++) e += (a[r] - b[r]) * (a[r] - b[r]);
             res.error_psi = std::sqrt(e / n_fissile);
             res.iterations = it + 1;
+            // EigenSolver::solve's convergence_ and iteration_times_
+            // (eigen_solver.cpp:185-190), the time since the solve began
+            history.insert(history.end(), {k, res.error_k, res.error_psi,
+                                           std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count()});
             if (k != k) throw std::runtime_error("Eigenvalue is not a number. Giving up.");
             if (res.error_k < o.k_tol && res.error_psi < o.psi_tol && it >= o.min_iter) {
                 res.converged = 1;
@@ -1108,6 +1114,12 @@ int orc_cmfd_solve(orc_solver *s, double *k)
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out)
 {
     return guard([&] { *out = s->eigen_solve(max_outer); });
+}
+int orc_history(orc_solver *s, const double **data, int64_t *n)
+{
+    *data = s->history.data();
+    *n = (int64_t)s->history.size() / 4;
+    return 0;
 }
 double orc_table_exp(double x) { return table().exp(x); }
 }

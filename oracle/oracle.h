@@ -116,6 +116,10 @@ int orc_homogenized_nu_fission(orc_solver *s, double *out);
 int orc_cmfd_system(orc_solver *s, double *op, double *xsnf, double *xsch, double *scat, double *vol);
 int orc_cmfd_solve(orc_solver *s, double *k);
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out);
+/* the last eigen_solve's outer iterations: [n][4] = k, error_k, error_psi,
+ * seconds since the solve began (EigenSolver's convergence_ and
+ * iteration_times_, eigen_solver.cpp:185-190) */
+int orc_history(orc_solver *s, const double **data, int64_t *n);
 /* exponential table check: value of MOCC's table exponential at x */
 double orc_table_exp(double x);
 

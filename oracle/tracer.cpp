@@ -566,6 +566,7 @@ struct Material {
 };
 struct Library {
     int ng = 0;
+    vector<double> bounds; // group upper energy bounds (material_lib.cpp:80-90)
     vector<Material> mats;
     std::map<string, int> by_name;
 };
@@ -595,7 +596,14 @@ Library read_xsl(const string &text)
         std::istringstream in(next());
         if (!(in >> lib.ng >> nmat)) throw Fail("Failed to read number of groups!");
     }
-    next(); // group bounds
+    {
+        std::istringstream in(next());
+        for (int g = 0; g < lib.ng; g++) {
+            double v;
+            if (!(in >> v)) throw Fail("Trouble reading group bounds!");
+            lib.bounds.push_back(v);
+        }
+    }
     const int G = lib.ng;
     for (int m = 0; m < nmat; m++) {
         std::istringstream head(next());
@@ -1579,6 +1587,19 @@ std::unique_ptr<orc_traced> trace_problem(const std::string &xml, const std::str
         D["ang_weight"].push_back(a.w);
         D["ang_rsintheta"].push_back(a.rsin);
     }
+    // every angle of the (modularised) quadrature, 8 octants, and the group
+    // bounds: what AngularQuadrature::output and FixedSourceSolver::output
+    // write (angular_quadrature.cpp:213-248, fixed_source_solver.cpp:119-129)
+    for (const Ang &a : Q.ang) {
+        D["quad_alpha"].push_back(a.alpha);
+        D["quad_theta"].push_back(a.theta);
+        D["quad_ox"].push_back(a.ox);
+        D["quad_oy"].push_back(a.oy);
+        D["quad_oz"].push_back(a.oz);
+        D["quad_weight"].push_back(a.w);
+    }
+    I["quad_n"] = {Q.n_pol, Q.n_azi};
+    D["group_bounds"] = B.lib.bounds;
     I["set_nx"] = snx;
     I["set_ny"] = sny;
     D["set_spacing"] = ssp;
