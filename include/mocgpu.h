@@ -34,6 +34,7 @@ extern "C" {
 #define MOCGPU_ERR_NAN 12           /* eigenvalue became NaN */
 #define MOCGPU_ERR_NOT_CONVERGED 13 /* iteration limit reached (result still valid) */
 #define MOCGPU_ERR_CANCELLED 14     /* batched solve cancelled by the caller */
+#define MOCGPU_ERR_NEGATIVE_FLUX 15 /* negative scalar flux met by transverse-leakage splitting */
 #define MOCGPU_ERR_CUDA 20          /* CUDA runtime error (out of memory included) */
 #define MOCGPU_ERR_CAPACITY 21      /* over a memory budget or a fixed scratch size */
 #define MOCGPU_ERR_INTERNAL 99
@@ -83,6 +84,10 @@ typedef struct mocgpu_options {
      * faces left at zero. XML: <sweeper incoming_update="off|mocc|surface">.
      * Every solve of one batch engine must ask for the same value. */
     int incoming_update;
+    /* MoCSweeper's allow_splitting_ (<sweeper tl_splitting>,
+     * src/sweepers/moc/moc_sweeper.cpp:119): see
+     * mocgpu_apply_transverse_leakage. Off by default. */
+    int tl_splitting;
 } mocgpu_options;
 
 typedef struct mocgpu_result {
@@ -181,10 +186,10 @@ int mocgpu_set_pin_flux_1g(mocgpu_sweeper *s, int group, const double *in /* [n_
 /* TransportSweeper::pin_powers (transport_sweeper.cpp:140-193), [ny][nx] */
 int mocgpu_pin_powers(mocgpu_sweeper *s, double *out);
 /* CoarseData current and surface flux after the last current sweep, [G][n_surf].
- * mocgpu_sweep tallies both, as MOCC's current worker does; the sweeps inside
+ * mocgpu_sweep_group tallies both, as MOCC's current worker does; the sweeps inside
  * mocgpu_eigen_solve tally surface fluxes only when the incoming_update
  * option reads them (CMFD itself reads the net currents), so after an eigen
- * solve without it the surface fluxes are those of the last mocgpu_sweep. */
+ * solve without it the surface fluxes are those of the last mocgpu_sweep_group. */
 int mocgpu_get_coarse_currents(mocgpu_sweeper *s, double *current, double *surface_flux);
 /* BoundaryCondition::get_boundary (src/core/boundary_condition.hpp:144-164):
  * the incoming angular flux entries of one group, every angle of octants
@@ -216,6 +221,16 @@ int mocgpu_cmfd_solve(mocgpu_sweeper *s, double *k);
  * faces at zero. For a MOCC build that keeps its CPU CMFD and calls the
  * sweeper's update_incoming_flux. */
 int mocgpu_update_incoming_flux(mocgpu_sweeper *s, const double *part, const double *part_old, int has_old, int mode);
+/* MoCSweeper::apply_transverse_leakage (src/sweepers/moc/moc_sweeper.cpp:
+ * 435-472), the hook through which MOCC's 2-D/3-D sweeper feeds the axial
+ * transverse leakage tl [n_fsr] of one group into the MoC source. Call it
+ * after the group's source is built and before mocgpu_sweep_group: tl is
+ * added to the group source; with the tl_splitting option, an FSR whose sum
+ * would be negative gets a zero source and Sigma_t raised by -sum / phi
+ * (phi its scalar flux of the group) for the sweeps that follow, the split
+ * staying until the next call (a negative phi there fails with
+ * MOCGPU_ERR_NEGATIVE_FLUX, as MOCC's "Negative flux when splitting"). */
+int mocgpu_apply_transverse_leakage(mocgpu_sweeper *s, int group, const double *tl);
 /* mocgpu_cmfd_solve without allocation (no MOCC counterpart). The CMFD work
  * vectors live in a fixed array inside the library (10 x 8192 doubles, 640
  * KiB per device) instead of a buffer of the handle, so no call allocates

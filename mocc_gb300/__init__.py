@@ -44,7 +44,7 @@ class _Options(C.Structure):
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
                 ("precision", C.c_int), ("sweep_kernel", C.c_int), ("bundles_per_unit", C.c_int),
-                ("window_rows", C.c_int), ("incoming_update", C.c_int)]
+                ("window_rows", C.c_int), ("incoming_update", C.c_int), ("tl_splitting", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -99,6 +99,7 @@ def load_library(build: bool = True):
         "mocgpu_problem_quadrature": (I, [P, IP, IP, DP, C.c_int64, I64P]),
         "mocgpu_problem_group_bounds": (I, [P, DP, I, IP]),
         "mocgpu_eigen_history": (I, [P, DP, C.c_int64, I64P]),
+        "mocgpu_apply_transverse_leakage": (I, [P, I, DP]),
         "mocgpu_problem_options": (I, [P, C.POINTER(_Options)]),
         "mocgpu_problem_set_options": (I, [P, C.POINTER(_Options)]),
         "mocgpu_problem_export": (I, [P, CP, VP, C.c_int64]),
@@ -390,6 +391,13 @@ class MoCSweeper:
         old = None if part_old is None else np.ascontiguousarray(part_old, dtype=np.float64)
         _check(self._lib.mocgpu_update_incoming_flux(self._h, _dp(part), None if old is None else _dp(old),
                                                      0 if old is None else 1, mode))
+
+    def apply_transverse_leakage(self, g: int, tl: np.ndarray):
+        """MoCSweeper::apply_transverse_leakage: adds tl [n_fsr] to group g's
+        source (after source_group(g)), split into Sigma_t where negative
+        when the tl_splitting option is on."""
+        tl = np.ascontiguousarray(tl, dtype=np.float64).reshape(self.n_reg)
+        _check(self._lib.mocgpu_apply_transverse_leakage(self._h, g, _dp(tl)))
 
     def layout(self) -> dict:
         """Bundled sweep layout of this handle's geometry."""

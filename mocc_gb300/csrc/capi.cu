@@ -129,6 +129,7 @@ void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
     c->bundles_per_unit = o.bundles_per_unit;
     c->window_rows = o.window_rows;
     c->incoming_update = o.incoming_update;
+    c->tl_splitting = o.tl_splitting ? 1 : 0;
 }
 void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
 {
@@ -157,6 +158,7 @@ void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
     o.window_rows = c->window_rows;
     REQUIRE(c->incoming_update >= 0 && c->incoming_update <= 2, "incoming_update must be 0, 1 or 2");
     o.incoming_update = c->incoming_update;
+    o.tl_splitting = c->tl_splitting != 0;
 }
 } // namespace
 
@@ -534,6 +536,14 @@ int mocgpu_update_incoming_flux(mocgpu_sweeper *s, const double *part, const dou
         REQUIRE(part && (part_old || !has_old), "null argument");
         REQUIRE(mode == 1 || mode == 2, "mode must be 1 (MOCC's lookup) or 2 (entry surface)");
         sw(s).update_incoming_flux(part, part_old, has_old, mode);
+    });
+}
+int mocgpu_apply_transverse_leakage(mocgpu_sweeper *s, int group, const double *tl)
+{
+    return guarded([&] {
+        auto &S = sw(s);
+        REQUIRE(tl && group >= 0 && group < S.flat().ng, "bad argument");
+        S.apply_transverse_leakage(group, tl);
     });
 }
 int mocgpu_cmfd_solve_static(mocgpu_sweeper *s, double *k)

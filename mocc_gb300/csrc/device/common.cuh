@@ -25,6 +25,7 @@ enum DeviceStatus : unsigned {
     DEV_NAN = 1u << 1,
     DEV_BAD_INDEX = 1u << 2,
     DEV_CMFD_NOT_CONVERGED = 1u << 3,
+    DEV_NEGATIVE_SPLIT_FLUX = 1u << 4, // transverse-leakage splitting met a negative scalar flux
 };
 
 // Host<->device bytes moved by the library (reported by the C ABI).

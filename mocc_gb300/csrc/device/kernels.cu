@@ -147,8 +147,43 @@ template <typename Real> __global__ void k_group_source(GeomView g, StateView st
     double xt = g.xstr[(size_t)m * G + group];
     double q = (src + st.phi[(size_t)group * g.n_fsr + r] * srow[group]) * (1.0 / (xt * kFpi));
     ((Real *)st.qbar)[r] = (Real)q;
-    ((Real *)st.sigt)[r] = (Real)xt;
+    // the sweep's Sigma_t: XSMesh::expand with the split (xs_mesh.hpp:282-296);
+    // the self-scatter source keeps the material's (source_isotropic.cpp:21-57)
+    ((Real *)st.sigt)[r] = (Real)(st.split ? xt + st.split[r] : xt);
 }
+
+template <typename Real> __global__ void k_apply_tl(GeomView g, StateView st, int group, const double *tl)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.n_fsr) return;
+    const int G = g.G, m = g.fsr_mat[r];
+    const double ph = st.phi[(size_t)group * g.n_fsr + r];
+    double s = st.src1g[r] + tl[r];
+    if (st.split) {
+        double sp = 0.0;
+        if (s < 0.0) {
+            if (ph < 0.0) atomicOr(st.status, (unsigned)DEV_NEGATIVE_SPLIT_FLUX);
+            sp = -s / ph;
+            s = 0.0;
+        }
+        st.split[r] = sp;
+    }
+    st.src1g[r] = s;
+    const double xt = g.xstr[(size_t)m * G + group];
+    const double sgg = g.scat[((size_t)m * G + group) * G + group];
+    ((Real *)st.qbar)[r] = (Real)((s + ph * sgg) * (1.0 / (xt * kFpi)));
+    ((Real *)st.sigt)[r] = (Real)(st.split ? xt + st.split[r] : xt);
+}
+template <typename Real>
+void launch_apply_transverse_leakage(const GeomView &g, const StateView &st, int group, const double *tl,
+                                     cudaStream_t s)
+{
+    { note_launch(); k_apply_tl<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group, tl); }
+}
+template void launch_apply_transverse_leakage<float>(const GeomView &, const StateView &, int, const double *,
+                                                     cudaStream_t);
+template void launch_apply_transverse_leakage<double>(const GeomView &, const StateView &, int, const double *,
+                                                      cudaStream_t);
 template <typename Real> void launch_group_source(const GeomView &g, const StateView &st, int group, cudaStream_t s)
 {
     { note_launch(); k_group_source<Real><<<(g.n_fsr + 255) / 256, 256, 0, s>>>(g, st, group); }

@@ -76,6 +76,9 @@ struct StateView {
     // normalisation and cleared
     float *cur32, *sfl32;
     double *part;              // [2][G][n_surf]: 2 (J+ + J-) of the last CMFD solve and the one before
+    // [n_fsr]: Sigma_t added by transverse-leakage splitting (MoCSweeper::
+    // split_), nullptr when <sweeper tl_splitting> is off
+    double *split;
     double *cflux;             // coarse (pin) flux [G][n_pin]
     double *red;               // per-solve scalars and reduction scratch (64 doubles)
     unsigned *status;
@@ -198,6 +201,13 @@ void launch_b_cmfd(const BatchViews &b, cudaStream_t s);
 // MoCSweeper::update_incoming_flux after each solve's CMFD (mode 1 or 2 as
 // for launch_incoming_update); counts the CMFD solves of each solve.
 void launch_b_incoming_update(const BatchViews &b, int precision, int mode, cudaStream_t s);
+// MoCSweeper::apply_transverse_leakage (moc_sweeper.cpp:435-472): adds the
+// transverse leakage tl [n_fsr] to the group source, with splitting when
+// st.split is set; then the group's qbar and Sigma_t as the next sweep uses
+// them.
+template <typename Real>
+void launch_apply_transverse_leakage(const GeomView &g, const StateView &st, int group, const double *tl,
+                                     cudaStream_t s);
 // pin powers of every active solve: out[slot * stride + cell], total at n_pin
 void launch_b_pin_powers(const BatchViews &b, double *out, int stride, cudaStream_t s);
 // Batched sweep (Gauss-Seidel boundary update) in streaming shape `shape`:

@@ -89,6 +89,10 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     shat_.alloc((size_t)G * f.n_surf);
     part_.alloc((size_t)2 * G * f.n_surf);
     part_.zero(stream_);
+    if (P.opts.tl_splitting) {
+        split_.alloc(f.n_fsr);
+        split_.zero(stream_);
+    }
     cmat_.alloc((size_t)G * 6 * nc);
     cfs_.alloc(nc);
     cfs_old_.alloc(nc);
@@ -121,6 +125,7 @@ Sweeper::Sweeper(const Problem &P, int precision, cudaStream_t stream, std::shar
     s.cur32 = cur32_.p;
     s.sfl32 = cur32_.p + (size_t)kCurCopies * f.n_surf;
     s.part = part_.p;
+    s.split = P.opts.tl_splitting ? split_.p : nullptr;
     s.cflux = cflux_.p;
     s.red = red_.p;
     s.status = status_.p;
@@ -235,6 +240,25 @@ void Sweeper::check_status()
         status_.zero(stream_);
         MOCGPU_THROW(12, "Eigenvalue is not a number. Giving up.");
     }
+    if (st & DEV_NEGATIVE_SPLIT_FLUX) {
+        status_.zero(stream_);
+        MOCGPU_THROW(15, "Negative flux when splitting");
+    }
+}
+
+void Sweeper::apply_transverse_leakage(int g, const double *tl)
+{
+    // the option may have been switched on since the handle was made
+    if (opts_.tl_splitting && !split_.p) {
+        split_.alloc(f_.n_fsr);
+        split_.zero(stream_);
+    }
+    sv_.split = opts_.tl_splitting ? split_.p : nullptr;
+    if (!tl_.p) tl_.alloc(f_.n_fsr);
+    MOCGPU_CUDA(copy_async(tl_.p, tl, sizeof(double) * f_.n_fsr, cudaMemcpyHostToDevice, stream_));
+    if (precision_ == 0) launch_apply_transverse_leakage<double>(gv_, sv_, g, tl_.p, stream_);
+    else launch_apply_transverse_leakage<float>(gv_, sv_, g, tl_.p, stream_);
+    check_status();
 }
 
 // MoCSweeper::initialize (moc_sweeper.cpp:234-253): phi = 1, psi = 1/4pi on

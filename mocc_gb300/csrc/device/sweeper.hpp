@@ -83,6 +83,10 @@ class Sweeper {
     // MoCSweeper::update_incoming_flux from partial-current sums computed
     // elsewhere (2 (J+ + J-) per [G][n_surf], this and the previous CMFD solve)
     void update_incoming_flux(const double *part, const double *part_old, int has_old, int mode);
+    // MoCSweeper::apply_transverse_leakage (moc_sweeper.cpp:435-472), after
+    // group_source(g): tl [n_fsr] (host) added to the group source, split
+    // into Sigma_t where the sum goes negative when <sweeper tl_splitting>
+    void apply_transverse_leakage(int g, const double *tl);
     EigenResult eigen_solve(int max_outer = -1);
     // the last eigen_solve's outer iterations, 4 values each: k, error_k,
     // error_psi, seconds since the solve began (EigenSolver's convergence_
@@ -147,6 +151,7 @@ class Sweeper {
     // CMFD
     DevBuf<double> cflux_, hxs_, hscat_, dtil_, dhat_, stil_, shat_, cmat_, cfs_, cfs_old_, cvec_, cstats_;
     DevBuf<double> part_; // [2][G][n_surf]: 2 (J+ + J-) of the last CMFD solve, then of the one before
+    DevBuf<double> split_, tl_; // [n_fsr]: split Sigma_t (zero until a leakage is applied), leakage staging
     DevBuf<double> pinbuf_;
 
     GeomView gv_{};

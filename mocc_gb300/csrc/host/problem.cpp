@@ -71,6 +71,7 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
         if (o.window_rows < -1 || (o.window_rows > 0 && o.window_rows % 16 != 0))
             MOCGPU_THROW(7, "window_rows must be -1 (automatic), 0 or a positive multiple of 16.");
     }
+    o.tl_splitting = sweeper->attr_bool("tl_splitting", false);
     if (sweeper->has_attr("incoming_update")) {
         std::string u = sanitize(sweeper->attr("incoming_update"));
         if (u == "off") o.incoming_update = 0;

@@ -36,6 +36,10 @@ struct SolverOptions {
     // is disabled), 1 as MOCC's code reads the partial currents, 2 from the
     // partial currents of each track's entry surface
     int incoming_update = 0;
+    // MoCSweeper's allow_splitting_ (<sweeper tl_splitting>, moc_sweeper.cpp:
+    // 119): a transverse-leakage source that would go negative in an FSR is
+    // moved into that FSR's Sigma_t instead (apply_transverse_leakage)
+    bool tl_splitting = false;
 };
 
 // Flat problem description. Angles cover octants 1-4 (2-D); tracks are

@@ -47,7 +47,7 @@ class _O(C.Structure):
                 ("cmfd", C.c_int), ("cmfd_enabled", C.c_int), ("cmfd_k_tol", C.c_double),
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
-                ("precision", C.c_int), ("incoming_update", C.c_int)]
+                ("precision", C.c_int), ("incoming_update", C.c_int), ("tl_splitting", C.c_int)]
 
 
 class _R(C.Structure):
@@ -95,6 +95,7 @@ def load():
             ("orc_cmfd_solve", I, [V, DP]), ("orc_homogenized_nu_fission", I, [V, DP]),
             ("orc_cmfd_system", I, [V, DP, DP, DP, DP, DP]), ("orc_eigen_solve", I, [V, I, C.POINTER(_R)]),
             ("orc_history", I, [V, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]),
+            ("orc_apply_transverse_leakage", I, [V, I, DP]),
             ("orc_table_exp", D, [D]),
             ("orc_trace_error", C.c_char_p, []), ("orc_trace", I, [C.c_char_p, C.c_char_p, I, C.POINTER(V)]),
             ("orc_traced_destroy", None, [V]), ("orc_traced_problem", C.POINTER(_P), [V]),
@@ -308,6 +309,10 @@ class OracleSolver:
         r = _R()
         _chk(self._lib.orc_eigen_solve(self._h, max_outer, C.byref(r)))
         return {f: getattr(r, f) for f, _ in _R._fields_}
+
+    def apply_transverse_leakage(self, g, tl):
+        tl = np.ascontiguousarray(tl, dtype=np.float64)
+        _chk(self._lib.orc_apply_transverse_leakage(self._h, g, _dp(tl)))
 
     def history(self) -> np.ndarray:
         """The last solve's outer iterations, [n][4]: k, error_k, error_psi,

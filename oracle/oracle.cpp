@@ -77,6 +77,7 @@ struct orc_solver {
     std::vector<double> mdiag, mW, mE, mS, mN;          // [G][n_cell]
     int64_t sweeps = 0, cmfd_its = 0;
     std::vector<double> history; // per outer iteration of eigen_solve: k, error_k, error_psi, seconds
+    std::vector<double> split;   // MoCSweeper::split_ (with tl_splitting; zero until a leakage is applied)
     int n_fissile = 0;
 
     // ---- indexing helpers (mesh.hpp / mesh.cpp) ----
@@ -200,6 +201,7 @@ struct orc_solver {
         src.assign(nreg, 0.0);
         q.assign(nreg, 0.0);
         xstr_exp.assign(nreg, 0.0);
+        if (o.tl_splitting) split.assign(nreg, 0.0);
         bc_in.assign((size_t)G * bcpg, 0.0);
         bc_out.assign(bcpg, 0.0);
         current.assign((size_t)nsurf * G, 0.0);
@@ -275,6 +277,26 @@ struct orc_solver {
             for (int gg = 0; gg < G; gg++)
                 if (gg != g) s += sc(r, g, gg) * flux[(size_t)r * G + gg];
             src[r] = s;
+        }
+    }
+    // MoCSweeper::apply_transverse_leakage (moc_sweeper.cpp:435-472)
+    void apply_transverse_leakage(int g, const double *tl)
+    {
+        if (!split.empty()) {
+            std::fill(split.begin(), split.end(), 0.0);
+            for (int r = 0; r < nreg; r++) {
+                double s = src[r] + tl[r];
+                if (s < 0.0) {
+                    const double f = flux[(size_t)r * G + g];
+                    if (f < 0.0) throw std::runtime_error("Negative flux when splitting");
+                    split[r] = -s / f;
+                    src[r] = 0.0;
+                } else {
+                    src[r] = s;
+                }
+            }
+        } else {
+            for (int r = 0; r < nreg; r++) src[r] += tl[r];
         }
     }
     // SourceIsotropic::self_scatter (source_isotropic.cpp:21-57)
@@ -425,7 +447,8 @@ struct orc_solver {
     // MoCSweeper::sweep (moc_sweeper.cpp:189-225)
     void sweep(int g)
     {
-        for (int r = 0; r < nreg; r++) xstr_exp[r] = xs(p.xstr, r, g);
+        // XSMesh::expand(group, split_) (xs_mesh.hpp:282-296)
+        for (int r = 0; r < nreg; r++) xstr_exp[r] = xs(p.xstr, r, g) + (split.empty() ? 0.0 : split[r]);
         for (int inner = 0; inner < o.n_inner; inner++) {
             self_scatter(g);
             if (inner == o.n_inner - 1 && coarse) {
@@ -1114,6 +1137,10 @@ int orc_cmfd_solve(orc_solver *s, double *k)
 int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out)
 {
     return guard([&] { *out = s->eigen_solve(max_outer); });
+}
+int orc_apply_transverse_leakage(orc_solver *s, int g, const double *tl)
+{
+    return guard([&] { s->apply_transverse_leakage(g, tl); });
 }
 int orc_history(orc_solver *s, const double **data, int64_t *n)
 {

@@ -65,6 +65,7 @@ typedef struct orc_options {
     int cmfd_max_iter, cmfd_negative_fixup;
     int n_inner, gs_boundary, precision;
     int incoming_update; /* 0 off, 1 MoCSweeper::update_incoming_flux as written, 2 entry-surface variant */
+    int tl_splitting;    /* MoCSweeper's allow_splitting_ (<sweeper tl_splitting>) */
 } orc_options;
 
 typedef struct orc_result {
@@ -120,6 +121,8 @@ int orc_eigen_solve(orc_solver *s, int max_outer, orc_result *out);
  * seconds since the solve began (EigenSolver's convergence_ and
  * iteration_times_, eigen_solver.cpp:185-190) */
 int orc_history(orc_solver *s, const double **data, int64_t *n);
+/* MoCSweeper::apply_transverse_leakage (moc_sweeper.cpp:435-472): tl [nreg] */
+int orc_apply_transverse_leakage(orc_solver *s, int g, const double *tl);
 /* exponential table check: value of MOCC's table exponential at x */
 double orc_table_exp(double x);
 

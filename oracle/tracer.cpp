@@ -1384,6 +1384,13 @@ void read_options(const Node &doc, orc_options &o, const Node *&sweeper)
         else if (u == "surface") o.incoming_update = 2;
         else if (u != "off") throw Fail("Unrecognized incoming_update option (off|mocc|surface).");
     }
+    // moc_sweeper.cpp:119: pugixml's as_bool, true when the value starts
+    // with 1, t, T, y or Y
+    o.tl_splitting = 0;
+    if (sweeper->has("tl_splitting")) {
+        const std::string v = sweeper->attr("tl_splitting");
+        o.tl_splitting = (!v.empty() && std::string("1tTyY").find(v[0]) != std::string::npos) ? 1 : 0;
+    }
 }
 
 Quad read_quad(const Node &q)

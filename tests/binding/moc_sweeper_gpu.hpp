@@ -139,6 +139,13 @@ class MoCSweeperGPU : public TransportSweeper {
                                           cd.has_old_partial() ? 1 : 0, 1),
               __LINE__);
     }
+    // MoCSweeper::apply_transverse_leakage (moc_sweeper.cpp:435-472), which
+    // MOCC's 2-D/3-D sweeper calls between building a group's source and
+    // sweeping it; tl is [n_reg], splitting as <sweeper tl_splitting> says
+    void apply_transverse_leakage(int group, const ArrayB1 &tl)
+    {
+        check(mocgpu_apply_transverse_leakage(gpu_, group, tl.data()), __LINE__);
+    }
     // EigenSolver::do_cmfd (eigen_solver.cpp:263-291) in one call: coarse
     // flux, homogenisation, CMFD::solve and the fine-flux rescale on the device
     void cmfd(real_t &k) { check(mocgpu_cmfd_solve(gpu_, &k), __LINE__); }
