@@ -88,6 +88,9 @@ typedef struct mocgpu_options {
      * src/sweepers/moc/moc_sweeper.cpp:119): see
      * mocgpu_apply_transverse_leakage. Off by default. */
     int tl_splitting;
+    /* <sweeper dump_fsr_flux> (src/sweepers/moc/moc_sweeper.cpp:103): the
+     * output datasets include fsr_flux/NNN. Off by default. */
+    int dump_fsr_flux;
 } mocgpu_options;
 
 typedef struct mocgpu_result {

@@ -44,7 +44,8 @@ class _Options(C.Structure):
                 ("cmfd_psi_tol", C.c_double), ("cmfd_resid_reduction", C.c_double), ("cmfd_max_iter", C.c_int),
                 ("cmfd_negative_fixup", C.c_int), ("n_inner", C.c_int), ("gs_boundary", C.c_int),
                 ("precision", C.c_int), ("sweep_kernel", C.c_int), ("bundles_per_unit", C.c_int),
-                ("window_rows", C.c_int), ("incoming_update", C.c_int), ("tl_splitting", C.c_int)]
+                ("window_rows", C.c_int), ("incoming_update", C.c_int), ("tl_splitting", C.c_int),
+                ("dump_fsr_flux", C.c_int)]
 
 
 class _Result(C.Structure):
@@ -522,9 +523,13 @@ class EigenSolver:
         _check(lib.mocgpu_eigen_history(h, _dp(out), n.value, C.byref(n)))
         return out
 
-    def output(self, dump_fsr_flux: bool = False) -> dict:
+    def output(self, dump_fsr_flux: bool | None = None) -> dict:
         """The datasets MOCC's EigenSolver::output writes after this solve,
-        {HDF5 path: array} (``mocc_gb300.output``)."""
+        {HDF5 path: array} (``mocc_gb300.output``); fsr_flux/NNN when
+        ``dump_fsr_flux``, by default when the input's <sweeper
+        dump_fsr_flux> asks for it."""
+        if dump_fsr_flux is None:
+            dump_fsr_flux = bool(self.problem.options["dump_fsr_flux"])
         from .output import eigen_output
         return eigen_output(self, dump_fsr_flux=dump_fsr_flux)
 

@@ -130,6 +130,7 @@ void opts_to_c(const mocgpu::SolverOptions &o, mocgpu_options *c)
     c->window_rows = o.window_rows;
     c->incoming_update = o.incoming_update;
     c->tl_splitting = o.tl_splitting ? 1 : 0;
+    c->dump_fsr_flux = o.dump_fsr_flux ? 1 : 0;
 }
 void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
 {
@@ -159,6 +160,7 @@ void opts_from_c(const mocgpu_options *c, mocgpu::SolverOptions &o)
     REQUIRE(c->incoming_update >= 0 && c->incoming_update <= 2, "incoming_update must be 0, 1 or 2");
     o.incoming_update = c->incoming_update;
     o.tl_splitting = c->tl_splitting != 0;
+    o.dump_fsr_flux = c->dump_fsr_flux != 0;
 }
 } // namespace
 

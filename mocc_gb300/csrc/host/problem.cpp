@@ -72,6 +72,7 @@ static void read_options(const XmlNode &doc, SolverOptions &o, const XmlNode *&s
             MOCGPU_THROW(7, "window_rows must be -1 (automatic), 0 or a positive multiple of 16.");
     }
     o.tl_splitting = sweeper->attr_bool("tl_splitting", false);
+    o.dump_fsr_flux = sweeper->attr_bool("dump_fsr_flux", false);
     if (sweeper->has_attr("incoming_update")) {
         std::string u = sanitize(sweeper->attr("incoming_update"));
         if (u == "off") o.incoming_update = 0;

@@ -40,6 +40,9 @@ struct SolverOptions {
     // 119): a transverse-leakage source that would go negative in an FSR is
     // moved into that FSR's Sigma_t instead (apply_transverse_leakage)
     bool tl_splitting = false;
+    // <sweeper dump_fsr_flux> (moc_sweeper.cpp:103): MoCSweeper::output also
+    // writes the FSR flux of every group
+    bool dump_fsr_flux = false;
 };
 
 // Flat problem description. Angles cover octants 1-4 (2-D); tracks are

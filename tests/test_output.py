@@ -47,6 +47,13 @@ def test_quadrature_and_group_bounds_match_oracle_tracer(ref_example, ref_xsl):
     assert len(b) == 7 and b[0] == 2.0e7 and b[-1] == 0.0635
 
 
+def test_dump_fsr_flux_option_is_read_from_the_sweeper_tag(ref_example, ref_xsl):
+    xml = ref_example["3x3"]
+    assert m.Problem(xml, ref_xsl).options["dump_fsr_flux"] == 0
+    tagged = xml.replace("<sweeper ", '<sweeper dump_fsr_flux="true" ', 1)
+    assert tagged != xml and m.Problem(tagged, ref_xsl).options["dump_fsr_flux"] == 1
+
+
 def test_npz_round_trip(tmp_path):
     d = {"convergence/k": np.array([1.0, 0.9]), "ng": np.array(7, dtype=np.int32),
          "flux/001": np.ones((1, 2, 3))}
