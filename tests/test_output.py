@@ -54,6 +54,66 @@ def test_dump_fsr_flux_option_is_read_from_the_sweeper_tag(ref_example, ref_xsl)
     assert tagged != xml and m.Problem(tagged, ref_xsl).options["dump_fsr_flux"] == 1
 
 
+class _FakeSweeper:
+    def __init__(self, G, ny, nx, n_fsr, rng):
+        self.n_group, self._ny, self._nx = G, ny, nx
+        self._pin = rng.uniform(0.1, 2.0, size=(ny * nx, G))
+        self._pin[0, :] = 0.0  # a pin without flux (counted out by Normalize)
+        self._fsr = rng.uniform(0.1, 2.0, size=(n_fsr, G))
+        self._pow = rng.uniform(0.5, 1.5, size=(ny, nx))
+
+    def get_pin_flux_1g(self, g):
+        return self._pin[:, g].copy()
+
+    def pin_powers(self):
+        return self._pow.copy()
+
+    def flux(self):
+        return self._fsr.copy()
+
+
+class _FakeProblem:
+    def __init__(self, ny, nx, n_fsr):
+        self.sizes = {"nx": nx, "ny": ny, "nfsr": n_fsr}
+        self.options = {"dump_fsr_flux": 0}
+
+    def group_bounds(self):
+        return np.array([2.0e7, 1.0e6, 0.625])
+
+    def quadrature(self):
+        return {"n_polar": 1, "n_azimuthal": 1, **{k: np.arange(8.0) for k in QUAD}}
+
+
+class _FakeSolver:
+    def __init__(self):
+        rng = np.random.default_rng(5)
+        self.sweeper, self.problem = _FakeSweeper(3, 2, 3, 10, rng), _FakeProblem(2, 3, 10)
+
+    def history(self):
+        return np.array([[1.1, 0.1, 0.2, 0.5], [1.05, 0.05, 0.01, 0.9]])
+
+
+def test_output_layout_and_normalize_on_a_fake_solver():
+    # the assembly of the datasets alone (no GPU): paths, shapes, MOCC's
+    # Normalize over the whole [pin][group] pin flux, fsr_flux only when asked
+    S = _FakeSolver()
+    d = out_mod.eigen_output(S)
+    assert not any(k.startswith("fsr_flux/") for k in d)
+    assert [k for k in d if k.startswith("flux/")] == ["flux/001", "flux/002", "flux/003"]
+    allf = np.concatenate([d[f"flux/{g:03d}"].ravel() for g in (1, 2, 3)])
+    assert d["flux/001"].shape == (1, 2, 3)
+    assert abs(allf.sum() - np.count_nonzero(allf > 0)) < 1e-12 * allf.size
+    ratio = d["flux/002"].reshape(-1)[1:] / S.sweeper._pin[1:, 1]
+    assert np.allclose(ratio, ratio[0])  # one common factor for all groups
+    assert np.array_equal(d["convergence/k"], [1.1, 1.05])
+    assert np.array_equal(d["convergence/iteration_time"], d["convergence/abscissae"])
+    assert d["pin_powers"].shape == (1, 2, 3) and int(d["ng"]) == 3
+    assert d["ang_quad/weight"].shape == (8,) and int(d["ang_quad/n_polar"]) == 1
+    d2 = out_mod.eigen_output(S, dump_fsr_flux=True)
+    assert d2["fsr_flux/002"].shape == (10, 1)
+    assert np.array_equal(d2["fsr_flux/002"][:, 0], S.sweeper._fsr[:, 1])
+
+
 def test_npz_round_trip(tmp_path):
     d = {"convergence/k": np.array([1.0, 0.9]), "ng": np.array(7, dtype=np.int32),
          "flux/001": np.ones((1, 2, 3))}
